@@ -1,0 +1,327 @@
+"""GB300-native dynamic single-source shortest paths (drop-in for the update path of
+ArindamK92/DynamicSSSPv2).
+
+The engine lives in the in-tree C ABI library ``_lib/libdsssp.so`` (include/dsssp.h); this
+module binds it with ctypes.  There is no CPU fallback: importing the package fails if the
+library has not been built (``python dynamicssspv2_gb300/_build.py``), and every engine call
+needs a CUDA device.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_lib" / "libdsssp.so"
+CLI_PATH = _PKG / "_lib" / "dsssp_main"
+
+if not LIB_PATH.exists():
+    raise ImportError(
+        f"{LIB_PATH} is missing: build it with `python dynamicssspv2_gb300/_build.py` "
+        "(the engine has no CPU fallback)"
+    )
+
+_lib = C.CDLL(str(LIB_PATH))
+
+OK = 0
+E_INVAL, E_OOM, E_BAD_VERTEX, E_CUDA, E_NO_CONVERGENCE, E_TIMEOUT = -1, -2, -3, -4, -5, -6
+E_BAD_TREE, E_OVERFLOW, E_IO, E_BAD_WEIGHT, E_NO_DEVICE, E_COOP = -7, -8, -9, -10, -11, -12
+UNREACHABLE = -1
+INS_UNIFORM, INS_RMAT, INS_LOCAL = 0, 1, 2
+
+CHANGE_DTYPE = np.dtype([("u", "<i4"), ("v", "<i4"), ("w", "<i4"), ("op", "<i4")])
+
+
+class DsssspError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        self.code = code
+        msg = _lib.dsssp_last_error().decode(errors="replace")
+        super().__init__(f"{what}: {_lib.dsssp_strerror(code).decode()} ({code}): {msg}")
+
+
+class Opts(C.Structure):
+    _fields_ = [
+        ("device", C.c_int32),
+        ("slack_pct", C.c_int32),
+        ("slack_min", C.c_int32),
+        ("small_deg", C.c_int32),
+        ("large_deg", C.c_int32),
+        ("chunk", C.c_int32),
+        ("bfs_levels", C.c_int32),
+        ("block", C.c_int32),
+        ("ctas_per_sm", C.c_int32),
+        ("timing", C.c_int32),
+        ("max_rounds", C.c_int64),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        (name, C.c_int64)
+        for name in (
+            "n_ins", "n_del", "n_ignored", "n_roots", "n_invalidated", "inv_levels", "pj_passes", "rounds",
+            "frontier_total", "edges_relaxed", "edges_inval", "del_probed", "updates", "overflow_entries", "repacks",
+        )
+    ] + [
+        (name, C.c_double)
+        for name in ("t_step1_ms", "t_inval_ms", "t_relax_ms", "t_update_ms", "t_total_ms", "bytes_alg",
+                     "bytes_alg_update")
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+_chgp = np.ctypeslib.ndpointer(dtype=CHANGE_DTYPE, flags="C_CONTIGUOUS")
+_P = C.c_void_p
+
+
+def _sig(name, restype, *argtypes):
+    f = getattr(_lib, name)
+    f.restype = restype
+    f.argtypes = list(argtypes)
+    return f
+
+
+_sig("dsssp_last_error", C.c_char_p)
+_sig("dsssp_strerror", C.c_char_p, C.c_int)
+_sig("dsssp_default_opts", None, C.POINTER(Opts))
+_sig("dsssp_graph_create", C.c_int, C.c_int32, C.c_int64, _i32p, _i32p, _i32p, C.POINTER(Opts), C.POINTER(_P))
+_sig("dsssp_graph_destroy", None, _P)
+_sig("dsssp_graph_info", C.c_int, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+     C.POINTER(C.c_int64), C.POINTER(C.c_int32))
+_sig("dsssp_tree_load", C.c_int, _P, _i32p, _i64p)
+_sig("dsssp_tree_compute", C.c_int, _P, C.c_int32, C.POINTER(Stats))
+_sig("dsssp_tree_read", C.c_int, _P, _P, _P)
+_sig("dsssp_apply_batch", C.c_int, _P, _P, C.c_int64, _P, C.POINTER(Stats))
+_sig("dsssp_apply_batch_async", C.c_int, _P, _P, C.c_int64, _P)
+_sig("dsssp_batch_finish", C.c_int, _P, C.POINTER(Stats))
+_sig("dsssp_graph_snapshot", C.c_int, _P)
+_sig("dsssp_graph_restore", C.c_int, _P, _P)
+_sig("dsssp_graph_compact", C.c_int, _P)
+_sig("dsssp_host_alloc", _P, C.c_size_t)
+_sig("dsssp_host_free", None, _P)
+_sig("dsssp_launch_count", C.c_int64)
+_sig("dsssp_free", None, _P)
+_sig("dsssp_read_graph_file", C.c_int, C.c_char_p, C.c_int32, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P),
+     C.POINTER(C.c_int64))
+_sig("dsssp_read_changes_file", C.c_int, C.c_char_p, C.c_int32, C.POINTER(_P), C.POINTER(C.c_int64))
+_sig("dsssp_read_sssp_file", C.c_int, C.c_char_p, C.c_int32, _i32p, _i64p, C.POINTER(C.c_int64))
+_sig("dsssp_write_sssp_file", C.c_int, C.c_char_p, C.c_int32, _i32p, _i64p)
+_sig("dsssp_gen_er", C.c_int, C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(_P),
+     C.POINTER(_P), C.POINTER(_P))
+_sig("dsssp_gen_rmat", C.c_int, C.c_int32, C.c_int64, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,
+     C.c_uint64, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P))
+_sig("dsssp_gen_grid", C.c_int, C.c_int32, C.c_int32, C.c_double, C.c_int64, C.c_int32, C.c_int32, C.c_uint64,
+     C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(C.c_int64))
+_sig("dsssp_gen_changes", C.c_int, C.c_int32, C.c_int64, _i32p, _i32p, _i32p, C.c_int64, C.c_int64, C.c_int32,
+     C.c_int32, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(_P))
+_sig("dsssp_max_degree_vertex", C.c_int32, C.c_int32, C.c_int64, _i32p, _i32p)
+
+EXPORTED = [
+    "dsssp_default_opts", "dsssp_graph_create", "dsssp_graph_destroy", "dsssp_graph_info", "dsssp_tree_load",
+    "dsssp_tree_compute", "dsssp_tree_read", "dsssp_apply_batch", "dsssp_apply_batch_async", "dsssp_batch_finish",
+    "dsssp_graph_snapshot", "dsssp_graph_restore", "dsssp_graph_compact", "dsssp_host_alloc", "dsssp_host_free",
+    "dsssp_launch_count", "dsssp_last_error", "dsssp_strerror", "dsssp_free", "dsssp_read_graph_file",
+    "dsssp_read_changes_file", "dsssp_read_sssp_file", "dsssp_write_sssp_file", "dsssp_gen_er", "dsssp_gen_rmat",
+    "dsssp_gen_grid", "dsssp_gen_changes", "dsssp_max_degree_vertex",
+]
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != OK:
+        raise DsssspError(rc, what)
+
+
+def _take_i32(p: C.c_void_p, n: int) -> np.ndarray:
+    if n == 0:
+        _lib.dsssp_free(p)
+        return np.zeros(0, np.int32)
+    arr = np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_int32)), shape=(n,)).copy()
+    _lib.dsssp_free(p)
+    return arr
+
+
+def _take_changes(p: C.c_void_p, n: int) -> np.ndarray:
+    if n == 0:
+        _lib.dsssp_free(p)
+        return np.zeros(0, CHANGE_DTYPE)
+    buf = (C.c_char * (16 * n)).from_address(p.value)
+    arr = np.frombuffer(bytes(buf), dtype=CHANGE_DTYPE).copy()
+    _lib.dsssp_free(p)
+    return arr
+
+
+def default_opts(**kw) -> Opts:
+    o = Opts()
+    _lib.dsssp_default_opts(C.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise TypeError(f"unknown option {k}")
+        setattr(o, k, v)
+    return o
+
+
+def make_changes(u, v, w, op) -> np.ndarray:
+    ch = np.zeros(len(u), CHANGE_DTYPE)
+    ch["u"], ch["v"], ch["w"], ch["op"] = u, v, w, op
+    return ch
+
+
+def launch_count() -> int:
+    return int(_lib.dsssp_launch_count())
+
+
+class Graph:
+    """Device-resident graph + shortest-path tree (one GPU)."""
+
+    def __init__(self, n: int, u, v, w, opts: Opts | None = None, **kw):
+        u = np.ascontiguousarray(u, np.int32)
+        v = np.ascontiguousarray(v, np.int32)
+        w = np.ascontiguousarray(w, np.int32)
+        if not (len(u) == len(v) == len(w)):
+            raise ValueError("edge arrays differ in length")
+        o = opts if opts is not None else default_opts(**kw)
+        h = _P()
+        _check(_lib.dsssp_graph_create(int(n), len(u), u, v, w, C.byref(o), C.byref(h)), "graph_create")
+        self._h = h
+        self.n = int(n)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.dsssp_graph_destroy(self._h)
+            self._h = _P()
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def info(self) -> dict:
+        n, e, c, b = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        s = C.c_int32()
+        _check(_lib.dsssp_graph_info(self._h, C.byref(n), C.byref(e), C.byref(c), C.byref(b), C.byref(s)), "info")
+        return {"n": n.value, "entries": e.value, "capacity": c.value, "device_bytes": b.value, "source": s.value}
+
+    def tree_load(self, parent, dist) -> None:
+        parent = np.ascontiguousarray(parent, np.int32)
+        dist = np.ascontiguousarray(dist, np.int64)
+        if len(parent) != self.n or len(dist) != self.n:
+            raise ValueError("tree arrays must have n entries")
+        _check(_lib.dsssp_tree_load(self._h, parent, dist), "tree_load")
+
+    def tree_compute(self, src: int) -> Stats:
+        st = Stats()
+        _check(_lib.dsssp_tree_compute(self._h, int(src), C.byref(st)), "tree_compute")
+        return st
+
+    def tree_read(self, parent: np.ndarray | None = None, dist: np.ndarray | None = None):
+        if parent is None:
+            parent = np.empty(self.n, np.int32)
+        if dist is None:
+            dist = np.empty(self.n, np.int64)
+        _check(_lib.dsssp_tree_read(self._h, parent.ctypes.data, dist.ctypes.data), "tree_read")
+        return parent, dist
+
+    def apply_batch(self, changes: np.ndarray, stream: int | None = None) -> Stats:
+        changes = np.ascontiguousarray(changes, CHANGE_DTYPE)
+        st = Stats()
+        _check(_lib.dsssp_apply_batch(self._h, changes.ctypes.data, len(changes), stream, C.byref(st)),
+               "apply_batch")
+        return st
+
+    def apply_batch_async(self, d_changes: int, k: int, stream: int | None = None) -> None:
+        _check(_lib.dsssp_apply_batch_async(self._h, d_changes, int(k), stream), "apply_batch_async")
+
+    def batch_finish(self) -> Stats:
+        st = Stats()
+        _check(_lib.dsssp_batch_finish(self._h, C.byref(st)), "batch_finish")
+        return st
+
+    def snapshot(self) -> None:
+        _check(_lib.dsssp_graph_snapshot(self._h), "snapshot")
+
+    def restore(self, stream: int | None = None) -> None:
+        _check(_lib.dsssp_graph_restore(self._h, stream), "restore")
+
+    def compact(self) -> None:
+        _check(_lib.dsssp_graph_compact(self._h), "compact")
+
+
+# ---- text formats ---------------------------------------------------------------------------
+
+def read_graph(path: str, n: int):
+    u, v, w, m = _P(), _P(), _P(), C.c_int64()
+    _check(_lib.dsssp_read_graph_file(str(path).encode(), int(n), C.byref(u), C.byref(v), C.byref(w), C.byref(m)),
+           "read_graph")
+    return _take_i32(u, m.value), _take_i32(v, m.value), _take_i32(w, m.value)
+
+
+def read_changes(path: str, n: int) -> np.ndarray:
+    p, k = _P(), C.c_int64()
+    _check(_lib.dsssp_read_changes_file(str(path).encode(), int(n), C.byref(p), C.byref(k)), "read_changes")
+    return _take_changes(p, k.value)
+
+
+def read_sssp(path: str, n: int):
+    parent = np.empty(n, np.int32)
+    dist = np.empty(n, np.int64)
+    lossy = C.c_int64()
+    _check(_lib.dsssp_read_sssp_file(str(path).encode(), int(n), parent, dist, C.byref(lossy)), "read_sssp")
+    return parent, dist, lossy.value
+
+
+def write_sssp(path: str, parent, dist) -> None:
+    parent = np.ascontiguousarray(parent, np.int32)
+    dist = np.ascontiguousarray(dist, np.int64)
+    _check(_lib.dsssp_write_sssp_file(str(path).encode(), len(parent), parent, dist), "write_sssp")
+
+
+# ---- generators -----------------------------------------------------------------------------
+
+def gen_er(n: int, m: int, wlo: int = 1, whi: int = 100, seed: int = 0):
+    u, v, w = _P(), _P(), _P()
+    _check(_lib.dsssp_gen_er(n, m, wlo, whi, seed, C.byref(u), C.byref(v), C.byref(w)), "gen_er")
+    return _take_i32(u, m), _take_i32(v, m), _take_i32(w, m)
+
+
+def gen_rmat(scale: int, m: int, a=0.57, b=0.19, c=0.19, wlo: int = 1, whi: int = 100, seed: int = 0):
+    u, v, w = _P(), _P(), _P()
+    _check(_lib.dsssp_gen_rmat(scale, m, a, b, c, wlo, whi, seed, C.byref(u), C.byref(v), C.byref(w)), "gen_rmat")
+    return _take_i32(u, m), _take_i32(v, m), _take_i32(w, m)
+
+
+def gen_grid(rows: int, cols: int, remove_frac: float, n_diag: int, wlo: int = 1, whi: int = 1000, seed: int = 0):
+    u, v, w, m = _P(), _P(), _P(), C.c_int64()
+    _check(_lib.dsssp_gen_grid(rows, cols, remove_frac, n_diag, wlo, whi, seed, C.byref(u), C.byref(v), C.byref(w),
+                               C.byref(m)), "gen_grid")
+    return _take_i32(u, m.value), _take_i32(v, m.value), _take_i32(w, m.value)
+
+
+def gen_changes(n: int, u, v, w, n_ins: int, n_del: int, kind: int = INS_UNIFORM, scale: int = 0,
+                p0: float = 0.0, p1: float = 0.0, p2: float = 0.0, wlo: int = 1, whi: int = 100,
+                seed: int = 0) -> np.ndarray:
+    u = np.ascontiguousarray(u, np.int32)
+    v = np.ascontiguousarray(v, np.int32)
+    w = np.ascontiguousarray(w, np.int32)
+    p = _P()
+    _check(_lib.dsssp_gen_changes(n, len(u), u, v, w, n_ins, n_del, kind, scale, p0, p1, p2, wlo, whi, seed,
+                                  C.byref(p)), "gen_changes")
+    return _take_changes(p, n_ins + n_del)
+
+
+def max_degree_vertex(n: int, u, v) -> int:
+    u = np.ascontiguousarray(u, np.int32)
+    v = np.ascontiguousarray(v, np.int32)
+    return int(_lib.dsssp_max_degree_vertex(n, len(u), u, v))

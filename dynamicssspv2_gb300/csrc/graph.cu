@@ -1,0 +1,1001 @@
+// graph.cu -- device graph store (CSR with per-row slack), tree load/read, batch
+// orchestration and the C ABI of include/dsssp.h.
+//
+// The graph store replaces the reference's host vector-of-vectors adjacency that is rebuilt
+// and re-copied for every batch (all_structure_undir.cuh:178-198, SSSPmainForUndirected.cu:
+// 42-91): rows live on the device, sorted by neighbour, each with free slots so insertions
+// append in place.  A row that runs out of slots triggers a repack (rows re-sorted, tombstones
+// dropped, slack restored) and the batch resumes after it.
+#include <atomic>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include <cub/device/device_scan.cuh>
+#include <cub/device/device_segmented_sort.cuh>
+#include <cuda_runtime.h>
+
+#include "../../include/dsssp.h"
+#include "engine.cuh"
+#include "host_common.h"
+
+namespace dsssp {
+
+cudaError_t launch_front(const UpdParams& p, int4* ovf, bool with_append, cudaStream_t s);
+cudaError_t launch_relocate(const UpdParams& p, cudaStream_t s);
+cudaError_t update_occupancy(int block, int* blocks_per_sm);
+cudaError_t launch_update(const UpdParams& p, int grid, int block, cudaStream_t s);
+
+static std::atomic<long long> g_launches{0};
+void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned blocks_for(long long n) { return (unsigned)((n + kThreads - 1) / kThreads); }
+
+// ---- build / repack kernels ------------------------------------------------------------
+
+__global__ void k_check_edges(const int* u, const int* v, const int* w, long long m, int n, Ctl* ctl) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    if (u[i] < 0 || u[i] >= n || v[i] < 0 || v[i] >= n) set_status(ctl, DSSSP_E_BAD_VERTEX);
+    else if (w[i] < 0) set_status(ctl, DSSSP_E_BAD_WEIGHT);
+}
+
+__global__ void k_degree(const int* u, const int* v, long long m, int* deg) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    atomicAdd(&deg[u[i]], 1);
+    atomicAdd(&deg[v[i]], 1);
+}
+
+// cap = deg + max(slack_min, deg * slack_pct / 100)
+__global__ void k_caps(const long long* deg, int n, int slack_pct, int slack_min, long long* cap) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const long long d = deg[v];
+    long long s = d * slack_pct / 100;
+    if (s < slack_min) s = slack_min;
+    cap[v] = d + s;
+}
+
+__device__ __forceinline__ unsigned long long make_key(int col, int wt) {
+    return ((unsigned long long)(unsigned)col << 32) | (unsigned)wt;
+}
+
+__global__ void k_scatter_packed(const int* u, const int* v, const int* w, long long m, const long long* poff,
+                                 int* cursor, unsigned long long* keys) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const int a = u[i], b = v[i];
+    keys[poff[a] + atomicAdd(&cursor[a], 1)] = make_key(b, w[i]);
+    keys[poff[b] + atomicAdd(&cursor[b], 1)] = make_key(a, w[i]);
+}
+
+// Packed (contiguous) sorted rows -> slack layout.  Thread per entry; row by binary search.
+__global__ void k_spread(const unsigned long long* keys, const long long* poff, const long long* start, int n,
+                         long long total, int2* adj) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= total) return;
+    int lo = 0, hi = n;  // last r with poff[r] <= e
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (poff[mid] <= e) lo = mid;
+        else hi = mid;
+    }
+    const unsigned long long k = keys[e];
+    adj[start[lo] + (e - poff[lo])] = make_int2((int)(k >> 32), (int)(unsigned)k);
+}
+
+__global__ void k_rows_init(const long long* start, const long long* deg, const long long* cap, int n,
+                            RowDesc* rows, int* sorted_len) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    RowDesc r;
+    r.start = start[v];
+    r.deg = (int)deg[v];
+    r.cap = (int)cap[v];
+    rows[v] = r;
+    sorted_len[v] = (int)deg[v];
+}
+
+// live entries of each row (warp per row); an overflowed row holds cap entries
+__global__ void k_count_live(const RowDesc* rows, const int2* adj, int n, int* live) {
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    if (gw >= n) return;
+    const RowDesc r = rows[gw];
+    const int len = r.deg < r.cap ? r.deg : r.cap;
+    int c = 0;
+    for (int j = (int)lane; j < len; j += 32) c += adj[r.start + j].y >= 0;
+    c = __reduce_add_sync(0xFFFFFFFFu, (unsigned)c);
+    if (lane == 0) live[gw] = c;
+}
+
+__global__ void k_ovf_count(const int4* ovf, int novf, int* live) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < novf) atomicAdd(&live[ovf[i].x], 1);
+}
+
+__global__ void k_pack_live(const RowDesc* rows, const int2* adj, int n, const long long* poff, int* cursor,
+                            unsigned long long* keys) {
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    if (gw >= n) return;
+    const RowDesc r = rows[gw];
+    const int len = r.deg < r.cap ? r.deg : r.cap;
+    int out = 0;
+    for (int b = 0; b < len; b += 32) {
+        const int j = b + (int)lane;
+        int2 e = make_int2(0, -1);
+        if (j < len) e = adj[r.start + j];
+        const bool keep = e.y >= 0;
+        const unsigned mask = __ballot_sync(0xFFFFFFFFu, keep);
+        if (keep) keys[poff[gw] + out + __popc(mask & ((1u << lane) - 1u))] = make_key(e.x, e.y);
+        out += __popc(mask);
+    }
+    if (lane == 0) cursor[gw] = out;
+}
+
+__global__ void k_pack_ovf(const int4* ovf, int novf, const long long* poff, int* cursor, unsigned long long* keys) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= novf) return;
+    const int4 o = ovf[i];
+    keys[poff[o.x] + atomicAdd(&cursor[o.x], 1)] = make_key(o.y, o.z);
+}
+
+__global__ void k_int_to_ll(const int* a, int n, long long* b) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < n) b[v] = a[v];
+}
+
+// ---- tree kernels --------------------------------------------------------------------------
+
+// parent -1 -> unreachable; otherwise parent in range and 0 <= dist < 2^32-1; the root is the
+// single vertex with parent[v] == v and it must have dist 0.
+__global__ void k_tree_pack(const int* parent, const long long* dist, int n, unsigned long long* state, Ctl* ctl) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const int p = parent[v];
+    if (p == -1) {
+        state[v] = kInfState;
+        return;
+    }
+    if (p < 0 || p >= n) {
+        set_status(ctl, DSSSP_E_BAD_TREE);
+        state[v] = kInfState;
+        return;
+    }
+    const long long d = dist[v];
+    if (d < 0 || d >= (long long)kDistInf) {
+        set_status(ctl, d < 0 ? DSSSP_E_BAD_TREE : DSSSP_E_OVERFLOW);
+        state[v] = kInfState;
+        return;
+    }
+    if (p == v) {
+        atomicAdd(&ctl->stat[0], 1ull);             // number of roots
+        atomicMin(&ctl->stat[1], (unsigned long long)v);  // root id
+        if (d != 0) set_status(ctl, DSSSP_E_BAD_TREE);
+    }
+    state[v] = ((unsigned long long)d << 32) | (unsigned)p;
+}
+
+__global__ void k_tree_unpack(const unsigned long long* state, int n, int* parent, long long* dist) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const unsigned long long s = state[v];
+    if (s == kInfState) {
+        if (parent) parent[v] = -1;
+        if (dist) dist[v] = DSSSP_UNREACHABLE;
+    } else {
+        if (parent) parent[v] = (int)(unsigned)s;
+        if (dist) dist[v] = (long long)(s >> 32);
+    }
+}
+
+__global__ void k_state_reset(unsigned long long* state, int n, int src) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < n) state[v] = v == src ? (unsigned long long)(unsigned)src : kInfState;
+}
+
+// ---- host helpers --------------------------------------------------------------------------
+
+int cuda_fail(cudaError_t e, const char* what) {
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return fail(DSSSP_E_OOM, "%s: out of device memory", what);
+    }
+    return fail(DSSSP_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                   \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+template <class T>
+int dalloc(T** p, size_t count, const char* what) {
+    *p = nullptr;
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return cuda_fail(e, what);
+    }
+    return DSSSP_OK;
+}
+
+template <class T>
+void dfree(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+}  // namespace
+}  // namespace dsssp
+
+using namespace dsssp;
+
+struct dsssp_graph {
+    int dev = 0;
+    int n = 0;
+    int src = -1;
+    int num_sms = 0;
+    dsssp_opts o{};
+    cudaStream_t stream = nullptr;
+    long long cap_total = 0;
+    long long entries = 0;
+    DevGraph dg{};
+    // batch buffers
+    int4* d_chg = nullptr;
+    long long chg_cap = 0;
+    long long* d_slot = nullptr;
+    int4* d_ovf = nullptr;
+    Ctl* h_ctl = nullptr;  // pinned mirror of the control block
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    unsigned epoch = 0;
+    int coop_grid = 0;
+    // pending batch
+    bool pending = false;
+    long long pend_k = 0;
+    const int4* pend_chg = nullptr;
+    cudaStream_t pend_stream = nullptr;
+    bool pend_events = false;
+    // tree staging
+    int* d_par = nullptr;
+    long long* d_dist = nullptr;
+    // snapshot
+    unsigned long long* s_state = nullptr;
+    RowDesc* s_rows = nullptr;
+    int* s_sorted = nullptr;
+    int2* s_adj = nullptr;
+    long long s_cap = 0;
+    long long s_entries = 0;
+    int s_src = -1;
+    bool has_snap = false;
+};
+
+namespace dsssp {
+namespace {
+
+int set_device(const dsssp_graph* g) {
+    cudaError_t e = cudaSetDevice(g->dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    return DSSSP_OK;
+}
+
+// Heavy-list capacity: (vertex, chunk) items of distinct heavy rows of one step.
+long long heavy_capacity(long long cap_total, const dsssp_opts& o) {
+    long long unit = o.chunk < o.large_deg ? o.chunk : o.large_deg;
+    if (unit < 1) unit = 1;
+    return 2 * (cap_total / unit) + 64;
+}
+
+int ensure_heavy(dsssp_graph* g) {
+    const long long need = heavy_capacity(g->cap_total, g->o);
+    if (g->dg.hcap >= need && g->dg.h0) return DSSSP_OK;
+    dfree(g->dg.h0);
+    dfree(g->dg.h1);
+    int rc = dalloc(&g->dg.h0, (size_t)need, "heavy list");
+    if (!rc) rc = dalloc(&g->dg.h1, (size_t)need, "heavy list");
+    g->dg.hcap = rc ? 0 : need;
+    return rc;
+}
+
+int ensure_batch(dsssp_graph* g, long long k) {
+    if (k <= g->chg_cap) return DSSSP_OK;
+    long long cap = k + k / 4 + 1024;
+    dfree(g->d_chg);
+    dfree(g->d_slot);
+    dfree(g->d_ovf);
+    g->chg_cap = 0;
+    int rc = dalloc(&g->d_chg, (size_t)cap, "change buffer");
+    if (!rc) rc = dalloc(&g->d_slot, (size_t)cap * 2, "slot buffer");
+    if (!rc) rc = dalloc(&g->d_ovf, (size_t)cap * 2, "overflow buffer");
+    if (!rc) g->chg_cap = cap;
+    return rc;
+}
+
+// deg (int, n) -> deg64 (n+1, last 0) and poff = exclusive scan (n+1, last = total)
+int row_offsets(dsssp_graph* g, const int* d_deg, long long** deg64, long long** poff, cudaStream_t s) {
+    const int n = g->n;
+    *deg64 = nullptr;
+    *poff = nullptr;
+    int rc = dalloc(deg64, (size_t)n + 1, "row degrees");
+    if (!rc) rc = dalloc(poff, (size_t)n + 1, "row offsets");
+    if (rc) return rc;
+    CK(cudaMemsetAsync(*deg64 + n, 0, sizeof(long long), s), "memset");
+    if (n > 0) {
+        k_int_to_ll<<<blocks_for(n), kThreads, 0, s>>>(d_deg, n, *deg64);
+        count_launch(1);
+    }
+    size_t tb = 0;
+    CK(cub::DeviceScan::ExclusiveSum(nullptr, tb, *deg64, *poff, n + 1, s), "scan");
+    void* tmp = nullptr;
+    CK(cudaMalloc(&tmp, tb ? tb : 1), "scan scratch");
+    cudaError_t e = cub::DeviceScan::ExclusiveSum(tmp, tb, *deg64, *poff, n + 1, s);
+    cudaFree(tmp);
+    CK(e, "scan");
+    return DSSSP_OK;
+}
+
+// Packed rows (keys at poff, row v holding deg64[v] keys) -> sorted rows in a fresh
+// slack-layout adjacency; replaces g's adjacency, rows and sorted prefix lengths.
+int layout_rows(dsssp_graph* g, unsigned long long* keys_in, long long total, const long long* deg64,
+                const long long* poff, cudaStream_t s) {
+    const int n = g->n;
+    long long *cap = nullptr, *start = nullptr;
+    unsigned long long* keys_out = nullptr;
+    void* tmp = nullptr;
+    int2* adj = nullptr;
+    long long cap_total = 0;
+    int rc = dalloc(&cap, (size_t)n + 1, "row caps");
+    if (!rc) rc = dalloc(&start, (size_t)n + 1, "row starts");
+    if (!rc) rc = dalloc(&keys_out, (size_t)total, "sort buffer");
+    if (!rc) {
+        cudaError_t e = cudaMemsetAsync(cap + n, 0, sizeof(long long), s);
+        if (n > 0 && e == cudaSuccess) {
+            k_caps<<<blocks_for(n), kThreads, 0, s>>>(deg64, n, g->o.slack_pct, g->o.slack_min, cap);
+            count_launch(1);
+        }
+        size_t tb1 = 0, tb2 = 0;
+        if (e == cudaSuccess) e = cub::DeviceScan::ExclusiveSum(nullptr, tb1, cap, start, n + 1, s);
+        if (e == cudaSuccess)
+            e = cub::DeviceSegmentedSort::SortKeys(nullptr, tb2, (const unsigned long long*)keys_in, keys_out, total,
+                                                   n, poff, poff + 1, s);
+        const size_t tb = tb1 > tb2 ? tb1 : tb2;
+        if (e == cudaSuccess) e = cudaMalloc(&tmp, tb ? tb : 1);
+        if (e == cudaSuccess) e = cub::DeviceScan::ExclusiveSum(tmp, tb1, cap, start, n + 1, s);
+        if (e == cudaSuccess && total > 0)
+            e = cub::DeviceSegmentedSort::SortKeys(tmp, tb2, (const unsigned long long*)keys_in, keys_out, total, n,
+                                                   poff, poff + 1, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&cap_total, start + n, sizeof(long long), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = cuda_fail(e, "row layout");
+    }
+    if (!rc) rc = dalloc(&adj, (size_t)cap_total, "adjacency");
+    if (!rc) {
+        if (total > 0) {
+            k_spread<<<blocks_for(total), kThreads, 0, s>>>(keys_out, poff, start, n, total, adj);
+            count_launch(1);
+        }
+        if (n > 0) {
+            k_rows_init<<<blocks_for(n), kThreads, 0, s>>>(start, deg64, cap, n, g->dg.rows, g->dg.sorted_len);
+            count_launch(1);
+        }
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = cuda_fail(e, "row layout");
+    }
+    if (!rc) {
+        dfree(g->dg.adj);
+        g->dg.adj = adj;
+        adj = nullptr;
+        g->cap_total = cap_total;
+        g->entries = total;
+        rc = ensure_heavy(g);
+    }
+    dfree(cap);
+    dfree(start);
+    dfree(keys_out);
+    if (tmp) cudaFree(tmp);
+    dfree(adj);
+    return rc;
+}
+
+// Drops tombstones, folds n_ovf overflow entries (row, col, wt) in, re-sorts every row and
+// restores slack.
+int repack(dsssp_graph* g, const int4* d_ovf, int n_ovf, cudaStream_t s) {
+    const int n = g->n;
+    int *live = nullptr, *cursor = nullptr;
+    long long *deg64 = nullptr, *poff = nullptr;
+    unsigned long long* keys = nullptr;
+    long long total = 0;
+    int rc = dalloc(&live, (size_t)n, "live counts");
+    if (!rc) rc = dalloc(&cursor, (size_t)n, "row cursors");
+    if (!rc && n > 0) {
+        const unsigned wb = (unsigned)(((long long)n * 32 + kThreads - 1) / kThreads);
+        k_count_live<<<wb, kThreads, 0, s>>>(g->dg.rows, g->dg.adj, n, live);
+        count_launch(1);
+        if (n_ovf > 0) {
+            k_ovf_count<<<blocks_for(n_ovf), kThreads, 0, s>>>(d_ovf, n_ovf, live);
+            count_launch(1);
+        }
+    }
+    if (!rc) rc = row_offsets(g, live, &deg64, &poff, s);
+    if (!rc) {
+        cudaError_t e = cudaMemcpyAsync(&total, poff + n, sizeof(long long), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = cuda_fail(e, "repack");
+    }
+    if (!rc) rc = dalloc(&keys, (size_t)total, "repack keys");
+    if (!rc && n > 0) {
+        const unsigned wb = (unsigned)(((long long)n * 32 + kThreads - 1) / kThreads);
+        k_pack_live<<<wb, kThreads, 0, s>>>(g->dg.rows, g->dg.adj, n, poff, cursor, keys);
+        count_launch(1);
+        if (n_ovf > 0) {
+            k_pack_ovf<<<blocks_for(n_ovf), kThreads, 0, s>>>(d_ovf, n_ovf, poff, cursor, keys);
+            count_launch(1);
+        }
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = cuda_fail(e, "repack");
+    }
+    if (!rc) rc = layout_rows(g, keys, total, deg64, poff, s);
+    dfree(live);
+    dfree(cursor);
+    dfree(deg64);
+    dfree(poff);
+    dfree(keys);
+    return rc;
+}
+
+UpdParams make_params(const dsssp_graph* g, const int4* chg, long long k, int mode) {
+    UpdParams p;
+    p.g = g->dg;
+    p.g.n = g->n;
+    p.g.src = g->src;
+    p.chg = chg;
+    p.k = k;
+    p.slot = g->d_slot;
+    p.epoch = g->epoch;
+    p.small_deg = g->o.small_deg;
+    p.large_deg = g->o.large_deg;
+    p.chunk = g->o.chunk;
+    p.bfs_levels = g->o.bfs_levels;
+    p.mode = mode;
+    p.max_rounds = g->o.max_rounds > 0 ? g->o.max_rounds : 2LL * g->n + 16;
+    return p;
+}
+
+int clear_ctl(dsssp_graph* g, cudaStream_t s) {
+    const size_t off = offsetof(Ctl, status);
+    CK(cudaMemsetAsync((char*)g->dg.ctl + off, 0, sizeof(Ctl) - off, s), "control block reset");
+    return DSSSP_OK;
+}
+
+int next_epoch(dsssp_graph* g, cudaStream_t s) {
+    if (g->epoch >= 0xFFFFFFF0u) {
+        CK(cudaMemsetAsync(g->dg.inv_tag, 0, sizeof(unsigned) * (size_t)g->n, s), "tag reset");
+        g->epoch = 0;
+    }
+    g->epoch++;
+    return DSSSP_OK;
+}
+
+// After a failed batch the device may not have advanced its round base: clear the frontier
+// tags and restart the tag sequence so no stale tag can suppress a later push.
+void reset_tags(dsssp_graph* g, cudaStream_t s) {
+    cudaMemsetAsync(g->dg.push_tag, 0, sizeof(unsigned) * (size_t)g->n, s);
+    const unsigned one = 1;
+    cudaMemcpyAsync(&g->dg.ctl->round_base, &one, sizeof(one), cudaMemcpyHostToDevice, s);
+    cudaStreamSynchronize(s);
+}
+
+int status_code(int st) {
+    switch (st) {
+        case 0: return DSSSP_OK;
+        case DSSSP_E_BAD_VERTEX: return fail(st, "change batch names a vertex outside 0..n-1");
+        case DSSSP_E_BAD_WEIGHT: return fail(st, "change batch inserts an edge with a negative weight");
+        case DSSSP_E_NO_CONVERGENCE: return fail(st, "relaxation did not converge within the round cap");
+        case DSSSP_E_TIMEOUT: return fail(st, "a device-side grid barrier timed out");  // detail set by caller
+        case DSSSP_E_BAD_TREE: return fail(st, "the shortest-path tree has a parent cycle");
+        case DSSSP_E_OVERFLOW: return fail(st, "a distance does not fit below 2^32-1");
+        default: return fail(DSSSP_E_CUDA, "device status %d", st);
+    }
+}
+
+void fill_stats(const dsssp_graph* g, const Ctl& c, dsssp_stats* st, bool events, long long k, int repacks) {
+    if (!st) return;
+    memset(st, 0, sizeof(*st));
+    st->n_ins = (int64_t)c.stat[ST_INS];
+    st->n_del = (int64_t)c.stat[ST_DEL];
+    st->n_ignored = (int64_t)c.stat[ST_IGN];
+    st->n_roots = (int64_t)c.stat[ST_ROOTS];
+    st->n_invalidated = (int64_t)c.stat[ST_INV];
+    st->inv_levels = (int64_t)c.stat[ST_LEVELS];
+    st->pj_passes = (int64_t)c.stat[ST_PJ];
+    st->rounds = (int64_t)c.stat[ST_ROUNDS];
+    st->frontier_total = (int64_t)c.stat[ST_FRONTIER];
+    st->edges_relaxed = (int64_t)c.stat[ST_EDGES_RELAX];
+    st->edges_inval = (int64_t)c.stat[ST_EDGES_INV];
+    st->del_probed = (int64_t)c.stat[ST_DEL_PROBED];
+    st->updates = (int64_t)c.stat[ST_UPDATES];
+    st->overflow_entries = (int64_t)c.stat[ST_OVF];
+    st->repacks = repacks;
+    if (c.ts[1] > c.ts[0]) st->t_inval_ms = (double)(c.ts[1] - c.ts[0]) * 1e-6;
+    if (c.ts[3] > c.ts[2]) st->t_relax_ms = (double)(c.ts[3] - c.ts[2]) * 1e-6;
+    if (c.ts[2] > c.ts[1] && c.ts[1] > 0) st->t_relax_ms += (double)(c.ts[2] - c.ts[1]) * 1e-6;
+    if (events) {
+        float a = 0, b = 0, t = 0;
+        if (cudaEventElapsedTime(&a, g->ev[0], g->ev[1]) == cudaSuccess) st->t_step1_ms = a;
+        if (cudaEventElapsedTime(&b, g->ev[1], g->ev[2]) == cudaSuccess) st->t_update_ms = b;
+        if (cudaEventElapsedTime(&t, g->ev[0], g->ev[2]) == cudaSuccess) st->t_total_ms = t;
+    }
+    // algorithmic bytes (byte model: each item is touched once by this algorithm)
+    const double n = (double)g->n;
+    double upd = 16.0 * (double)st->edges_relaxed + 16.0 * (double)st->edges_inval +
+                 28.0 * (double)st->frontier_total + 44.0 * (double)st->n_invalidated +
+                 16.0 * (double)st->updates + 24.0 * (double)st->n_ins;
+    if (st->pj_passes > 0) upd += n * (12.0 + 12.0 * (double)st->pj_passes);
+    const double front = 16.0 * (double)k + 48.0 * (double)st->n_ins + 56.0 * (double)st->n_del +
+                         8.0 * (double)st->del_probed + 16.0 * (double)st->n_roots;
+    st->bytes_alg_update = upd;
+    st->bytes_alg = upd + front;
+}
+
+// Enqueues one batch (records already on the device).  with_append = false resumes after a
+// repack (insertions were already placed).
+int enqueue_batch(dsssp_graph* g, const int4* d_chg, long long k, cudaStream_t s, bool with_append) {
+    int rc = clear_ctl(g, s);
+    if (rc) return rc;
+    UpdParams p = make_params(g, d_chg, k, 0);
+    const bool ev = g->o.timing != 0;
+    if (ev) CK(cudaEventRecord(g->ev[0], s), "event");
+    CK(launch_front(p, g->d_ovf, with_append, s), "insert/delete kernels");
+    if (ev) CK(cudaEventRecord(g->ev[1], s), "event");
+    CK(launch_update(p, g->coop_grid, g->o.block, s), "update kernel");
+    if (ev) CK(cudaEventRecord(g->ev[2], s), "event");
+    CK(cudaMemcpyAsync(g->h_ctl, g->dg.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s), "status read");
+    return DSSSP_OK;
+}
+
+int finish_batch(dsssp_graph* g, dsssp_stats* st) {
+    if (!g->pending) {
+        if (st) memset(st, 0, sizeof(*st));
+        return DSSSP_OK;
+    }
+    g->pending = false;
+    cudaStream_t s = g->pend_stream;
+    CK(cudaStreamSynchronize(s), "batch");
+    int repacks = 0;
+    if (g->h_ctl->status == kStatusOverflowPending) {
+        const Ctl first = *g->h_ctl;
+        int rc = repack(g, g->d_ovf, g->h_ctl->ovf_count, s);
+        if (rc) return rc;
+        repacks = 1;
+        UpdParams p = make_params(g, g->pend_chg, g->pend_k, 0);
+        CK(launch_relocate(p, s), "relocate");
+        rc = enqueue_batch(g, g->pend_chg, g->pend_k, s, false);
+        if (rc) return rc;
+        CK(cudaStreamSynchronize(s), "batch");
+        for (int i : {ST_INS, ST_DEL, ST_IGN, ST_OVF}) g->h_ctl->stat[i] = first.stat[i];
+    }
+    fill_stats(g, *g->h_ctl, st, g->pend_events, g->pend_k, repacks);
+    if (g->h_ctl->status != 0) reset_tags(g, s);
+    if (g->h_ctl->stat[ST_DIST_OVF] > 0 && g->h_ctl->status == 0) return status_code(DSSSP_E_OVERFLOW);
+    if (g->h_ctl->status == DSSSP_E_TIMEOUT) {
+        const unsigned* d = g->h_ctl->diag;
+        return fail(DSSSP_E_TIMEOUT,
+                    "grid barrier #%u timed out with %u of %d CTAs arrived; %u CTAs timed out; "
+                    "CTA barrier counts at exit: min %u max %u",
+                    d[0], d[1], g->coop_grid, d[2], 0xFFFFFFFFu - d[4], d[3]);
+    }
+    return status_code(g->h_ctl->status);
+}
+
+}  // namespace
+}  // namespace dsssp
+
+// =========================================================================================
+// C ABI
+// =========================================================================================
+
+extern "C" {
+
+void dsssp_default_opts(dsssp_opts* o) {
+    if (!o) return;
+    o->device = 0;
+    o->slack_pct = 25;
+    o->slack_min = 4;
+    o->small_deg = 8;
+    o->large_deg = 1024;
+    o->chunk = 1024;
+    o->bfs_levels = 48;
+    o->block = 256;
+    o->ctas_per_sm = 0;
+    o->timing = 1;
+    o->max_rounds = 0;
+}
+
+const char* dsssp_strerror(int code) {
+    switch (code) {
+        case DSSSP_OK: return "ok";
+        case DSSSP_E_INVAL: return "invalid argument";
+        case DSSSP_E_OOM: return "out of memory";
+        case DSSSP_E_BAD_VERTEX: return "vertex id out of range";
+        case DSSSP_E_CUDA: return "CUDA error";
+        case DSSSP_E_NO_CONVERGENCE: return "no convergence within the round cap";
+        case DSSSP_E_TIMEOUT: return "device-side wait timed out";
+        case DSSSP_E_BAD_TREE: return "invalid shortest-path tree";
+        case DSSSP_E_OVERFLOW: return "distance overflow";
+        case DSSSP_E_IO: return "file I/O error";
+        case DSSSP_E_BAD_WEIGHT: return "negative edge weight";
+        case DSSSP_E_NO_DEVICE: return "no CUDA device";
+        case DSSSP_E_COOP: return "persistent kernel cannot be co-resident";
+        default: return "unknown error";
+    }
+}
+
+int64_t dsssp_launch_count(void) { return (int64_t)g_launches.load(); }
+
+void* dsssp_host_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaMallocHost(&p, bytes ? bytes : 1) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+void dsssp_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+void dsssp_graph_destroy(dsssp_graph* g) {
+    if (!g) return;
+    cudaSetDevice(g->dev);
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    DevGraph& d = g->dg;
+    dfree(d.state); dfree(d.rows); dfree(d.sorted_len); dfree(d.adj); dfree(d.inv_tag);
+    dfree(d.push_tag); dfree(d.jm); dfree(d.invq); dfree(d.q0); dfree(d.q1); dfree(d.h0); dfree(d.h1);
+    dfree(d.ctl);
+    dfree(g->d_chg); dfree(g->d_slot); dfree(g->d_ovf); dfree(g->d_par); dfree(g->d_dist);
+    dfree(g->s_state); dfree(g->s_rows); dfree(g->s_sorted); dfree(g->s_adj);
+    if (g->h_ctl) cudaFreeHost(g->h_ctl);
+    for (auto& e : g->ev)
+        if (e) cudaEventDestroy(e);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+}
+
+static int check_opts(const dsssp_opts& o) {
+    if (o.slack_pct < 0 || o.slack_min < 0 || o.small_deg < 0 || o.large_deg < o.small_deg || o.chunk < 32 ||
+        o.bfs_levels < 0 || o.block < 32 || o.block > 256 || o.block % 32 || o.ctas_per_sm < 0 || o.max_rounds < 0)
+        return fail(DSSSP_E_INVAL, "invalid dsssp_opts");
+    return DSSSP_OK;
+}
+
+int dsssp_graph_create(int32_t n, int64_t m, const int32_t* u, const int32_t* v, const int32_t* w,
+                       const dsssp_opts* opts, dsssp_graph** out) {
+    if (!out) return fail(DSSSP_E_INVAL, "graph_create: out is NULL");
+    *out = nullptr;
+    if (n <= 0 || n >= 0x7FFFFFF0 || m < 0 || (m > 0 && (!u || !v || !w)))
+        return fail(DSSSP_E_INVAL, "graph_create: bad sizes or NULL edge arrays");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(DSSSP_E_NO_DEVICE, "no CUDA device is available");
+    }
+    dsssp_graph* g = new dsssp_graph();
+    if (opts) g->o = *opts;
+    else dsssp_default_opts(&g->o);
+    int rc = check_opts(g->o);
+    if (rc) { delete g; return rc; }
+    if (g->o.device < 0 || g->o.device >= ndev) { delete g; return fail(DSSSP_E_INVAL, "device %d does not exist", g->o.device); }
+    g->dev = g->o.device;
+    g->n = n;
+    rc = set_device(g);
+    if (rc) { delete g; return rc; }
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, g->dev);
+    cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, g->dev);
+    if (!coop) { delete g; return fail(DSSSP_E_COOP, "device does not support cooperative launch"); }
+    int per_sm = 0;
+    if (update_occupancy(g->o.block, &per_sm) != cudaSuccess || per_sm < 1) {
+        delete g;
+        return fail(DSSSP_E_COOP, "update kernel has no occupancy at block %d", g->o.block);
+    }
+    if (g->o.ctas_per_sm > 0 && g->o.ctas_per_sm < per_sm) per_sm = g->o.ctas_per_sm;
+    g->coop_grid = per_sm * g->num_sms;
+    cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { dsssp_graph_destroy(g); return cuda_fail(e, "stream"); }
+    for (auto& ev : g->ev)
+        if ((e = cudaEventCreate(&ev)) != cudaSuccess) { dsssp_graph_destroy(g); return cuda_fail(e, "event"); }
+    if (cudaMallocHost((void**)&g->h_ctl, sizeof(Ctl)) != cudaSuccess) {
+        dsssp_graph_destroy(g);
+        return fail(DSSSP_E_OOM, "pinned control block");
+    }
+    memset(g->h_ctl, 0, sizeof(Ctl));
+    DevGraph& d = g->dg;
+    const size_t N = (size_t)n;
+    rc = dalloc(&d.state, N, "state");
+    if (!rc) rc = dalloc(&d.rows, N, "rows");
+    if (!rc) rc = dalloc(&d.sorted_len, N, "sorted_len");
+    if (!rc) rc = dalloc(&d.inv_tag, N, "inv_tag");
+    if (!rc) rc = dalloc(&d.push_tag, N, "push_tag");
+    if (!rc) rc = dalloc(&d.jm, N, "jm");
+    if (!rc) rc = dalloc(&d.invq, N, "invq");
+    if (!rc) rc = dalloc(&d.q0, N, "frontier");
+    if (!rc) rc = dalloc(&d.q1, N, "frontier");
+    if (!rc) rc = dalloc(&d.ctl, 1, "control block");
+    if (rc) { dsssp_graph_destroy(g); return rc; }
+    cudaStream_t s = g->stream;
+    cudaMemsetAsync(d.state, 0xFF, sizeof(unsigned long long) * N, s);
+    cudaMemsetAsync(d.inv_tag, 0, sizeof(unsigned) * N, s);
+    cudaMemsetAsync(d.push_tag, 0, sizeof(unsigned) * N, s);
+    cudaMemsetAsync(d.ctl, 0, sizeof(Ctl), s);
+    Ctl init{};
+    init.round_base = 1;
+    cudaMemcpyAsync(d.ctl, &init, sizeof(Ctl), cudaMemcpyHostToDevice, s);
+
+    // edges -> packed rows -> sorted slack layout
+    int *du = nullptr, *dv = nullptr, *dw = nullptr, *deg = nullptr, *cursor = nullptr;
+    long long *deg64 = nullptr, *poff = nullptr;
+    unsigned long long* keys = nullptr;
+    rc = dalloc(&du, (size_t)m, "edge upload");
+    if (!rc) rc = dalloc(&dv, (size_t)m, "edge upload");
+    if (!rc) rc = dalloc(&dw, (size_t)m, "edge upload");
+    if (!rc) rc = dalloc(&deg, N, "degrees");
+    if (!rc) rc = dalloc(&cursor, N, "cursors");
+    if (!rc && m > 0) {
+        e = cudaMemcpyAsync(du, u, sizeof(int) * (size_t)m, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dv, v, sizeof(int) * (size_t)m, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dw, w, sizeof(int) * (size_t)m, cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) rc = cuda_fail(e, "edge upload");
+    }
+    if (!rc) {
+        cudaMemsetAsync(deg, 0, sizeof(int) * N, s);
+        cudaMemsetAsync(cursor, 0, sizeof(int) * N, s);
+        if (m > 0) {
+            k_check_edges<<<blocks_for(m), kThreads, 0, s>>>(du, dv, dw, m, n, d.ctl);
+            count_launch(1);
+        }
+        e = cudaMemcpyAsync(g->h_ctl, d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = cuda_fail(e, "edge check");
+        else if (g->h_ctl->status != 0)
+            rc = fail(g->h_ctl->status, g->h_ctl->status == DSSSP_E_BAD_WEIGHT ? "graph has a negative edge weight"
+                                                                               : "graph names a vertex outside 0..n-1");
+    }
+    if (!rc && m > 0) {
+        k_degree<<<blocks_for(m), kThreads, 0, s>>>(du, dv, m, deg);
+        count_launch(1);
+    }
+    if (!rc) rc = row_offsets(g, deg, &deg64, &poff, s);
+    if (!rc) rc = dalloc(&keys, (size_t)(2 * m), "build keys");
+    if (!rc && m > 0) {
+        k_scatter_packed<<<blocks_for(m), kThreads, 0, s>>>(du, dv, dw, m, poff, cursor, keys);
+        count_launch(1);
+    }
+    dfree(du); dfree(dv); dfree(dw);
+    if (!rc) rc = layout_rows(g, keys, 2 * m, deg64, poff, s);
+    dfree(deg); dfree(cursor); dfree(deg64); dfree(poff); dfree(keys);
+    if (rc) { dsssp_graph_destroy(g); return rc; }
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { dsssp_graph_destroy(g); return cuda_fail(e, "graph build"); }
+    *out = g;
+    return DSSSP_OK;
+}
+
+int dsssp_graph_info(const dsssp_graph* g, int64_t* n, int64_t* entries, int64_t* capacity,
+                     int64_t* device_bytes, int32_t* source) {
+    if (!g) return fail(DSSSP_E_INVAL, "graph_info: NULL graph");
+    if (n) *n = g->n;
+    if (entries) *entries = g->entries;
+    if (capacity) *capacity = g->cap_total;
+    if (source) *source = g->src;
+    if (device_bytes) {
+        const long long N = g->n;
+        long long b = N * (8 + 16 + 4 + 4 + 4 + 4 + 4 + 4 + 4) + g->cap_total * 8 + 2 * g->dg.hcap * 8 +
+                      g->chg_cap * (16 + 16 + 32) + (long long)sizeof(Ctl);
+        if (g->d_par) b += N * 12;
+        if (g->has_snap) b += N * (8 + 16 + 4) + g->s_cap * 8;
+        *device_bytes = b;
+    }
+    return DSSSP_OK;
+}
+
+int dsssp_tree_load(dsssp_graph* g, const int32_t* parent, const int64_t* dist) {
+    if (!g || !parent || !dist) return fail(DSSSP_E_INVAL, "tree_load: NULL argument");
+    int rc = set_device(g);
+    if (rc) return rc;
+    if (g->pending) return fail(DSSSP_E_INVAL, "tree_load: a batch is still pending");
+    cudaStream_t s = g->stream;
+    if (!g->d_par) {
+        rc = dalloc(&g->d_par, (size_t)g->n, "tree staging");
+        if (!rc) rc = dalloc(&g->d_dist, (size_t)g->n, "tree staging");
+        if (rc) return rc;
+    }
+    rc = clear_ctl(g, s);
+    if (rc) return rc;
+    const unsigned long long big = ~0ull;
+    CK(cudaMemcpyAsync(&g->dg.ctl->stat[1], &big, sizeof(big), cudaMemcpyHostToDevice, s), "tree load");
+    CK(cudaMemcpyAsync(g->d_par, parent, sizeof(int) * (size_t)g->n, cudaMemcpyHostToDevice, s), "tree upload");
+    CK(cudaMemcpyAsync(g->d_dist, dist, sizeof(long long) * (size_t)g->n, cudaMemcpyHostToDevice, s), "tree upload");
+    k_tree_pack<<<blocks_for(g->n), kThreads, 0, s>>>(g->d_par, g->d_dist, g->n, g->dg.state, g->dg.ctl);
+    count_launch(1);
+    CK(cudaMemcpyAsync(g->h_ctl, g->dg.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s), "tree load");
+    CK(cudaStreamSynchronize(s), "tree load");
+    if (g->h_ctl->status != 0) {
+        cudaMemsetAsync(g->dg.state, 0xFF, sizeof(unsigned long long) * (size_t)g->n, s);
+        cudaStreamSynchronize(s);
+        g->src = -1;
+        return fail(g->h_ctl->status, "tree_load: %s", g->h_ctl->status == DSSSP_E_OVERFLOW
+                                                              ? "a distance does not fit below 2^32-1"
+                                                              : "bad parent id, negative distance or root distance != 0");
+    }
+    if (g->h_ctl->stat[0] != 1) {
+        cudaMemsetAsync(g->dg.state, 0xFF, sizeof(unsigned long long) * (size_t)g->n, s);
+        cudaStreamSynchronize(s);
+        g->src = -1;
+        return fail(DSSSP_E_BAD_TREE, "tree_load: %llu vertices are their own parent (need exactly one root)",
+                    (unsigned long long)g->h_ctl->stat[0]);
+    }
+    g->src = (int)g->h_ctl->stat[1];
+    return DSSSP_OK;
+}
+
+int dsssp_tree_compute(dsssp_graph* g, int32_t src, dsssp_stats* st) {
+    if (!g) return fail(DSSSP_E_INVAL, "tree_compute: NULL graph");
+    if (src < 0 || src >= g->n) return fail(DSSSP_E_BAD_VERTEX, "tree_compute: source %d outside 0..%d", src, g->n - 1);
+    int rc = set_device(g);
+    if (rc) return rc;
+    if (g->pending) return fail(DSSSP_E_INVAL, "tree_compute: a batch is still pending");
+    cudaStream_t s = g->stream;
+    g->src = src;
+    rc = clear_ctl(g, s);
+    if (rc) return rc;
+    const bool ev = g->o.timing != 0;
+    if (ev) CK(cudaEventRecord(g->ev[0], s), "event");
+    k_state_reset<<<blocks_for(g->n), kThreads, 0, s>>>(g->dg.state, g->n, src);
+    count_launch(1);
+    if (ev) CK(cudaEventRecord(g->ev[1], s), "event");
+    UpdParams p = make_params(g, nullptr, 0, 1);
+    CK(launch_update(p, g->coop_grid, g->o.block, s), "update kernel");
+    if (ev) CK(cudaEventRecord(g->ev[2], s), "event");
+    CK(cudaMemcpyAsync(g->h_ctl, g->dg.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s), "status read");
+    CK(cudaStreamSynchronize(s), "tree compute");
+    fill_stats(g, *g->h_ctl, st, ev, 0, 0);
+    if (g->h_ctl->status != 0) reset_tags(g, s);
+    if (g->h_ctl->stat[ST_DIST_OVF] > 0 && g->h_ctl->status == 0) return status_code(DSSSP_E_OVERFLOW);
+    return status_code(g->h_ctl->status);
+}
+
+int dsssp_tree_read(dsssp_graph* g, int32_t* parent, int64_t* dist) {
+    if (!g) return fail(DSSSP_E_INVAL, "tree_read: NULL graph");
+    int rc = set_device(g);
+    if (rc) return rc;
+    if (g->pending) return fail(DSSSP_E_INVAL, "tree_read: a batch is still pending");
+    cudaStream_t s = g->stream;
+    if (!g->d_par) {
+        rc = dalloc(&g->d_par, (size_t)g->n, "tree staging");
+        if (!rc) rc = dalloc(&g->d_dist, (size_t)g->n, "tree staging");
+        if (rc) return rc;
+    }
+    k_tree_unpack<<<blocks_for(g->n), kThreads, 0, s>>>(g->dg.state, g->n, g->d_par, g->d_dist);
+    count_launch(1);
+    if (parent) CK(cudaMemcpyAsync(parent, g->d_par, sizeof(int) * (size_t)g->n, cudaMemcpyDeviceToHost, s), "tree read");
+    if (dist) CK(cudaMemcpyAsync(dist, g->d_dist, sizeof(long long) * (size_t)g->n, cudaMemcpyDeviceToHost, s), "tree read");
+    CK(cudaStreamSynchronize(s), "tree read");
+    return DSSSP_OK;
+}
+
+int dsssp_apply_batch_async(dsssp_graph* g, const dsssp_change* d_changes, int64_t k, void* stream) {
+    if (!g || k < 0 || (k > 0 && !d_changes)) return fail(DSSSP_E_INVAL, "apply_batch: bad arguments");
+    int rc = set_device(g);
+    if (rc) return rc;
+    if (g->pending) return fail(DSSSP_E_INVAL, "apply_batch: previous batch not finished");
+    if (g->src < 0) return fail(DSSSP_E_BAD_TREE, "apply_batch: no tree loaded");
+    cudaStream_t s = stream ? (cudaStream_t)stream : g->stream;
+    if (k == 0) return DSSSP_OK;
+    rc = ensure_batch(g, k);
+    if (!rc) rc = next_epoch(g, s);
+    if (!rc) rc = enqueue_batch(g, (const int4*)d_changes, k, s, true);
+    if (rc) return rc;
+    g->pending = true;
+    g->pend_k = k;
+    g->pend_chg = (const int4*)d_changes;
+    g->pend_stream = s;
+    g->pend_events = g->o.timing != 0;
+    return DSSSP_OK;
+}
+
+int dsssp_batch_finish(dsssp_graph* g, dsssp_stats* st) {
+    if (!g) return fail(DSSSP_E_INVAL, "batch_finish: NULL graph");
+    int rc = set_device(g);
+    if (rc) return rc;
+    return finish_batch(g, st);
+}
+
+int dsssp_apply_batch(dsssp_graph* g, const dsssp_change* changes, int64_t k, void* stream, dsssp_stats* st) {
+    if (!g || k < 0 || (k > 0 && !changes)) return fail(DSSSP_E_INVAL, "apply_batch: bad arguments");
+    int rc = set_device(g);
+    if (rc) return rc;
+    if (st) memset(st, 0, sizeof(*st));
+    if (k == 0) return DSSSP_OK;
+    rc = ensure_batch(g, k);
+    if (rc) return rc;
+    cudaStream_t s = stream ? (cudaStream_t)stream : g->stream;
+    CK(cudaMemcpyAsync(g->d_chg, changes, sizeof(int4) * (size_t)k, cudaMemcpyHostToDevice, s), "batch upload");
+    rc = dsssp_apply_batch_async(g, (const dsssp_change*)g->d_chg, k, s);
+    if (rc) return rc;
+    return finish_batch(g, st);
+}
+
+int dsssp_graph_snapshot(dsssp_graph* g) {
+    if (!g) return fail(DSSSP_E_INVAL, "snapshot: NULL graph");
+    int rc = set_device(g);
+    if (rc) return rc;
+    if (g->pending) return fail(DSSSP_E_INVAL, "snapshot: a batch is still pending");
+    if (!g->s_state) {
+        rc = dalloc(&g->s_state, (size_t)g->n, "snapshot");
+        if (!rc) rc = dalloc(&g->s_rows, (size_t)g->n, "snapshot");
+        if (!rc) rc = dalloc(&g->s_sorted, (size_t)g->n, "snapshot");
+        if (rc) return rc;
+    }
+    if (g->s_cap != g->cap_total) {
+        dfree(g->s_adj);
+        rc = dalloc(&g->s_adj, (size_t)g->cap_total, "snapshot");
+        if (rc) return rc;
+        g->s_cap = g->cap_total;
+    }
+    cudaStream_t s = g->stream;
+    const size_t N = (size_t)g->n;
+    CK(cudaMemcpyAsync(g->s_state, g->dg.state, N * 8, cudaMemcpyDeviceToDevice, s), "snapshot");
+    CK(cudaMemcpyAsync(g->s_rows, g->dg.rows, N * sizeof(RowDesc), cudaMemcpyDeviceToDevice, s), "snapshot");
+    CK(cudaMemcpyAsync(g->s_sorted, g->dg.sorted_len, N * 4, cudaMemcpyDeviceToDevice, s), "snapshot");
+    CK(cudaMemcpyAsync(g->s_adj, g->dg.adj, (size_t)g->cap_total * 8, cudaMemcpyDeviceToDevice, s), "snapshot");
+    CK(cudaStreamSynchronize(s), "snapshot");
+    g->s_entries = g->entries;
+    g->s_src = g->src;
+    g->has_snap = true;
+    return DSSSP_OK;
+}
+
+int dsssp_graph_restore(dsssp_graph* g, void* stream) {
+    if (!g || !g->has_snap) return fail(DSSSP_E_INVAL, "restore: no snapshot");
+    int rc = set_device(g);
+    if (rc) return rc;
+    if (g->pending) return fail(DSSSP_E_INVAL, "restore: a batch is still pending");
+    cudaStream_t s = stream ? (cudaStream_t)stream : g->stream;
+    if (g->cap_total != g->s_cap) {
+        CK(cudaStreamSynchronize(s), "restore");
+        dfree(g->dg.adj);
+        rc = dalloc(&g->dg.adj, (size_t)g->s_cap, "adjacency");
+        if (rc) return rc;
+        g->cap_total = g->s_cap;
+        rc = ensure_heavy(g);
+        if (rc) return rc;
+    }
+    const size_t N = (size_t)g->n;
+    CK(cudaMemcpyAsync(g->dg.state, g->s_state, N * 8, cudaMemcpyDeviceToDevice, s), "restore");
+    CK(cudaMemcpyAsync(g->dg.rows, g->s_rows, N * sizeof(RowDesc), cudaMemcpyDeviceToDevice, s), "restore");
+    CK(cudaMemcpyAsync(g->dg.sorted_len, g->s_sorted, N * 4, cudaMemcpyDeviceToDevice, s), "restore");
+    CK(cudaMemcpyAsync(g->dg.adj, g->s_adj, (size_t)g->s_cap * 8, cudaMemcpyDeviceToDevice, s), "restore");
+    g->entries = g->s_entries;
+    g->src = g->s_src;
+    return DSSSP_OK;
+}
+
+int dsssp_graph_compact(dsssp_graph* g) {
+    if (!g) return fail(DSSSP_E_INVAL, "compact: NULL graph");
+    int rc = set_device(g);
+    if (rc) return rc;
+    if (g->pending) return fail(DSSSP_E_INVAL, "compact: a batch is still pending");
+    return repack(g, nullptr, 0, g->stream);
+}
+
+}  // extern "C"

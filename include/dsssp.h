@@ -1,0 +1,217 @@
+/*
+ * dsssp.h -- C ABI of the GB300-native dynamic single-source-shortest-path engine.
+ *
+ * The engine keeps an undirected, integer-weighted graph and a shortest-path tree resident
+ * on one GPU and applies batches of edge insertions and deletions to them.  It is a drop-in
+ * for the update path of ArindamK92/DynamicSSSPv2 (SSSPmainForUndirected.cu, whose only
+ * interface is its command line and three text formats); each entry point below names the
+ * part of the reference it replaces.
+ *
+ * Conventions
+ *   - Every function that can fail returns 0 (DSSSP_OK) or a negative DSSSP_E* code;
+ *     dsssp_last_error() gives a message for the calling thread's last failure.
+ *   - Host buffers are owned by the caller; device memory is owned by the library.
+ *   - Vertex ids are 0..n-1.  Weights are int32 >= 0.  A distance is an integer below
+ *     2^32-1; an unreachable vertex has parent -1 and distance DSSSP_UNREACHABLE.
+ *   - A dsssp_graph is not thread-safe; separate graphs may be used from separate threads.
+ *   - Memory returned by the text readers and generators is released with dsssp_free().
+ */
+#ifndef DSSSP_H
+#define DSSSP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DSSSP_OK 0
+#define DSSSP_E_INVAL (-1)          /* bad argument */
+#define DSSSP_E_OOM (-2)            /* device or host allocation failed */
+#define DSSSP_E_BAD_VERTEX (-3)     /* vertex id outside 0..n-1 */
+#define DSSSP_E_CUDA (-4)           /* CUDA runtime error */
+#define DSSSP_E_NO_CONVERGENCE (-5) /* relaxation round cap reached */
+#define DSSSP_E_TIMEOUT (-6)        /* a bounded device-side wait gave up */
+#define DSSSP_E_BAD_TREE (-7)       /* tree has no unique root, a parent cycle or bad ids */
+#define DSSSP_E_OVERFLOW (-8)       /* a distance does not fit below 2^32-1 */
+#define DSSSP_E_IO (-9)             /* file could not be opened or written */
+#define DSSSP_E_BAD_WEIGHT (-10)    /* negative weight on an edge that is added */
+#define DSSSP_E_NO_DEVICE (-11)     /* no usable CUDA device */
+#define DSSSP_E_COOP (-12)          /* the persistent update kernel could not be co-resident */
+
+#define DSSSP_UNREACHABLE (-1)
+
+typedef struct dsssp_graph dsssp_graph;
+
+/* One change record: op 1 = insert, op 0 = delete, any other op is ignored
+ * (the reference's changeEdge, all_structure_undir.cuh:52-57, read by readin_changes,
+ * all_structure_undir.cuh:89-126).  16 bytes. */
+typedef struct {
+    int32_t u, v, w, op;
+} dsssp_change;
+
+/* Tunables.  dsssp_default_opts() fills defaults; the autotuner writes the same fields. */
+typedef struct {
+    int32_t device;       /* CUDA device ordinal */
+    int32_t slack_pct;    /* per-row insertion slack, percent of the row's degree */
+    int32_t slack_min;    /* minimum free slots per row */
+    int32_t small_deg;    /* frontier vertices with degree <= small_deg: one thread each */
+    int32_t large_deg;    /* degree <= large_deg: one warp each; above: CTA per chunk */
+    int32_t chunk;        /* edges per CTA work item of the large bucket */
+    int32_t bfs_levels;   /* subtree walk levels before switching to pointer jumping */
+    int32_t block;        /* threads per CTA of the update kernel (multiple of 32) */
+    int32_t ctas_per_sm;  /* resident CTAs per SM of the update kernel; 0 = occupancy max */
+    int32_t timing;       /* 1 = record CUDA events and phase timestamps into the stats */
+    int64_t max_rounds;   /* relaxation round cap; 0 = n + 1 */
+} dsssp_opts;
+
+/* Counters of one batch (or one tree computation), read back from the device. */
+typedef struct {
+    int64_t n_ins;             /* insertion records (op 1) */
+    int64_t n_del;             /* deletion records (op 0) */
+    int64_t n_ignored;         /* records with another op */
+    int64_t n_roots;           /* vertices cut off directly by a deleted tree edge */
+    int64_t n_invalidated;     /* all vertices of the cut-off subtrees (roots included) */
+    int64_t inv_levels;        /* subtree-walk levels */
+    int64_t pj_passes;         /* pointer-jumping passes (0 if the walk finished) */
+    int64_t rounds;            /* relaxation rounds */
+    int64_t frontier_total;    /* sum of frontier sizes over the rounds */
+    int64_t edges_relaxed;     /* adjacency entries scanned by relaxation rounds and seeds */
+    int64_t edges_inval;       /* adjacency entries scanned by the subtree walk and pulls */
+    int64_t del_probed;        /* adjacency entries examined to find deleted edges */
+    int64_t updates;           /* atomic updates that lowered a distance */
+    int64_t overflow_entries;  /* inserted entries that did not fit a row's slack */
+    int64_t repacks;           /* adjacency repacks this call triggered */
+    double t_step1_ms;         /* insert + delete kernels (CUDA events) */
+    double t_inval_ms;         /* subtree invalidation (device timestamps) */
+    double t_relax_ms;         /* seeding + relaxation rounds (device timestamps) */
+    double t_update_ms;        /* the persistent update kernel (CUDA events) */
+    double t_total_ms;         /* the whole batch on the device (CUDA events) */
+    double bytes_alg;          /* algorithmic bytes of the batch (see the design doc byte model) */
+    double bytes_alg_update;   /* the part moved by the persistent update kernel */
+} dsssp_stats;
+
+/* ---- engine ------------------------------------------------------------------------ */
+
+void dsssp_default_opts(dsssp_opts* o);
+
+/* Builds the device-resident graph (CSR rows sorted by neighbour, with per-row slack) from
+ * an undirected edge list; each line (u[i], v[i], w[i]) adds both directions.
+ * Replaces read_graphEdges + the CSR flatten and copy (all_structure_undir.cuh:178-198,
+ * SSSPmainForUndirected.cu:42-91).  o may be NULL for defaults. */
+int dsssp_graph_create(int32_t n, int64_t m, const int32_t* u, const int32_t* v,
+                       const int32_t* w, const dsssp_opts* o, dsssp_graph** out);
+
+void dsssp_graph_destroy(dsssp_graph* g);
+
+/* n, live adjacency entries, slot capacity, device bytes held, source (-1 if no tree). */
+int dsssp_graph_info(const dsssp_graph* g, int64_t* n, int64_t* entries, int64_t* capacity,
+                     int64_t* device_bytes, int32_t* source);
+
+/* Loads a shortest-path tree: parent[v] (-1 = unreachable, the root has parent[root]==root
+ * and dist 0) and dist[v].  Replaces read_SSSP's copy into managed memory
+ * (all_structure_undir.cuh:133-171, SSSPmainForUndirected.cu:147-165). */
+int dsssp_tree_load(dsssp_graph* g, const int32_t* parent, const int64_t* dist);
+
+/* Computes the tree from scratch on the GPU from source src (replaces running
+ * seqSSSPwithDist_undir.cpp to make the initial SSSP file). */
+int dsssp_tree_compute(dsssp_graph* g, int32_t src, dsssp_stats* st);
+
+/* Reads the current tree back into host arrays of n entries (either may be NULL).
+ * Replaces printSSSP and the host print of SSSPmainForUndirected.cu:298-312. */
+int dsssp_tree_read(dsssp_graph* g, int32_t* parent, int64_t* dist);
+
+/* Applies one change batch from host memory and waits for it: copies the records to the
+ * device, appends insertions into row slack, deletes every entry matching a deletion,
+ * invalidates cut-off subtrees and relaxes to the new shortest-path tree.
+ * Replaces STEP1 + STEP2 of SSSPmainForUndirected.cu:196-292 (deleteEdge, insertEdge,
+ * filterAffectedNodes, updateNeighbors_del, filterAllAffected, updateNeighbors).
+ * stream is a cudaStream_t (NULL = the library's own stream).  st may be NULL. */
+int dsssp_apply_batch(dsssp_graph* g, const dsssp_change* changes, int64_t k, void* stream,
+                      dsssp_stats* st);
+
+/* Asynchronous form for callers that keep the batch on the device: enqueues the update
+ * of k records at device address d_changes on stream and returns without waiting.
+ * dsssp_batch_finish() waits, handles a slack overflow and reports the status. */
+int dsssp_apply_batch_async(dsssp_graph* g, const dsssp_change* d_changes, int64_t k,
+                            void* stream);
+int dsssp_batch_finish(dsssp_graph* g, dsssp_stats* st);
+
+/* Device-side copy of the graph and tree, and its restore (benchmark repetition). */
+int dsssp_graph_snapshot(dsssp_graph* g);
+int dsssp_graph_restore(dsssp_graph* g, void* stream);
+
+/* Removes tombstones and re-sorts every row, restoring full slack (off the update path). */
+int dsssp_graph_compact(dsssp_graph* g);
+
+/* Pinned host memory for fast copies (cudaMallocHost) and its release. */
+void* dsssp_host_alloc(size_t bytes);
+void dsssp_host_free(void* p);
+
+/* Number of kernels this library has launched in this process. */
+int64_t dsssp_launch_count(void);
+
+const char* dsssp_last_error(void);
+const char* dsssp_strerror(int code);
+void dsssp_free(void* p);
+
+/* ---- reference text formats (all_structure_undir.cuh:89-198, README.md:25-37) ---- */
+
+/* graph file: "u v w" per line, each undirected edge once.  Vertex ids must be < n
+ * (the reference's AdjList.at throws otherwise).  Allocates *u, *v, *w. */
+int dsssp_read_graph_file(const char* path, int32_t n, int32_t** u, int32_t** v, int32_t** w,
+                          int64_t* m);
+
+/* change file: "u v w op" per line.  Allocates *changes (all lines with 4 fields; the
+ * engine ignores ops other than 0/1 as the reference does). */
+int dsssp_read_changes_file(const char* path, int32_t n, dsssp_change** changes, int64_t* k);
+
+/* SSSP file: "node parent dist" per line, read with the semantics of read_SSSP: missing
+ * vertices and parent -1 mean unreachable.  dist may be written as an integer or in the
+ * %g form the reference's Dijkstra prints; *lossy counts values that were not integers.
+ * Fills caller arrays parent[n], dist[n]. */
+int dsssp_read_sssp_file(const char* path, int32_t n, int32_t* parent, int64_t* dist,
+                         int64_t* lossy);
+
+/* Writes "node parent dist" lines (integers; unreachable: parent -1 dist -1). */
+int dsssp_write_sssp_file(const char* path, int32_t n, const int32_t* parent,
+                          const int64_t* dist);
+
+/* ---- seeded synthetic inputs (SplitMix64-based counter PRNG, same result on any host) --- */
+
+/* Erdos-Renyi: exactly m distinct undirected pairs u<v, w uniform in [wlo, whi]. */
+int dsssp_gen_er(int32_t n, int64_t m, int32_t wlo, int32_t whi, uint64_t seed, int32_t** u,
+                 int32_t** v, int32_t** w);
+
+/* RMAT(a, b, c, 1-a-b-c) on 2^scale vertices: exactly m distinct non-self-loop pairs
+ * (u<v after normalisation, ids not permuted), w uniform in [wlo, whi]. */
+int dsssp_gen_rmat(int32_t scale, int64_t m, double a, double b, double c, int32_t wlo,
+                   int32_t whi, uint64_t seed, int32_t** u, int32_t** v, int32_t** w);
+
+/* rows x cols grid, id = r*cols + c: 4-neighbour edges with a fraction remove_frac removed
+ * uniformly, plus n_diag distinct random diagonals (r+-1, c+-1); w uniform in [wlo, whi]. */
+int dsssp_gen_grid(int32_t rows, int32_t cols, double remove_frac, int64_t n_diag,
+                   int32_t wlo, int32_t whi, uint64_t seed, int32_t** u, int32_t** v,
+                   int32_t** w, int64_t* m);
+
+/* Insertion endpoint models for dsssp_gen_changes. */
+#define DSSSP_INS_UNIFORM 0 /* uniform random pairs */
+#define DSSSP_INS_RMAT 1    /* pairs drawn from RMAT(p0, p1, p2) on 2^scale vertices */
+#define DSSSP_INS_LOCAL 2   /* pairs within Chebyshev distance p0 on a grid of `scale` columns */
+
+/* A change batch over the graph (eu, ev, ew): n_ins insertions of pairs that are not edges
+ * of the graph (and distinct), w uniform in [wlo, whi]; n_del deletions sampled without
+ * replacement from the graph's lines.  Records are shuffled.  Allocates *changes. */
+int dsssp_gen_changes(int32_t n, int64_t m, const int32_t* eu, const int32_t* ev,
+                      const int32_t* ew, int64_t n_ins, int64_t n_del, int32_t ins_kind,
+                      int32_t scale, double p0, double p1, double p2, int32_t wlo, int32_t whi,
+                      uint64_t seed, dsssp_change** changes);
+
+/* Vertex of maximum degree (lowest id on ties) of an edge list. */
+int32_t dsssp_max_degree_vertex(int32_t n, int64_t m, const int32_t* u, const int32_t* v);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DSSSP_H */

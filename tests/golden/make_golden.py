@@ -1,0 +1,170 @@
+"""Generates tests/golden/golden.json by running the reference itself.
+
+Runs only where the reference sources are present (it builds oracle/_ref/ first):
+  - oracle/_ref/op_ssspSeq  = seqSSSPwithDist_undir.cpp compiled as-is (initial trees and the
+                              recomputed tree of the updated graph);
+  - oracle/_ref/ref_update  = the reference's readers and update kernels replayed on the CPU
+                              (oracle/ref_harness.cpp).
+Case 0 is the reference's own sample (graph.txt / SSSP.txt / cE.txt, README.md:18).  The
+other cases are seeded random graphs with the edge cases the engine must handle: weight-0
+edges, parallel edges, deletions of absent edges, insert+delete of the same edge in one batch,
+disconnected vertices.  The updated-graph file given to op_ssspSeq is built here in plain
+Python from the batch semantics (insertions appended, then every line matching a deletion's
+endpoint pair and weight removed), independently of oracle/oracle.c.
+
+usage: python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+REF = Path("/root/reference")
+REFBIN = ROOT / "oracle" / "_ref"
+
+
+def build_ref() -> None:
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "all", "ref", f"REF={REF}"], check=True)
+
+
+def write_lines(path: Path, rows) -> None:
+    path.write_text("".join(" ".join(str(x) for x in r) + "\n" for r in rows))
+
+
+def run_seq(graph: Path, n: int):
+    out = subprocess.run([str(REFBIN / "op_ssspSeq"), str(graph), str(n)], check=True, capture_output=True,
+                         text=True).stdout
+    parent = [0] * n
+    dist = [0.0] * n
+    for line in out.splitlines():
+        f = line.split()
+        if len(f) < 3:
+            continue
+        i = int(f[0])
+        parent[i] = int(f[1])
+        dist[i] = float(f[2])
+    return parent, dist
+
+
+def run_ref_update(graph: Path, n: int, m: int, sssp: Path, ce: Path):
+    out = subprocess.run([str(REFBIN / "ref_update"), str(graph), str(n), str(m), str(sssp), str(ce)], check=True,
+                         capture_output=True, text=True).stdout
+    dist = [0] * n
+    parent = [0] * n
+    rounds = {}
+    for line in out.splitlines():
+        f = line.split()
+        if f[0].startswith("rounds"):
+            rounds[f[0]] = int(f[1])
+            continue
+        i = int(f[0])
+        dist[i] = int(f[1])
+        parent[i] = int(f[2])
+    return dist, parent, rounds
+
+
+def updated_lines(edges, changes):
+    dels = {(min(u, v), max(u, v), w) for (u, v, w, op) in changes if op == 0}
+    lines = list(edges) + [(u, v, w) for (u, v, w, op) in changes if op == 1]
+    return [(u, v, w) for (u, v, w) in lines if (min(u, v), max(u, v), w) not in dels]
+
+
+def random_case(rng: np.random.Generator, n: int, m: int, wmax: int, n_ins: int, n_del: int, extras: bool):
+    edges = []
+    for _ in range(m):
+        a, b = int(rng.integers(0, n)), int(rng.integers(0, n))
+        if a == b:
+            continue
+        edges.append((a, b, int(rng.integers(0 if extras else 1, wmax + 1))))
+    if extras:
+        for _ in range(max(1, m // 20)):  # parallel edges, some with the same weight
+            a, b, w = edges[int(rng.integers(0, len(edges)))]
+            edges.append((b, a, w if rng.random() < 0.5 else int(rng.integers(0, wmax + 1))))
+    changes = []
+    for _ in range(n_ins):
+        a, b = int(rng.integers(0, n)), int(rng.integers(0, n))
+        if a == b:
+            continue
+        changes.append((a, b, int(rng.integers(0 if extras else 1, wmax + 1)), 1))
+    for _ in range(n_del):
+        a, b, w = edges[int(rng.integers(0, len(edges)))]
+        changes.append((a, b, w, 0))
+    if extras:
+        # an insertion deleted again in the same batch, a deletion of an absent edge,
+        # a deletion whose weight does not match, and an ignored op
+        a, b, w, _ = changes[0]
+        changes.append((b, a, w, 0))
+        changes.append((0, n - 1, 7, 0))
+        a, b, w = edges[1]
+        changes.append((a, b, w + 1000, 0))
+        changes.append((1, 2, 3, 5))
+    order = rng.permutation(len(changes))
+    return edges, [changes[i] for i in order]
+
+
+def make_case(tmp: Path, name: str, n: int, edges, changes, sssp_rows=None):
+    g = tmp / f"{name}_graph.txt"
+    s = tmp / f"{name}_SSSP.txt"
+    c = tmp / f"{name}_cE.txt"
+    u = tmp / f"{name}_updated.txt"
+    write_lines(g, edges)
+    write_lines(c, changes)
+    if sssp_rows is None:
+        par0, dist0 = run_seq(g, n)
+        sssp_rows = [(i, par0[i], int(dist0[i])) for i in range(n)]
+    write_lines(s, sssp_rows)
+    upd = updated_lines(edges, changes)
+    write_lines(u, upd)
+    par1, dist1 = run_seq(u, n)
+    rd, rp, rounds = run_ref_update(g, n, len(edges), s, c)
+    return {
+        "name": name,
+        "n": n,
+        "edges": [list(e) for e in edges],
+        "changes": [list(x) for x in changes],
+        "sssp_in": [list(r) for r in sssp_rows],
+        "seq_after": {"parent": par1, "dist": [int(x) for x in dist1], "inf": 1000 * n},
+        "ref_update": {"dist": rd, "parent": rp, "rounds": rounds},
+    }
+
+
+def main() -> int:
+    if not (REF / "seqSSSPwithDist_undir.cpp").exists():
+        print("reference sources not present; nothing to do", file=sys.stderr)
+        return 1
+    build_ref()
+    cases = []
+    with tempfile.TemporaryDirectory() as td:
+        tmp = Path(td)
+        sample_edges = [tuple(int(x) for x in l.split()[:3]) for l in (REF / "graph.txt").read_text().splitlines() if l.split()]
+        sample_changes = [tuple(int(x) for x in l.split()[:4]) for l in (REF / "cE.txt").read_text().splitlines() if l.split()]
+        sample_sssp = [tuple(int(x) for x in l.split()[:3]) for l in (REF / "SSSP.txt").read_text().splitlines() if l.split()]
+        cases.append(make_case(tmp, "sample", 6, sample_edges, sample_changes, sample_sssp))
+        rng = np.random.default_rng(20261203)
+        specs = [
+            ("er_small", 40, 120, 20, 10, 10, False),
+            ("er_extras", 60, 200, 9, 15, 15, True),
+            ("sparse_disconnected", 120, 100, 50, 20, 20, False),
+            ("dense_weights0", 30, 250, 3, 20, 25, True),
+            ("mid", 200, 700, 100, 40, 40, True),
+            ("mid_delete_heavy", 200, 600, 30, 5, 120, False),
+            ("mid_insert_heavy", 200, 500, 30, 120, 5, True),
+        ]
+        for name, n, m, wmax, ni, nd, extras in specs:
+            edges, changes = random_case(rng, n, m, wmax, ni, nd, extras)
+            cases.append(make_case(tmp, name, n, edges, changes))
+    out = HERE / "golden.json"
+    out.write_text(json.dumps({"generator": "tests/golden/make_golden.py", "cases": cases}, separators=(",", ":")))
+    print(f"wrote {out} ({out.stat().st_size} bytes, {len(cases)} cases)")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

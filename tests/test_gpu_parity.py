@@ -1,0 +1,263 @@
+"""GPU parity: the engine (through the C ABI) against the oracle and the reference's golden
+outputs.  Distances must be bit-exact; parents must form a valid shortest-path tree."""
+import numpy as np
+import pytest
+
+import dynamicssspv2_gb300 as D
+from oracle import pyoracle as O
+from tests.common import case_arrays, check_against_oracle, golden_cases, tree_from_rows
+
+pytestmark = pytest.mark.gpu
+
+CASES = golden_cases()
+
+
+def initial_tree(n, u, v, w, src=0):
+    g = O.csr(n, u, v, w)
+    dist, parent = O.dijkstra(n, g, src)
+    return parent, dist
+
+
+def run_engine(n, u, v, w, changes, parent, dist, **opts):
+    with D.Graph(n, u, v, w, **opts) as g:
+        g.tree_load(parent, dist)
+        st = g.apply_batch(changes)
+        p, d = g.tree_read()
+    return p, d, st
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_golden_cases(case):
+    """Updated distances == the reference's seqSSSPwithDist_undir.cpp on the updated graph."""
+    n = case["n"]
+    u, v, w, ch = case_arrays(case)
+    parent, dist = tree_from_rows(n, case["sssp_in"])
+    p, d, st = run_engine(n, u, v, w, ch, parent, dist)
+    want_p = np.array(case["seq_after"]["parent"])
+    want_d = np.array(case["seq_after"]["dist"])
+    assert ((p == -1) == (want_p == -1)).all()
+    reach = want_p != -1
+    assert (d[reach] == want_d[reach]).all()
+    check_against_oracle(n, u, v, w, ch, 0, p, d, case["name"])
+    assert st.n_ins == int((ch["op"] == 1).sum()) and st.n_del == int((ch["op"] == 0).sum())
+
+
+def test_sample_known_answer():
+    case = CASES[0]
+    n = case["n"]
+    u, v, w, ch = case_arrays(case)
+    parent, dist = tree_from_rows(n, case["sssp_in"])
+    p, d, _ = run_engine(n, u, v, w, ch, parent, dist)
+    assert d.tolist() == [0, 4, 6, 6, 4, 9]
+    assert p.tolist() in ([0, 4, 0, 1, 0, 2], [0, 4, 4, 1, 0, 2])
+
+
+OPTION_SETS = [
+    {},
+    {"bfs_levels": 0},                                     # pointer jumping only
+    {"bfs_levels": 1},                                     # walk one level, then pointer jumping
+    {"small_deg": 0, "large_deg": 0, "chunk": 32},          # every row on the CTA-chunk path
+    {"small_deg": 0, "large_deg": 1 << 20},                # every row one warp
+    {"small_deg": 1 << 20, "large_deg": 1 << 20},          # every row one thread
+    {"slack_pct": 0, "slack_min": 0},                      # every insertion overflows -> repack
+    {"block": 64, "ctas_per_sm": 1},
+]
+
+
+@pytest.mark.parametrize("opts", OPTION_SETS, ids=[str(o) or "default" for o in OPTION_SETS])
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_random_er_batches(opts, seed):
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(200, 3000))
+    m = int(n * rng.uniform(1.5, 6))
+    u, v, w = D.gen_er(n, m, 1, 50, seed)
+    ch = D.gen_changes(n, u, v, w, m // 20, m // 10, seed=seed + 100)
+    parent, dist = initial_tree(n, u, v, w)
+    p, d, st = run_engine(n, u, v, w, ch, parent, dist, **opts)
+    check_against_oracle(n, u, v, w, ch, 0, p, d, f"seed {seed} {opts}")
+    if opts.get("slack_pct") == 0:
+        assert st.repacks == 1 and st.overflow_entries > 0
+
+
+def test_zero_weights_multiedges_selfloops():
+    """Weight-0 edges (equal-distance ties must not form parent cycles), parallel edges and
+    self-loops, with deletions hitting them."""
+    rng = np.random.default_rng(7)
+    n = 300
+    u = rng.integers(0, n, 2000).astype(np.int32)
+    v = rng.integers(0, n, 2000).astype(np.int32)
+    w = rng.integers(0, 4, 2000).astype(np.int32)
+    u[:50], v[:50] = np.arange(50), np.arange(50)  # self-loops
+    u = np.concatenate([u, u[100:200]])
+    v = np.concatenate([v, v[100:200]])
+    w = np.concatenate([w, w[100:200]])  # exact duplicates
+    parent, dist = initial_tree(n, u, v, w)
+    idx = rng.choice(len(u), 300, replace=False)
+    ins_u = rng.integers(0, n, 200)
+    ins_v = rng.integers(0, n, 200)
+    ch = D.make_changes(np.concatenate([u[idx], ins_u]), np.concatenate([v[idx], ins_v]),
+                        np.concatenate([w[idx], rng.integers(0, 3, 200)]), np.concatenate([np.zeros(300), np.ones(200)]))
+    ch = ch[rng.permutation(len(ch))]
+    for opts in ({}, {"bfs_levels": 0}):
+        p, d, _ = run_engine(n, u, v, w, ch, parent, dist, **opts)
+        check_against_oracle(n, u, v, w, ch, 0, p, d, f"zero weights {opts}")
+
+
+def test_insert_then_delete_same_edge_in_one_batch():
+    """The reference seeds relaxation from an insertion even when the same batch deletes it
+    (gpuFunctions_undir.cuh:217-251 runs after the tombstoning); the engine must not."""
+    n = 4
+    u = np.array([0, 1, 2], np.int32)
+    v = np.array([1, 2, 3], np.int32)
+    w = np.array([10, 10, 10], np.int32)
+    parent, dist = initial_tree(n, u, v, w)
+    ch = D.make_changes([0, 3], [3, 0], [1, 1], [1, 0])
+    p, d, _ = run_engine(n, u, v, w, ch, parent, dist)
+    assert d.tolist() == [0, 10, 20, 30]
+    check_against_oracle(n, u, v, w, ch, 0, p, d, "insert+delete")
+
+
+def test_disconnect_and_reconnect():
+    # path 0-1-2-3-4; delete 1-2 (cuts 2,3,4), insert 4-0 w 100
+    u = np.array([0, 1, 2, 3], np.int32)
+    v = np.array([1, 2, 3, 4], np.int32)
+    w = np.array([1, 1, 1, 1], np.int32)
+    parent, dist = initial_tree(5, u, v, w)
+    ch = D.make_changes([1], [2], [1], [0])
+    p, d, st = run_engine(5, u, v, w, ch, parent, dist)
+    assert p.tolist() == [0, 0, -1, -1, -1] and d.tolist() == [0, 1, -1, -1, -1]
+    assert st.n_roots == 1 and st.n_invalidated == 3
+    ch2 = D.make_changes([1, 4], [2, 0], [1, 100], [0, 1])
+    p, d, _ = run_engine(5, u, v, w, ch2, parent, dist)
+    assert d.tolist() == [0, 1, 102, 101, 100]
+
+
+def test_source_never_invalidated():
+    """Deleting a self-loop on the source invalidates it in the reference (Parent[src]==src);
+    the engine keeps the source at distance 0."""
+    u = np.array([0, 0, 1], np.int32)
+    v = np.array([0, 1, 2], np.int32)
+    w = np.array([3, 2, 2], np.int32)
+    parent, dist = initial_tree(3, u, v, w)
+    ch = D.make_changes([0], [0], [3], [0])
+    p, d, _ = run_engine(3, u, v, w, ch, parent, dist)
+    assert d.tolist() == [0, 2, 4]
+
+
+@pytest.mark.parametrize("kind", ["rmat", "grid"])
+def test_tree_compute_from_scratch(kind):
+    if kind == "rmat":
+        n = 1 << 13
+        u, v, w = D.gen_rmat(13, 8 * n, seed=3)
+        src = D.max_degree_vertex(n, u, v)
+    else:
+        n = 64 * 64
+        u, v, w = D.gen_grid(64, 64, 0.05, 40, 1, 1000, seed=3)
+        src = 0
+    with D.Graph(n, u, v, w) as g:
+        st = g.tree_compute(src)
+        p, d = g.tree_read()
+    check_against_oracle(n, u, v, w, None, src, p, d, kind)
+    assert st.rounds > 0
+
+
+def test_sequence_of_batches():
+    """Five batches in a row on one resident graph, each checked against a full recompute."""
+    n, m = 4000, 16000
+    u, v, w = D.gen_er(n, m, 1, 100, 11)
+    parent, dist = initial_tree(n, u, v, w)
+    cu, cv, cw = u.copy(), v.copy(), w.copy()
+    with D.Graph(n, u, v, w, slack_pct=5, slack_min=1) as g:
+        g.tree_load(parent, dist)
+        for b in range(5):
+            ch = D.gen_changes(n, cu, cv, cw, 400, 600, seed=200 + b)
+            g.apply_batch(ch)
+            p, d = g.tree_read()
+            check_against_oracle(n, cu, cv, cw, ch, 0, p, d, f"batch {b}")
+            # the graph after the batch becomes the base of the next one
+            gr, kept = O.updated_graph(n, cu, cv, cw, ch, return_kept=True)
+            ins = ch[ch["op"] == 1]
+            lu = np.concatenate([cu, ins["u"]])
+            lv = np.concatenate([cv, ins["v"]])
+            lw = np.concatenate([cw, ins["w"]])
+            keep = kept[: len(lu)].astype(bool)
+            cu, cv, cw = lu[keep].astype(np.int32), lv[keep].astype(np.int32), lw[keep].astype(np.int32)
+        g.compact()
+        ch = D.gen_changes(n, cu, cv, cw, 100, 100, seed=999)
+        g.apply_batch(ch)
+        p, d = g.tree_read()
+        check_against_oracle(n, cu, cv, cw, ch, 0, p, d, "after compact")
+
+
+def test_config_small_er_exact():
+    """10,000 vertices, 50,000 edges, 500 insertions + 500 deletions, source 0."""
+    n, m = 10_000, 50_000
+    u, v, w = D.gen_er(n, m, 1, 100, 0)
+    ch = D.gen_changes(n, u, v, w, 500, 500, seed=1)
+    parent, dist = initial_tree(n, u, v, w)
+    p, d, st = run_engine(n, u, v, w, ch, parent, dist)
+    check_against_oracle(n, u, v, w, ch, 0, p, d, "config small")
+    assert st.n_ins == 500 and st.n_del == 500 and st.repacks == 0
+
+
+def test_snapshot_restore_repeats_exactly():
+    n, m = 3000, 12000
+    u, v, w = D.gen_er(n, m, 1, 100, 5)
+    ch = D.gen_changes(n, u, v, w, 300, 300, seed=6)
+    parent, dist = initial_tree(n, u, v, w)
+    with D.Graph(n, u, v, w) as g:
+        g.tree_load(parent, dist)
+        g.snapshot()
+        g.apply_batch(ch)
+        p1, d1 = g.tree_read()
+        g.restore()
+        p0, d0 = g.tree_read()
+        assert (d0 == dist).all() and (p0 == parent).all()
+        g.apply_batch(ch)
+        p2, d2 = g.tree_read()
+    assert (d1 == d2).all()
+    check_against_oracle(n, u, v, w, ch, 0, p2, d2, "after restore")
+
+
+def test_errors_leave_graph_unchanged():
+    n, m = 500, 2000
+    u, v, w = D.gen_er(n, m, 1, 100, 8)
+    parent, dist = initial_tree(n, u, v, w)
+    with D.Graph(n, u, v, w) as g:
+        g.tree_load(parent, dist)
+        bad = D.make_changes([1, 2], [n + 5, 3], [1, 1], [1, 1])
+        with pytest.raises(D.DsssspError) as e:
+            g.apply_batch(bad)
+        assert e.value.code == D.E_BAD_VERTEX
+        neg = D.make_changes([1], [2], [-4], [1])
+        with pytest.raises(D.DsssspError) as e:
+            g.apply_batch(neg)
+        assert e.value.code == D.E_BAD_WEIGHT
+        p, d = g.tree_read()
+        assert (p == parent).all() and (d == dist).all()
+        two_roots = parent.copy()
+        two_roots[5] = 5
+        d2 = dist.copy()
+        d2[5] = 0
+        with pytest.raises(D.DsssspError) as e:
+            g.tree_load(two_roots, d2)
+        assert e.value.code == D.E_BAD_TREE
+    with pytest.raises(D.DsssspError) as e:
+        D.Graph(3, [0], [5], [1])
+    assert e.value.code == D.E_BAD_VERTEX
+
+
+def test_parent_cycle_is_reported():
+    """A tree with a parent cycle below a cut-off vertex: pointer jumping gives up after a
+    bounded number of passes and reports DSSSP_E_BAD_TREE."""
+    n = 6
+    u = np.array([0, 1, 2, 3, 4], np.int32)
+    v = np.array([1, 2, 3, 4, 5], np.int32)
+    w = np.ones(5, np.int32)
+    parent = np.array([0, 0, 1, 4, 3, 4], np.int32)  # 3 <-> 4 cycle
+    dist = np.array([0, 1, 2, 3, 4, 5], np.int64)
+    with D.Graph(n, u, v, w, bfs_levels=0) as g:
+        g.tree_load(parent, dist)
+        with pytest.raises(D.DsssspError) as e:
+            g.apply_batch(D.make_changes([0], [1], [1], [0]))
+        assert e.value.code == D.E_BAD_TREE
