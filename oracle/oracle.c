@@ -12,22 +12,53 @@
 /* Updated graph (all_structure_undir.cuh:89-126 + gpuFunctions_undir.cuh:179-215)       */
 /* ------------------------------------------------------------------------------------ */
 
-typedef struct {
-    uint64_t pair; /* min(u,v) << 32 | max(u,v) */
-    int32_t w;
-} del_key;
-
-static int cmp_del_key(const void* a, const void* b) {
-    const del_key* x = (const del_key*)a;
-    const del_key* y = (const del_key*)b;
-    if (x->pair != y->pair) return x->pair < y->pair ? -1 : 1;
-    if (x->w != y->w) return x->w < y->w ? -1 : 1;
-    return 0;
-}
-
 static uint64_t pair_key(int32_t a, int32_t b) {
     uint32_t lo = (uint32_t)(a < b ? a : b), hi = (uint32_t)(a < b ? b : a);
     return ((uint64_t)lo << 32) | hi;
+}
+
+/* open-addressing set of (endpoint pair, weight) deletion keys */
+typedef struct {
+    uint64_t* pair;
+    int32_t* w;
+    uint8_t* used;
+    uint64_t mask;
+} del_set;
+
+static uint64_t mix_key(uint64_t p, int32_t w) {
+    uint64_t z = p ^ ((uint64_t)(uint32_t)w * 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static void del_set_init(del_set* s, int64_t n) {
+    uint64_t cap = 16;
+    while (cap < (uint64_t)n * 2 + 16) cap <<= 1;
+    s->pair = (uint64_t*)malloc(sizeof(uint64_t) * cap);
+    s->w = (int32_t*)malloc(sizeof(int32_t) * cap);
+    s->used = (uint8_t*)calloc(cap, 1);
+    s->mask = cap - 1;
+}
+
+static void del_set_free(del_set* s) { free(s->pair); free(s->w); free(s->used); }
+
+static void del_set_add(del_set* s, uint64_t p, int32_t w) {
+    uint64_t h = mix_key(p, w) & s->mask;
+    while (s->used[h]) {
+        if (s->pair[h] == p && s->w[h] == w) return;
+        h = (h + 1) & s->mask;
+    }
+    s->used[h] = 1; s->pair[h] = p; s->w[h] = w;
+}
+
+static int del_set_has(const del_set* s, uint64_t p, int32_t w) {
+    uint64_t h = mix_key(p, w) & s->mask;
+    while (s->used[h]) {
+        if (s->pair[h] == p && s->w[h] == w) return 1;
+        h = (h + 1) & s->mask;
+    }
+    return 0;
 }
 
 /* Marks which lines (m base lines followed by the insertions, in batch order) survive. */
@@ -40,39 +71,32 @@ static int64_t mark_lines(int32_t n, int64_t m, const int32_t* eu, const int32_t
         if (cop[i] == 1) n_ins++;
         else if (cop[i] == 0) n_del++;
     }
-    del_key* dk = (del_key*)malloc(sizeof(del_key) * (size_t)(n_del ? n_del : 1));
-    int64_t j = 0;
+    del_set ds;
+    del_set_init(&ds, n_del);
     for (int64_t i = 0; i < k; i++) {
         if (cop[i] != 0 && cop[i] != 1) continue;
         if (cu[i] < 0 || cu[i] >= n || cv[i] < 0 || cv[i] >= n) {
-            free(dk);
+            del_set_free(&ds);
             return -1;
         }
-        if (cop[i] == 0) {
-            dk[j].pair = pair_key(cu[i], cv[i]);
-            dk[j].w = cw[i];
-            j++;
-        }
+        if (cop[i] == 0) del_set_add(&ds, pair_key(cu[i], cv[i]), cw[i]);
     }
-    qsort(dk, (size_t)n_del, sizeof(del_key), cmp_del_key);
     int64_t L = m + n_ins, line = 0, nnz = 0;
     for (int64_t i = 0; i < m + k; i++) {
         int32_t a, b, w;
         if (i < m) {
             a = eu[i]; b = ev[i]; w = ew[i];
-            if (a < 0 || a >= n || b < 0 || b >= n) { free(dk); return -1; }
+            if (a < 0 || a >= n || b < 0 || b >= n) { del_set_free(&ds); return -1; }
         } else {
             int64_t c = i - m;
             if (cop[c] != 1) continue;
             a = cu[c]; b = cv[c]; w = cw[c];
         }
-        del_key q = {pair_key(a, b), w};
-        int alive = n_del == 0 ||
-                    bsearch(&q, dk, (size_t)n_del, sizeof(del_key), cmp_del_key) == NULL;
+        int alive = n_del == 0 || !del_set_has(&ds, pair_key(a, b), w);
         keep[line++] = (uint8_t)alive;
         if (alive) nnz += 2;
     }
-    free(dk);
+    del_set_free(&ds);
     *n_lines_out = L;
     return nnz;
 }
