@@ -63,6 +63,7 @@ class Stats(C.Structure):
         for name in (
             "n_ins", "n_del", "n_ignored", "n_roots", "n_invalidated", "inv_levels", "pj_passes", "rounds",
             "frontier_total", "edges_relaxed", "edges_inval", "del_probed", "updates", "overflow_entries", "repacks",
+            "n_killed", "work_items",
         )
     ] + [
         (name, C.c_double)

@@ -1,6 +1,6 @@
 // engine.cuh -- device data layout and primitives of the dynamic SSSP engine (sm_103a).
 //
-// Layout in HBM (one graph):
+// Layout in HBM (one graph of n vertices):
 //   state[n]      u64  (dist << 32) | parent      dist 0xFFFFFFFF = unreachable, parent
 //                                                 0xFFFFFFFF = none; one atomicMin keeps
 //                                                 distance and parent consistent
@@ -10,9 +10,12 @@
 //   inv_tag[n]    u32  batch epoch in which the vertex was cut off
 //   push_tag[n]   u32  round tag of the last frontier push (de-duplication)
 //   jm[n]         u32  pointer-jumping word (ancestor or terminal tag)
-//   invq[n]       u32  every vertex cut off in this batch, in discovery order
-//   q[2][n]       u32  frontier double buffer, h[2][n] heavy-vertex lists
-//   ctl           control block: grid barrier, status word, queue counters, statistics
+//   invq[n]       u32  vertices cut off directly by a deleted tree edge
+//   work items    8 B  (vertex, chunk): a pushed vertex of degree d becomes ceil(d/te) thread
+//                      items of te edges, or, above large_deg, ceil(d/chunk) CTA items;
+//                      rt/rc = relaxation frontier (double buffer), it/ic = cut-off vertices
+//   ctl           control block: grid barrier, status word, list counters, statistics, one
+//                 128-byte line per group of fields that different CTAs hit at the same time
 #pragma once
 #include <cstdint>
 
@@ -26,6 +29,8 @@ constexpr unsigned long long kDistInf = 0xFFFFFFFFull;
 constexpr unsigned kTagOk = 0xFFFFFFFFu;   // pointer jumping: reaches the root untouched
 constexpr unsigned kTagInv = 0xFFFFFFFEu;  // pointer jumping: below a cut-off vertex
 constexpr int kStatusOverflowPending = 1;  // internal: an insertion did not fit its row
+constexpr unsigned long long kHashEmpty = 0xFFFFFFFFFFFFFFFFull;
+constexpr int kHashNoWeight = (int)0x80808080;  // byte-fill sentinel; deletions with w < 0 are not hashed
 
 struct __align__(16) RowDesc {
     long long start;
@@ -48,36 +53,46 @@ enum StatIdx {
     ST_DEL_PROBED,
     ST_UPDATES,
     ST_OVF,
-    ST_PUSHES,
+    ST_ITEMS,
     ST_DIST_OVF,
     ST_COUNT
 };
 
-// Device control block.  Fields from `status` on are cleared before every batch.
-struct Ctl {
+// Device control block.  Everything from line 1 on is cleared before every batch.
+struct __align__(128) Ctl {
+    // line 0 (persistent)
     unsigned bar_gen;
     unsigned round_base;
-    unsigned pad0[2];
-    // ---- cleared per batch ----
+    unsigned pad0[30];
+    // line 1
     int status;
     int ovf_count;
+    unsigned inv_count;  // roots appended by k_delete
+    unsigned killed;     // insertions removed by a deletion of the same batch
+    unsigned pad1[28];
+    // line 2
     unsigned bar_count;
-    unsigned inv_count;
-    unsigned cq[3];   // frontier counts (round r reads cq[r%3])
-    unsigned ch[3];   // heavy-list counts of the relaxation rounds
-    unsigned bh[3];   // heavy-list counts of the subtree walk
-    unsigned ph;      // heavy-list count of the pull pass
-    unsigned pjf[3];  // pointer-jumping "still moving" flags
-    unsigned lc[3];   // subtree walk: vertices cut off during level L counted in lc[(L+1)%3]
-    unsigned pj_cnt;  // vertices cut off by pointer jumping
-    unsigned pad1[2];
-    // barrier diagnostics: first timed-out barrier index, arrivals seen then, CTAs that timed
-    // out, and per-CTA barrier counts at exit (max, 0xFFFFFFFF - min)
-    unsigned diag[6];
-    unsigned pad2[2];
+    unsigned pad2[31];
+    // line 3: relaxation lists, round r reads slot r%3
+    unsigned rcT[3];
+    unsigned rcC[3];
+    unsigned pad3[26];
+    // line 4: cut-off lists (level L appends to slot (L+1)%3), pointer jumping
+    unsigned ltT[3];
+    unsigned ltC[3];
+    unsigned pjT;
+    unsigned pjC;
+    unsigned pjf[3];
+    unsigned pad4[21];
+    // line 5: barrier diagnostics (first timed-out barrier, arrivals then, CTAs that timed
+    // out, max barrier count at exit, 0xFFFFFFFF - min barrier count at exit)
+    unsigned diag[8];
+    unsigned pad5[24];
+    // lines 6-7
     unsigned long long stat[ST_COUNT];
-    unsigned long long ts[8];  // %globaltimer stamps: 0 start, 1 after invalidation,
-                               // 2 after seeding, 3 end
+    // line 8: %globaltimer stamps: 0 start, 1 after invalidation, 2 after seeding, 3 end
+    unsigned long long ts[8];
+    unsigned long long pad6[8];
 };
 
 struct DevGraph {
@@ -89,11 +104,14 @@ struct DevGraph {
     unsigned* push_tag;
     unsigned* jm;
     unsigned* invq;
-    unsigned* q0;
-    unsigned* q1;
-    uint2* h0;  // heavy lists: (vertex, chunk index) work items
-    uint2* h1;
-    long long hcap;
+    uint2* rt0;  // relaxation thread items, double buffer
+    uint2* rt1;
+    uint2* rc0;  // relaxation CTA items, double buffer
+    uint2* rc1;
+    uint2* it;   // cut-off vertices' thread items
+    uint2* ic;   // cut-off vertices' CTA items
+    long long tcap;
+    long long ccap;
     Ctl* ctl;
     int n;
     int src;
@@ -101,15 +119,19 @@ struct DevGraph {
 
 struct UpdParams {
     DevGraph g;
-    const int4* chg;        // (u, v, w, op) records
+    const int4* chg;  // (u, v, w, op) records
     long long k;
-    const long long* slot;  // per change: 2 adjacency indices of an inserted entry
+    int* ins_state;   // per record: 1 = insertion that survives the batch
+    unsigned long long* hpair;  // deletion set: endpoint pair -> weight (open addressing)
+    int* hw;
+    unsigned long long hmask;
+    int4* ovf;        // insertions that did not fit their row: (row, col, wt, record)
     unsigned epoch;
-    int small_deg;
-    int large_deg;
-    int chunk;
+    int te;           // edges per thread item
+    int large_deg;    // rows above this become CTA items
+    int chunk;        // edges per CTA item
     int bfs_levels;
-    int mode;  // 0 = batch update, 1 = from scratch (state already reset, src seeded)
+    int mode;         // 0 = batch update, 1 = from scratch (state already reset)
     long long max_rounds;
 };
 
@@ -133,6 +155,17 @@ __device__ __forceinline__ unsigned long long globaltimer() {
 
 __device__ __forceinline__ void set_status(Ctl* ctl, int code) { atomicCAS(&ctl->status, 0, code); }
 
+__device__ __forceinline__ unsigned long long dmix64(unsigned long long z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ unsigned long long dpair_key(unsigned a, unsigned b) {
+    return a < b ? ((unsigned long long)a << 32) | b : ((unsigned long long)b << 32) | a;
+}
+
 // ---- warp helpers (must be called by all 32 lanes) -------------------------------------
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
@@ -149,13 +182,12 @@ __device__ __forceinline__ void warp_append(bool pred, unsigned val, unsigned* l
     if (pred) list[base + __popc(mask & ((1u << lane) - 1u))] = val;
 }
 
-// Appends cnt items (val, 0..cnt-1) for every lane with pred set, one atomic per warp.
-// Returns false (and appends nothing) if the list would exceed cap.
-__device__ __forceinline__ bool warp_append_chunks(bool pred, unsigned val, unsigned cnt, uint2* list,
-                                                   unsigned* counter, long long cap) {
-    unsigned c = pred ? cnt : 0u;
+// Appends items (val, 0..cnt-1) for every lane, one atomic per warp.  Returns false (and
+// appends nothing) if the list would exceed cap.
+__device__ __forceinline__ bool warp_append_chunks(unsigned val, unsigned cnt, uint2* list, unsigned* counter,
+                                                   long long cap) {
     const unsigned lane = lane_id();
-    unsigned incl = c;
+    unsigned incl = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const unsigned t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
@@ -167,8 +199,8 @@ __device__ __forceinline__ bool warp_append_chunks(bool pred, unsigned val, unsi
     if (lane == 31) base = atomicAdd(counter, total);
     base = __shfl_sync(0xFFFFFFFFu, base, 31);
     if ((long long)base + total > cap) return false;
-    const unsigned first = base + incl - c;
-    for (unsigned k = 0; k < c; k++) list[first + k] = make_uint2(val, k);
+    const unsigned first = base + incl - cnt;
+    for (unsigned k = 0; k < cnt; k++) list[first + k] = make_uint2(val, k);
     return true;
 }
 
@@ -178,6 +210,12 @@ __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v)
         unsigned long long w = __shfl_xor_sync(0xFFFFFFFFu, v, o);
         v = w < v ? w : v;
     }
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
     return v;
 }
 

@@ -22,8 +22,7 @@
 
 namespace dsssp {
 
-cudaError_t launch_front(const UpdParams& p, int4* ovf, bool with_append, cudaStream_t s);
-cudaError_t launch_relocate(const UpdParams& p, cudaStream_t s);
+cudaError_t launch_front(const UpdParams& p, int grid, cudaStream_t s);
 cudaError_t update_occupancy(int block, int* blocks_per_sm);
 cudaError_t launch_update(const UpdParams& p, int grid, int block, cudaStream_t s);
 
@@ -252,8 +251,11 @@ struct dsssp_graph {
     // batch buffers
     int4* d_chg = nullptr;
     long long chg_cap = 0;
-    long long* d_slot = nullptr;
+    int* d_ins_state = nullptr;
     int4* d_ovf = nullptr;
+    unsigned long long* d_hpair = nullptr;  // deletion set of the batch
+    int* d_hw = nullptr;
+    unsigned long long hcap = 0;
     Ctl* h_ctl = nullptr;  // pinned mirror of the control block
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     unsigned epoch = 0;
@@ -287,35 +289,58 @@ int set_device(const dsssp_graph* g) {
     return DSSSP_OK;
 }
 
-// Heavy-list capacity: (vertex, chunk) items of distinct heavy rows of one step.
-long long heavy_capacity(long long cap_total, const dsssp_opts& o) {
-    long long unit = o.chunk < o.large_deg ? o.chunk : o.large_deg;
-    if (unit < 1) unit = 1;
-    return 2 * (cap_total / unit) + 64;
+// Work-list capacities.  A vertex enters a given list at most once per step (push tags,
+// cut-off tags), so a list holds at most sum_v ceil(deg_v / te) thread items and
+// sum over rows above large_deg of ceil(deg_v / chunk) CTA items.
+long long thread_item_capacity(long long cap_total, long long n, const dsssp_opts& o) {
+    return cap_total / o.small_deg + n + 64;
 }
 
-int ensure_heavy(dsssp_graph* g) {
-    const long long need = heavy_capacity(g->cap_total, g->o);
-    if (g->dg.hcap >= need && g->dg.h0) return DSSSP_OK;
-    dfree(g->dg.h0);
-    dfree(g->dg.h1);
-    int rc = dalloc(&g->dg.h0, (size_t)need, "heavy list");
-    if (!rc) rc = dalloc(&g->dg.h1, (size_t)need, "heavy list");
-    g->dg.hcap = rc ? 0 : need;
+long long cta_item_capacity(long long cap_total, const dsssp_opts& o) {
+    return cap_total / o.chunk + cap_total / (o.large_deg > 0 ? o.large_deg : 1) + 64;
+}
+
+int ensure_work(dsssp_graph* g) {
+    const long long nt = thread_item_capacity(g->cap_total, g->n, g->o);
+    const long long nc = cta_item_capacity(g->cap_total, g->o);
+    DevGraph& d = g->dg;
+    if (d.tcap >= nt && d.ccap >= nc && d.rt0) return DSSSP_OK;
+    dfree(d.rt0); dfree(d.rt1); dfree(d.rc0); dfree(d.rc1); dfree(d.it); dfree(d.ic);
+    d.tcap = d.ccap = 0;
+    int rc = dalloc(&d.rt0, (size_t)nt, "work list");
+    if (!rc) rc = dalloc(&d.rt1, (size_t)nt, "work list");
+    if (!rc) rc = dalloc(&d.it, (size_t)nt, "work list");
+    if (!rc) rc = dalloc(&d.rc0, (size_t)nc, "work list");
+    if (!rc) rc = dalloc(&d.rc1, (size_t)nc, "work list");
+    if (!rc) rc = dalloc(&d.ic, (size_t)nc, "work list");
+    if (!rc) {
+        d.tcap = nt;
+        d.ccap = nc;
+    }
     return rc;
 }
 
 int ensure_batch(dsssp_graph* g, long long k) {
     if (k <= g->chg_cap) return DSSSP_OK;
     long long cap = k + k / 4 + 1024;
+    unsigned long long h = 64;
+    while (h < 2ull * (unsigned long long)cap) h <<= 1;
     dfree(g->d_chg);
-    dfree(g->d_slot);
+    dfree(g->d_ins_state);
     dfree(g->d_ovf);
+    dfree(g->d_hpair);
+    dfree(g->d_hw);
     g->chg_cap = 0;
+    g->hcap = 0;
     int rc = dalloc(&g->d_chg, (size_t)cap, "change buffer");
-    if (!rc) rc = dalloc(&g->d_slot, (size_t)cap * 2, "slot buffer");
+    if (!rc) rc = dalloc(&g->d_ins_state, (size_t)cap, "insertion state");
     if (!rc) rc = dalloc(&g->d_ovf, (size_t)cap * 2, "overflow buffer");
-    if (!rc) g->chg_cap = cap;
+    if (!rc) rc = dalloc(&g->d_hpair, (size_t)h, "deletion set");
+    if (!rc) rc = dalloc(&g->d_hw, (size_t)h, "deletion set");
+    if (!rc) {
+        g->chg_cap = cap;
+        g->hcap = h;
+    }
     return rc;
 }
 
@@ -396,7 +421,7 @@ int layout_rows(dsssp_graph* g, unsigned long long* keys_in, long long total, co
         adj = nullptr;
         g->cap_total = cap_total;
         g->entries = total;
-        rc = ensure_heavy(g);
+        rc = ensure_work(g);
     }
     dfree(cap);
     dfree(start);
@@ -459,9 +484,13 @@ UpdParams make_params(const dsssp_graph* g, const int4* chg, long long k, int mo
     p.g.src = g->src;
     p.chg = chg;
     p.k = k;
-    p.slot = g->d_slot;
+    p.ins_state = g->d_ins_state;
+    p.hpair = g->d_hpair;
+    p.hw = g->d_hw;
+    p.hmask = g->hcap ? g->hcap - 1 : 0;
+    p.ovf = g->d_ovf;
     p.epoch = g->epoch;
-    p.small_deg = g->o.small_deg;
+    p.te = g->o.small_deg;
     p.large_deg = g->o.large_deg;
     p.chunk = g->o.chunk;
     p.bfs_levels = g->o.bfs_levels;
@@ -471,7 +500,7 @@ UpdParams make_params(const dsssp_graph* g, const int4* chg, long long k, int mo
 }
 
 int clear_ctl(dsssp_graph* g, cudaStream_t s) {
-    const size_t off = offsetof(Ctl, status);
+    const size_t off = offsetof(Ctl, status);  // line 1 onwards
     CK(cudaMemsetAsync((char*)g->dg.ctl + off, 0, sizeof(Ctl) - off, s), "control block reset");
     return DSSSP_OK;
 }
@@ -534,27 +563,41 @@ void fill_stats(const dsssp_graph* g, const Ctl& c, dsssp_stats* st, bool events
         if (cudaEventElapsedTime(&b, g->ev[1], g->ev[2]) == cudaSuccess) st->t_update_ms = b;
         if (cudaEventElapsedTime(&t, g->ev[0], g->ev[2]) == cudaSuccess) st->t_total_ms = t;
     }
+    st->n_killed = (int64_t)c.killed;
+    st->work_items = (int64_t)c.stat[ST_ITEMS];
     // algorithmic bytes (byte model: each item is touched once by this algorithm)
+    //   per adjacency entry scanned 16 (entry + neighbour state), per work item 40 (item write
+    //   + read, row descriptor, owner state), per pushed vertex 20 (push tag, degree), per
+    //   distance-lowering atomic 8, per cut-off vertex 12 (state, tag), per insertion seed 24,
+    //   per pointer-jumping pass 12 n
     const double n = (double)g->n;
-    double upd = 16.0 * (double)st->edges_relaxed + 16.0 * (double)st->edges_inval +
-                 28.0 * (double)st->frontier_total + 44.0 * (double)st->n_invalidated +
-                 16.0 * (double)st->updates + 24.0 * (double)st->n_ins;
+    double upd = 16.0 * (double)(st->edges_relaxed + st->edges_inval) + 40.0 * (double)st->work_items +
+                 20.0 * (double)st->frontier_total + 8.0 * (double)st->updates + 12.0 * (double)st->n_invalidated +
+                 24.0 * (double)st->n_ins;
     if (st->pj_passes > 0) upd += n * (12.0 + 12.0 * (double)st->pj_passes);
-    const double front = 16.0 * (double)k + 48.0 * (double)st->n_ins + 56.0 * (double)st->n_del +
+    //   front kernels: 16 per record (read by each of the three), 48 per insertion (two
+    //   descriptor atomics + two entries + hash probe), 56 per deletion (two descriptors, two
+    //   prefix lengths, two states, hash slot) + 8 per probed entry + 16 per root
+    const double front = 48.0 * (double)k + 48.0 * (double)st->n_ins + 56.0 * (double)st->n_del +
                          8.0 * (double)st->del_probed + 16.0 * (double)st->n_roots;
     st->bytes_alg_update = upd;
     st->bytes_alg = upd + front;
 }
 
-// Enqueues one batch (records already on the device).  with_append = false resumes after a
-// repack (insertions were already placed).
-int enqueue_batch(dsssp_graph* g, const int4* d_chg, long long k, cudaStream_t s, bool with_append) {
+// Enqueues one batch (records already on the device).
+int enqueue_batch(dsssp_graph* g, const int4* d_chg, long long k, cudaStream_t s) {
     int rc = clear_ctl(g, s);
     if (rc) return rc;
+    const size_t hb = (size_t)(2ull * (unsigned long long)k);
+    unsigned long long h = 64;
+    while (h < hb) h <<= 1;  // this batch uses the first h slots of the deletion set
+    CK(cudaMemsetAsync(g->d_hpair, 0xFF, sizeof(unsigned long long) * h, s), "deletion set reset");
+    CK(cudaMemsetAsync(g->d_hw, 0x80, sizeof(int) * h, s), "deletion set reset");
     UpdParams p = make_params(g, d_chg, k, 0);
+    p.hmask = h - 1;
     const bool ev = g->o.timing != 0;
     if (ev) CK(cudaEventRecord(g->ev[0], s), "event");
-    CK(launch_front(p, g->d_ovf, with_append, s), "insert/delete kernels");
+    CK(launch_front(p, g->num_sms * 8, s), "insert/delete kernels");
     if (ev) CK(cudaEventRecord(g->ev[1], s), "event");
     CK(launch_update(p, g->coop_grid, g->o.block, s), "update kernel");
     if (ev) CK(cudaEventRecord(g->ev[2], s), "event");
@@ -572,16 +615,17 @@ int finish_batch(dsssp_graph* g, dsssp_stats* st) {
     CK(cudaStreamSynchronize(s), "batch");
     int repacks = 0;
     if (g->h_ctl->status == kStatusOverflowPending) {
-        const Ctl first = *g->h_ctl;
+        // insertions are placed and deletions applied; the rows that ran out of slack are
+        // rebuilt with the overflow entries folded in, then the update kernel runs
         int rc = repack(g, g->d_ovf, g->h_ctl->ovf_count, s);
         if (rc) return rc;
         repacks = 1;
+        CK(cudaMemsetAsync(&g->dg.ctl->status, 0, sizeof(int), s), "status reset");
         UpdParams p = make_params(g, g->pend_chg, g->pend_k, 0);
-        CK(launch_relocate(p, s), "relocate");
-        rc = enqueue_batch(g, g->pend_chg, g->pend_k, s, false);
-        if (rc) return rc;
+        CK(launch_update(p, g->coop_grid, g->o.block, s), "update kernel");
+        CK(cudaMemcpyAsync(g->h_ctl, g->dg.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s), "status read");
         CK(cudaStreamSynchronize(s), "batch");
-        for (int i : {ST_INS, ST_DEL, ST_IGN, ST_OVF}) g->h_ctl->stat[i] = first.stat[i];
+        g->pend_events = false;  // the event interval does not cover the repack
     }
     fill_stats(g, *g->h_ctl, st, g->pend_events, g->pend_k, repacks);
     if (g->h_ctl->status != 0) reset_tags(g, s);
@@ -660,9 +704,10 @@ void dsssp_graph_destroy(dsssp_graph* g) {
     if (g->stream) cudaStreamSynchronize(g->stream);
     DevGraph& d = g->dg;
     dfree(d.state); dfree(d.rows); dfree(d.sorted_len); dfree(d.adj); dfree(d.inv_tag);
-    dfree(d.push_tag); dfree(d.jm); dfree(d.invq); dfree(d.q0); dfree(d.q1); dfree(d.h0); dfree(d.h1);
-    dfree(d.ctl);
-    dfree(g->d_chg); dfree(g->d_slot); dfree(g->d_ovf); dfree(g->d_par); dfree(g->d_dist);
+    dfree(d.push_tag); dfree(d.jm); dfree(d.invq); dfree(d.rt0); dfree(d.rt1); dfree(d.rc0); dfree(d.rc1);
+    dfree(d.it); dfree(d.ic); dfree(d.ctl);
+    dfree(g->d_chg); dfree(g->d_ins_state); dfree(g->d_ovf); dfree(g->d_hpair); dfree(g->d_hw);
+    dfree(g->d_par); dfree(g->d_dist);
     dfree(g->s_state); dfree(g->s_rows); dfree(g->s_sorted); dfree(g->s_adj);
     if (g->h_ctl) cudaFreeHost(g->h_ctl);
     for (auto& e : g->ev)
@@ -672,7 +717,8 @@ void dsssp_graph_destroy(dsssp_graph* g) {
 }
 
 static int check_opts(const dsssp_opts& o) {
-    if (o.slack_pct < 0 || o.slack_min < 0 || o.small_deg < 0 || o.large_deg < o.small_deg || o.chunk < 32 ||
+    if (o.slack_pct < 0 || o.slack_min < 0 || o.small_deg < 4 || o.small_deg > 64 || o.small_deg % 4 ||
+        o.large_deg < o.small_deg || o.chunk < 32 ||
         o.bfs_levels < 0 || o.block < 32 || o.block > 256 || o.block % 32 || o.ctas_per_sm < 0 || o.max_rounds < 0)
         return fail(DSSSP_E_INVAL, "invalid dsssp_opts");
     return DSSSP_OK;
@@ -728,8 +774,6 @@ int dsssp_graph_create(int32_t n, int64_t m, const int32_t* u, const int32_t* v,
     if (!rc) rc = dalloc(&d.push_tag, N, "push_tag");
     if (!rc) rc = dalloc(&d.jm, N, "jm");
     if (!rc) rc = dalloc(&d.invq, N, "invq");
-    if (!rc) rc = dalloc(&d.q0, N, "frontier");
-    if (!rc) rc = dalloc(&d.q1, N, "frontier");
     if (!rc) rc = dalloc(&d.ctl, 1, "control block");
     if (rc) { dsssp_graph_destroy(g); return rc; }
     cudaStream_t s = g->stream;
@@ -799,8 +843,9 @@ int dsssp_graph_info(const dsssp_graph* g, int64_t* n, int64_t* entries, int64_t
     if (source) *source = g->src;
     if (device_bytes) {
         const long long N = g->n;
-        long long b = N * (8 + 16 + 4 + 4 + 4 + 4 + 4 + 4 + 4) + g->cap_total * 8 + 2 * g->dg.hcap * 8 +
-                      g->chg_cap * (16 + 16 + 32) + (long long)sizeof(Ctl);
+        long long b = N * (8 + 16 + 4 + 4 + 4 + 4 + 4) + g->cap_total * 8 + 3 * g->dg.tcap * 8 +
+                      3 * g->dg.ccap * 8 + g->chg_cap * (16 + 4 + 32) + (long long)g->hcap * 12 +
+                      (long long)sizeof(Ctl);
         if (g->d_par) b += N * 12;
         if (g->has_snap) b += N * (8 + 16 + 4) + g->s_cap * 8;
         *device_bytes = b;
@@ -903,7 +948,7 @@ int dsssp_apply_batch_async(dsssp_graph* g, const dsssp_change* d_changes, int64
     if (k == 0) return DSSSP_OK;
     rc = ensure_batch(g, k);
     if (!rc) rc = next_epoch(g, s);
-    if (!rc) rc = enqueue_batch(g, (const int4*)d_changes, k, s, true);
+    if (!rc) rc = enqueue_batch(g, (const int4*)d_changes, k, s);
     if (rc) return rc;
     g->pending = true;
     g->pend_k = k;
@@ -977,7 +1022,7 @@ int dsssp_graph_restore(dsssp_graph* g, void* stream) {
         rc = dalloc(&g->dg.adj, (size_t)g->s_cap, "adjacency");
         if (rc) return rc;
         g->cap_total = g->s_cap;
-        rc = ensure_heavy(g);
+        rc = ensure_work(g);
         if (rc) return rc;
     }
     const size_t N = (size_t)g->n;

@@ -2,24 +2,30 @@
 //
 // One batch (replaces SSSPmainForUndirected.cu:196-281) is four launches on one stream:
 //   k_prepare   validate and count the change records
-//   k_append    insertions go into row slack (atomic degree bump), both directions
-//               (replaces the host-side append of all_structure_undir.cuh:106-117)
-//   k_delete    every adjacency entry matching a deletion is tombstoned (binary search in
-//               the sorted row prefix + scan of the appended tail) and the child end of a
-//               deleted tree edge is cut off (replaces deleteEdge, gpuFunctions_undir.cuh:179-215)
+//   k_delete    the child end of a deleted tree edge is cut off and every adjacency entry
+//               matching a deletion is tombstoned (binary search in the sorted row prefix +
+//               scan of older appended entries); deletions also go into a device hash set
+//               (replaces deleteEdge, gpuFunctions_undir.cuh:179-215)
+//   k_append    insertions that no deletion of the batch removes go into row slack (atomic
+//               degree bump, both directions).  The reference appends every insertion and
+//               then tombstones matches (all_structure_undir.cuh:106-117 before
+//               gpuFunctions_undir.cuh:201-213); skipping the removed ones gives the same graph.
 //   k_update    one persistent cooperative kernel with a bounded grid barrier:
-//               A. cut-off subtrees are walked level by level from the cut-off roots
-//                  (replaces filterAffectedNodes + updateNeighbors_del and its host loop,
-//                  gpuFunctions_undir.cuh:125-144, 312-349, MAIN:219-239); after
-//                  bfs_levels levels it switches to pointer jumping over the parent array
+//               A. cut-off subtrees are walked level by level from the roots (replaces
+//                  filterAffectedNodes + updateNeighbors_del and its host loop,
+//                  gpuFunctions_undir.cuh:125-144, 312-349, MAIN:219-239); after bfs_levels
+//                  levels it switches to pointer jumping over the parent array
 //               B. surviving insertions relax their endpoints (replaces insertEdge,
 //                  gpuFunctions_undir.cuh:217-251) and every cut-off vertex pulls its best
 //                  live neighbour
-//               C. frontier relaxation rounds with degree buckets (thread / warp per vertex,
-//                  CTA per chunk for heavy rows) and 64-bit atomicMin on the packed
+//               C. frontier relaxation rounds with 64-bit atomicMin on the packed
 //                  (dist, parent) word until the frontier is empty (replaces
 //                  filterAllAffected + updateNeighbors and its host loop,
 //                  gpuFunctions_undir.cuh:162-174, 370-433, MAIN:263-281)
+// Load balance: a vertex entering a frontier is split by degree into work items -- rows of
+// at most te edges are one thread's item, longer rows up to large_deg become ceil(deg/te)
+// thread items (a warp's worth for a few hundred edges), longer ones become CTA items of
+// `chunk` edges -- so every round is one even wave over all threads.
 #include <cuda_runtime.h>
 
 #include "engine.cuh"
@@ -30,16 +36,20 @@ namespace {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr unsigned kSpinLimit = 1u << 24;  // x ~200 ns sleeps: a barrier gives up after ~3 s
+constexpr int kMaxWarps = 8;               // update kernel blocks have at most 256 threads
+constexpr int kBuf = 160;                  // per-warp push buffer, flushed at >= 32 entries
 
 __shared__ unsigned s_nbar;  // grid barriers this CTA has passed
+__shared__ unsigned s_pbuf[kMaxWarps][kBuf];
 
 struct LocalStats {
-    unsigned long long edges_relax = 0, edges_inv = 0, updates = 0, dist_ovf = 0;
+    unsigned long long edges_relax = 0, edges_inv = 0, updates = 0, dist_ovf = 0, frontier = 0, items = 0,
+                       marked = 0;
 };
 
 // Grid-wide barrier for a cooperative launch.  The wait is bounded: on timeout the status
-// word gets DSSSP_E_TIMEOUT and every CTA leaves at its next barrier.  Returns false when
-// the kernel must stop (timeout or any error status).
+// word gets DSSSP_E_TIMEOUT (with where it happened in ctl->diag) and every CTA leaves at
+// its next barrier.  Returns false when the kernel must stop (timeout or any error).
 __device__ bool grid_sync(Ctl* ctl) {
     __shared__ int s_go;
     __syncthreads();
@@ -65,8 +75,8 @@ __device__ bool grid_sync(Ctl* ctl) {
                 __nanosleep(spins < 32 ? 32 : 200);
             }
         }
-        s_nbar++;
         __threadfence();
+        s_nbar++;
         s_go = __ldcg(&ctl->status) == 0;
     }
     __syncthreads();
@@ -108,30 +118,76 @@ __device__ __forceinline__ bool relax_to(unsigned long long* state, unsigned c, 
     return false;
 }
 
+// Destination of pushed vertices: a thread-item list and a CTA-item list with counters.
+struct Out {
+    uint2* tl;
+    unsigned* tcnt;
+    long long tcap;
+    uint2* cl;
+    unsigned* ccnt;
+    long long ccap;
+};
+
+// Splits the vertex each lane holds into work items (warp-collective).
+__device__ __forceinline__ void expand(bool valid, unsigned v, const UpdParams& p, const Out& o, LocalStats& ls) {
+    const int deg = valid ? p.g.rows[v].deg : 0;
+    const bool heavy = deg > p.large_deg;
+    const unsigned nt = (!heavy && deg > 0) ? (unsigned)((deg + p.te - 1) / p.te) : 0u;
+    const unsigned nc = heavy ? (unsigned)((deg + p.chunk - 1) / p.chunk) : 0u;
+    const bool ok1 = warp_append_chunks(v, nt, o.tl, o.tcnt, o.tcap);
+    const bool ok2 = warp_append_chunks(v, nc, o.cl, o.ccnt, o.ccap);
+    if (!(ok1 && ok2) && lane_id() == 0) set_status(p.g.ctl, -4 /* work list capacity: internal error */);
+    ls.items += nt + nc;
+}
+
+// Per-warp shared-memory buffer of pushed vertices; expanded into items 32 at a time.
+struct PushBuf {
+    unsigned* buf;
+    int count;  // warp-uniform
+
+    __device__ __forceinline__ void add(bool pred, unsigned v) {
+        const unsigned mask = __ballot_sync(kFull, pred);
+        if (pred) buf[count + __popc(mask & ((1u << lane_id()) - 1u))] = v;
+        count += __popc(mask);
+        __syncwarp();
+    }
+
+    __device__ __forceinline__ void flush(const UpdParams& p, const Out& o, LocalStats& ls, bool all) {
+        while (count >= 32 || (all && count > 0)) {
+            const int take = count < 32 ? count : 32;
+            const bool has = (int)lane_id() < take;
+            const unsigned v = has ? buf[count - take + (int)lane_id()] : 0u;
+            __syncwarp();
+            count -= take;
+            expand(has, v, p, o, ls);
+        }
+    }
+};
+
 // ---- per-edge operations ---------------------------------------------------------------
 // visit4 handles up to four adjacency entries per lane and is called by all 32 lanes.
 
 struct RelaxOp {
-    unsigned long long* state;
-    const int2* adj;
-    unsigned* push_tag;
+    const UpdParams* p;
     unsigned tag;
-    unsigned* qout;
-    unsigned* qcnt;
+    Out out;
+    PushBuf pb;
     LocalStats* ls;
 
-    __device__ __forceinline__ unsigned long long prep(unsigned v) const { return __ldcg(&state[v]) >> 32; }
+    __device__ __forceinline__ unsigned long long prep(unsigned v) const { return __ldcg(&p->g.state[v]) >> 32; }
     __device__ __forceinline__ bool skip(unsigned long long du) const { return du >= kDistInf; }
     __device__ __forceinline__ void begin_lane(unsigned) {}
     __device__ __forceinline__ void end_lane(unsigned, bool) {}
-    __device__ __forceinline__ void begin_warp(unsigned) {}
-    __device__ __forceinline__ void end_warp(unsigned) {}
+    __device__ __forceinline__ void begin_group(unsigned) {}
+    __device__ __forceinline__ void end_group(unsigned) {}
+    __device__ __forceinline__ void finish() { pb.flush(*p, out, *ls, true); }
 
     __device__ __forceinline__ void visit4(unsigned u, unsigned long long du, const long long (&j)[4],
                                            const bool (&ok)[4]) {
+        unsigned long long* state = p->g.state;
         int2 e[4];
 #pragma unroll
-        for (int q = 0; q < 4; q++) e[q] = ok[q] ? __ldg(&adj[j[q]]) : make_int2(0, -1);
+        for (int q = 0; q < 4; q++) e[q] = ok[q] ? __ldg(&p->g.adj[j[q]]) : make_int2(0, -1);
         unsigned long long cur[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) cur[q] = e[q].y >= 0 ? __ldcg(&state[e[q].x]) : 0ull;
@@ -139,34 +195,35 @@ struct RelaxOp {
         for (int q = 0; q < 4; q++) {
             bool push = false;
             if (e[q].y >= 0) push = relax_to(state, (unsigned)e[q].x, du + (unsigned)e[q].y, u, e[q].y, cur[q], *ls);
-            const bool doit = push && claim_push(push_tag, (unsigned)e[q].x, tag);
-            warp_append(doit, (unsigned)e[q].x, qout, qcnt);
+            const bool doit = push && claim_push(p->g.push_tag, (unsigned)e[q].x, tag);
+            ls->frontier += doit ? 1 : 0;
+            pb.add(doit, (unsigned)e[q].x);
             ls->edges_relax += ok[q] ? 1 : 0;
         }
+        pb.flush(*p, out, *ls, false);
     }
 };
 
 struct MarkOp {
-    unsigned long long* state;
-    const int2* adj;
-    unsigned* inv_tag;
-    unsigned epoch;
-    unsigned* invq;
-    unsigned* inv_count;
+    const UpdParams* p;
+    Out out;
+    PushBuf pb;
     LocalStats* ls;
 
     __device__ __forceinline__ unsigned long long prep(unsigned) const { return 0; }
     __device__ __forceinline__ bool skip(unsigned long long) const { return false; }
     __device__ __forceinline__ void begin_lane(unsigned) {}
     __device__ __forceinline__ void end_lane(unsigned, bool) {}
-    __device__ __forceinline__ void begin_warp(unsigned) {}
-    __device__ __forceinline__ void end_warp(unsigned) {}
+    __device__ __forceinline__ void begin_group(unsigned) {}
+    __device__ __forceinline__ void end_group(unsigned) {}
+    __device__ __forceinline__ void finish() { pb.flush(*p, out, *ls, true); }
 
     __device__ __forceinline__ void visit4(unsigned x, unsigned long long, const long long (&j)[4],
                                            const bool (&ok)[4]) {
+        unsigned long long* state = p->g.state;
         int2 e[4];
 #pragma unroll
-        for (int q = 0; q < 4; q++) e[q] = ok[q] ? __ldg(&adj[j[q]]) : make_int2(0, -1);
+        for (int q = 0; q < 4; q++) e[q] = ok[q] ? __ldg(&p->g.adj[j[q]]) : make_int2(0, -1);
         unsigned long long s[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) s[q] = e[q].y >= 0 ? __ldcg(&state[e[q].x]) : kInfState;
@@ -174,21 +231,21 @@ struct MarkOp {
         for (int q = 0; q < 4; q++) {
             const unsigned c = (unsigned)e[q].x;
             bool mark = e[q].y >= 0 && (unsigned)s[q] == x;
-            if (mark) mark = atomicExch(&inv_tag[c], epoch) != epoch;
+            if (mark) mark = atomicExch(&p->g.inv_tag[c], p->epoch) != p->epoch;
             if (mark) state[c] = kInfState;
-            warp_append(mark, c, invq, inv_count);
+            ls->marked += mark ? 1 : 0;
+            pb.add(mark, c);
             ls->edges_inv += ok[q] ? 1 : 0;
         }
+        pb.flush(*p, out, *ls, false);
     }
 };
 
 struct PullOp {
-    unsigned long long* state;
-    const int2* adj;
-    unsigned* push_tag;
+    const UpdParams* p;
     unsigned tag;
-    unsigned* qout;
-    unsigned* qcnt;
+    Out out;
+    PushBuf pb;
     LocalStats* ls;
     unsigned long long best;
     bool need;
@@ -196,13 +253,15 @@ struct PullOp {
     __device__ __forceinline__ unsigned long long prep(unsigned) const { return 0; }
     __device__ __forceinline__ bool skip(unsigned long long) const { return false; }
     __device__ __forceinline__ void begin_lane(unsigned) { best = kInfState; need = false; }
-    __device__ __forceinline__ void begin_warp(unsigned) { best = kInfState; need = false; }
+    __device__ __forceinline__ void begin_group(unsigned) { best = kInfState; need = false; }
+    __device__ __forceinline__ void finish() { pb.flush(*p, out, *ls, true); }
 
     __device__ __forceinline__ void visit4(unsigned x, unsigned long long, const long long (&j)[4],
                                            const bool (&ok)[4]) {
+        unsigned long long* state = p->g.state;
         int2 e[4];
 #pragma unroll
-        for (int q = 0; q < 4; q++) e[q] = ok[q] ? __ldg(&adj[j[q]]) : make_int2(0, -1);
+        for (int q = 0; q < 4; q++) e[q] = ok[q] ? __ldg(&p->g.adj[j[q]]) : make_int2(0, -1);
         unsigned long long s[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) s[q] = e[q].y >= 0 ? __ldcg(&state[e[q].x]) : kInfState;
@@ -223,157 +282,128 @@ struct PullOp {
             }
         }
     }
-    // flush of one lane's own vertex
+    // a lane's own item
     __device__ __forceinline__ void end_lane(unsigned x, bool valid) {
         bool improved = false;
         if (valid && best != kInfState) {
-            const unsigned long long old = atomicMin(&state[x], best);
+            const unsigned long long old = atomicMin(&p->g.state[x], best);
             if ((old >> 32) > (best >> 32)) {
                 improved = true;
                 ls->updates++;
             }
         }
-        const bool doit = valid && (need || improved) && claim_push(push_tag, x, tag);
-        warp_append(doit, x, qout, qcnt);
+        const bool doit = valid && (need || improved) && claim_push(p->g.push_tag, x, tag);
+        ls->frontier += doit ? 1 : 0;
+        pb.add(doit, x);
+        pb.flush(*p, out, *ls, false);
     }
-    // flush of a vertex shared by the warp
-    __device__ __forceinline__ void end_warp(unsigned x) {
+    // an item shared by the warp (part of a CTA item)
+    __device__ __forceinline__ void end_group(unsigned x) {
         const unsigned long long b = warp_min_u64(best);
         const bool nd = __any_sync(kFull, need);
         bool improved = false;
         if (lane_id() == 0 && b != kInfState) {
-            const unsigned long long old = atomicMin(&state[x], b);
+            const unsigned long long old = atomicMin(&p->g.state[x], b);
             if ((old >> 32) > (b >> 32)) {
                 improved = true;
                 ls->updates++;
             }
         }
-        const bool doit = lane_id() == 0 && (nd || improved) && claim_push(push_tag, x, tag);
-        warp_append(doit, x, qout, qcnt);
+        const bool doit = lane_id() == 0 && (nd || improved) && claim_push(p->g.push_tag, x, tag);
+        ls->frontier += doit ? 1 : 0;
+        pb.add(doit, x);
+        pb.flush(*p, out, *ls, false);
     }
 };
 
-// ---- granularities ---------------------------------------------------------------------
-
+// Processes one step's work: CTA items (one CTA per chunk of a long row), then thread
+// items (te edges each) in one grid-stride wave.
 template <class Op>
-__device__ __forceinline__ void lane_row(Op& op, unsigned v, unsigned long long du, long long start, int deg,
-                                         int maxd, bool valid) {
-    op.begin_lane(v);
-    for (int b = 0; b < maxd; b += 4) {
-        long long j[4];
-        bool ok[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            ok[q] = b + q < deg;
-            j[q] = start + b + q;
-        }
-        op.visit4(v, du, j, ok);
-    }
-    op.end_lane(v, valid);
-}
-
-template <class Op>
-__device__ __forceinline__ void warp_row(Op& op, unsigned v, unsigned long long du, long long start, int deg) {
-    const int lane = (int)lane_id();
-    op.begin_warp(v);
-    for (int b = 0; b < deg; b += 128) {
-        long long j[4];
-        bool ok[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const int idx = b + q * 32 + lane;
-            ok[q] = idx < deg;
-            j[q] = start + idx;
-        }
-        op.visit4(v, du, j, ok);
-    }
-    op.end_warp(v);
-}
-
-template <class Op>
-__device__ __forceinline__ void cta_chunk(Op& op, unsigned v, unsigned long long du, long long start, int deg,
-                                          unsigned chunk_id, int chunk) {
-    const long long lo = (long long)chunk_id * chunk;
-    const long long hi = min((long long)deg, lo + chunk);
-    op.begin_warp(v);
-    for (long long b = lo; b < hi; b += 4LL * blockDim.x) {
-        long long j[4];
-        bool ok[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const long long idx = b + (long long)q * blockDim.x + threadIdx.x;
-            ok[q] = idx < hi;
-            j[q] = start + idx;
-        }
-        op.visit4(v, du, j, ok);
-    }
-    op.end_warp(v);
-}
-
-// Processes a work list with degree buckets: heavy vertices handed over by the previous
-// step (CTA per chunk), then the light items 32 per warp -- degree <= small_deg one thread
-// each, up to large_deg one warp each; heavier ones go to heavy_out for the next step.
-template <class Op>
-__device__ void run_items(Op& op, const UpdParams& p, const unsigned* items, unsigned count,
-                          const uint2* heavy, unsigned hcount, uint2* heavy_out,
-                          unsigned* heavy_out_cnt) {
+__device__ void run_items(Op& op, const UpdParams& p, const uint2* tl, unsigned nt, const uint2* cl, unsigned nc) {
     const RowDesc* rows = p.g.rows;
     const unsigned lane = lane_id();
-    const unsigned gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
-    // heavy rows handed over by the previous step: one CTA per (vertex, chunk) item
-    for (unsigned t = blockIdx.x; t < hcount; t += gridDim.x) {
-        const uint2 it = __ldcg(&heavy[t]);
+    const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned nthreads = gridDim.x * blockDim.x;
+    for (unsigned t = blockIdx.x; t < nc; t += gridDim.x) {
+        const uint2 it = __ldcg(&cl[t]);
         const RowDesc rd = rows[it.x];
         const unsigned long long du = __shfl_sync(kFull, op.prep(it.x), 0);
-        if (!op.skip(du)) cta_chunk(op, it.x, du, rd.start, rd.deg, it.y, p.chunk);
+        if (op.skip(du)) continue;
+        const long long lo = (long long)it.y * p.chunk;
+        const long long hi = min((long long)rd.deg, lo + p.chunk);
+        op.begin_group(it.x);
+        for (long long b = lo; b < hi; b += 4LL * blockDim.x) {
+            long long j[4];
+            bool ok[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const long long idx = b + (long long)q * blockDim.x + threadIdx.x;
+                ok[q] = idx < hi;
+                j[q] = rd.start + idx;
+            }
+            op.visit4(it.x, du, j, ok);
+        }
+        op.end_group(it.x);
     }
-    for (unsigned base = gwarp * 32; base < count; base += nwarps * 32) {
+    for (unsigned base = gtid - lane; base < nt; base += nthreads) {
         const unsigned i = base + lane;
-        const bool has = i < count;
-        const unsigned v = has ? __ldcg(&items[i]) : 0u;
+        const bool has = i < nt;
+        const uint2 it = has ? __ldcg(&tl[i]) : make_uint2(0u, 0u);
         RowDesc rd;
         rd.start = 0;
         rd.deg = 0;
         rd.cap = 0;
-        if (has) rd = rows[v];
-        const unsigned long long du = has ? op.prep(v) : kDistInf;
-        const bool live = has && !op.skip(du) && rd.deg > 0;
-        const int deg = live ? rd.deg : 0;
-        const bool is_small = live && deg <= p.small_deg;
-        const bool is_heavy = live && deg > p.large_deg;
-        const unsigned nch = is_heavy ? (unsigned)((deg + p.chunk - 1) / p.chunk) : 0u;
-        if (!warp_append_chunks(is_heavy, v, nch, heavy_out, heavy_out_cnt, p.g.hcap) && lane == 0)
-            set_status(p.g.ctl, -4 /* heavy list capacity: internal error */);
-        const int sdeg = is_small ? deg : 0;
-        const int maxd = (int)__reduce_max_sync(kFull, (unsigned)sdeg);
-        if (maxd > 0) lane_row(op, v, du, rd.start, sdeg, maxd, is_small);
-        unsigned mm = __ballot_sync(kFull, live && !is_small && !is_heavy);
-        while (mm) {
-            const int l = __ffs(mm) - 1;
-            mm &= mm - 1;
-            const unsigned vv = __shfl_sync(kFull, v, l);
-            const long long st = __shfl_sync(kFull, rd.start, l);
-            const int dg = __shfl_sync(kFull, deg, l);
-            const unsigned long long dd = __shfl_sync(kFull, du, l);
-            warp_row(op, vv, dd, st, dg);
+        if (has) rd = rows[it.x];
+        const unsigned long long du = has ? op.prep(it.x) : kDistInf;
+        const bool live = has && !op.skip(du);
+        const long long lo = (long long)it.y * p.te;
+        const long long hi = live ? min((long long)rd.deg, lo + p.te) : lo;
+        op.begin_lane(it.x);
+        for (int b = 0; b < p.te; b += 4) {
+            long long j[4];
+            bool ok[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const long long idx = lo + b + q;
+                ok[q] = idx < hi;
+                j[q] = rd.start + idx;
+            }
+            op.visit4(it.x, du, j, ok);
         }
+        op.end_lane(it.x, live);
     }
+    op.finish();
 }
 
+// Block-reduced statistics: one atomic per block and counter.
 __device__ void flush_stats(Ctl* ctl, const LocalStats& ls) {
-    unsigned long long v[4] = {ls.edges_relax, ls.edges_inv, ls.updates, ls.dist_ovf};
-    const int idx[4] = {ST_EDGES_RELAX, ST_EDGES_INV, ST_UPDATES, ST_DIST_OVF};
+    __shared__ unsigned long long s_acc[7];
+    if (threadIdx.x < 7) s_acc[threadIdx.x] = 0;
+    __syncthreads();
+    const unsigned long long v[7] = {ls.edges_relax, ls.edges_inv, ls.updates, ls.dist_ovf,
+                                     ls.frontier, ls.items, ls.marked};
 #pragma unroll
-    for (int s = 0; s < 4; s++) {
-        unsigned long long x = v[s];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
-        if (lane_id() == 0 && x) atomicAdd(&ctl->stat[idx[s]], x);
+    for (int s = 0; s < 7; s++) {
+        const unsigned long long x = warp_sum_u64(v[s]);
+        if (lane_id() == 0 && x) atomicAdd(&s_acc[s], x);
     }
+    __syncthreads();
+    const int idx[7] = {ST_EDGES_RELAX, ST_EDGES_INV, ST_UPDATES, ST_DIST_OVF, ST_FRONTIER, ST_ITEMS, ST_INV};
+    if (threadIdx.x < 7 && s_acc[threadIdx.x]) atomicAdd(&ctl->stat[idx[threadIdx.x]], s_acc[threadIdx.x]);
 }
 
-// ---- row search -------------------------------------------------------------------------
+__device__ void block_add(unsigned long long* dst, unsigned long long x) {
+    __shared__ unsigned long long s_sum;
+    __syncthreads();
+    if (threadIdx.x == 0) s_sum = 0;
+    __syncthreads();
+    x = warp_sum_u64(x);
+    if (lane_id() == 0 && x) atomicAdd(&s_sum, x);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_sum) atomicAdd(dst, s_sum);
+}
+
+// ---- row search and the deletion set -------------------------------------------------------
 
 // First index in adj[lo, hi) whose column is >= c (the prefix is sorted by column).
 __device__ __forceinline__ long long lower_col(const int2* adj, long long lo, long long hi, int c) {
@@ -385,77 +415,72 @@ __device__ __forceinline__ long long lower_col(const int2* adj, long long lo, lo
     return lo;
 }
 
+// Inserts (pair, w) into the open-addressing deletion set.  Probing depends only on the pair;
+// a slot whose pair matches but whose weight is taken by another weight is skipped.
+__device__ bool hash_insert(const UpdParams& p, unsigned long long pair, int w) {
+    unsigned long long h = dmix64(pair) & p.hmask;
+    for (unsigned long long probe = 0; probe <= p.hmask; probe++) {
+        const unsigned long long old = atomicCAS(&p.hpair[h], kHashEmpty, pair);
+        if (old == kHashEmpty || old == pair) {
+            const int ow = atomicCAS(&p.hw[h], kHashNoWeight, w);
+            if (ow == kHashNoWeight || ow == w) return true;
+        }
+        h = (h + 1) & p.hmask;
+    }
+    return false;
+}
+
+__device__ bool hash_contains(const UpdParams& p, unsigned long long pair, int w) {
+    unsigned long long h = dmix64(pair) & p.hmask;
+    for (unsigned long long probe = 0; probe <= p.hmask; probe++) {
+        const unsigned long long k = p.hpair[h];
+        if (k == kHashEmpty) return false;
+        if (k == pair && p.hw[h] == w) return true;
+        h = (h + 1) & p.hmask;
+    }
+    return false;
+}
+
 }  // namespace
 
 // ---- kernels -----------------------------------------------------------------------------
 
 __global__ void k_prepare(UpdParams p) {
     Ctl* ctl = p.g.ctl;
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned ins = 0, del = 0, ign = 0;
-    if (i < p.k) {
+    unsigned long long ins = 0, del = 0, ign = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.k;
+         i += (long long)gridDim.x * blockDim.x) {
         const int4 c = p.chg[i];
         if (c.w == 1 || c.w == 0) {
             if (c.x < 0 || c.x >= p.g.n || c.y < 0 || c.y >= p.g.n) set_status(ctl, -3 /* BAD_VERTEX */);
             else if (c.w == 1 && c.z < 0) set_status(ctl, -10 /* BAD_WEIGHT */);
-            if (c.w == 1) ins = 1;
-            else del = 1;
+            if (c.w == 1) ins++;
+            else del++;
         } else {
-            ign = 1;
+            ign++;
         }
     }
-    ins = __reduce_add_sync(kFull, ins);
-    del = __reduce_add_sync(kFull, del);
-    ign = __reduce_add_sync(kFull, ign);
-    if (lane_id() == 0) {
-        if (ins) atomicAdd(&ctl->stat[ST_INS], ins);
-        if (del) atomicAdd(&ctl->stat[ST_DEL], del);
-        if (ign) atomicAdd(&ctl->stat[ST_IGN], ign);
-    }
+    block_add(&ctl->stat[ST_INS], ins);
+    block_add(&ctl->stat[ST_DEL], del);
+    block_add(&ctl->stat[ST_IGN], ign);
 }
 
-// Insertions: both directions go into row slack.  An entry that does not fit is written to
-// the overflow list and the batch is deferred to a host-side repack (status 1).
-__global__ void k_append(UpdParams p, int4* ovf) {
-    Ctl* ctl = p.g.ctl;
-    if (__ldcg(&ctl->status) < 0) return;
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.k) return;
-    const int4 c = p.chg[i];
-    if (c.w != 1) return;
-    long long* slot = const_cast<long long*>(p.slot);
-#pragma unroll
-    for (int side = 0; side < 2; side++) {
-        const int r = side ? c.y : c.x, col = side ? c.x : c.y;
-        RowDesc* rd = &p.g.rows[r];
-        const int pos = atomicAdd(&rd->deg, 1);
-        if (pos < rd->cap) {
-            const long long at = rd->start + pos;
-            p.g.adj[at] = make_int2(col, c.z);
-            slot[2 * i + side] = at;
-        } else {
-            const int o = atomicAdd(&ctl->ovf_count, 1);
-            ovf[o] = make_int4(r, col, c.z, (int)i);
-            slot[2 * i + side] = -1;
-            atomicAdd(&ctl->stat[ST_OVF], 1ull);
-            atomicCAS(&ctl->status, 0, kStatusOverflowPending);
-        }
-    }
-}
-
-// Deletions: cut off the child end of a deleted tree edge, tombstone every matching entry.
+// Deletions: cut off the child end of a deleted tree edge, tombstone every matching entry,
+// record the deletion in the batch's deletion set.
 __global__ void k_delete(UpdParams p) {
     Ctl* ctl = p.g.ctl;
-    if (__ldcg(&ctl->status) != 0) return;
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    bool cut = false;
-    unsigned cutv = 0;
-    unsigned long long probed = 0;
-    if (i < p.k) {
-        const int4 c = p.chg[i];
+    if (__ldcg(&ctl->status) != 0) return;  // set by k_prepare: same for every thread
+    const unsigned lane = lane_id();
+    const long long nthreads = (long long)gridDim.x * blockDim.x;
+    unsigned long long probed = 0, roots = 0;
+    for (long long base = (long long)blockIdx.x * blockDim.x + threadIdx.x - lane; base < p.k; base += nthreads) {
+        const long long i = base + lane;
+        const int4 c = i < p.k ? p.chg[i] : make_int4(0, 0, 0, -1);
+        bool cut = false;
+        unsigned cutv = 0;
         if (c.w == 0) {
             const unsigned a = (unsigned)c.x, b = (unsigned)c.y;
-            // gpuFunctions_undir.cuh:189-198: child end first checked as b, then as a
+            // gpuFunctions_undir.cuh:189-198: the child end is checked as b first, then as a
             if (b != (unsigned)p.g.src && (unsigned)__ldcg(&p.g.state[b]) == a) cutv = b, cut = true;
             else if (a != (unsigned)p.g.src && (unsigned)__ldcg(&p.g.state[a]) == b) cutv = a, cut = true;
             if (cut) {
@@ -474,37 +499,52 @@ __global__ void k_delete(UpdParams p) {
                 for (j = sl; j < end; j++, probed++)
                     if (p.g.adj[j].x == col && p.g.adj[j].y == c.z) p.g.adj[j].y = -1;
             }
+            if (c.z >= 0 && !hash_insert(p, dpair_key(a, b), c.z)) set_status(ctl, -4 /* deletion set full */);
         }
+        warp_append(cut, cutv, p.g.invq, &ctl->inv_count);
+        roots += cut ? 1 : 0;
     }
-    warp_append(cut, cutv, p.g.invq, &ctl->inv_count);
-    const unsigned nc = __popc(__ballot_sync(kFull, cut));
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) probed += __shfl_xor_sync(kFull, probed, o);
-    if (lane_id() == 0) {
-        if (nc) atomicAdd(&ctl->stat[ST_ROOTS], (unsigned long long)nc);
-        if (probed) atomicAdd(&ctl->stat[ST_DEL_PROBED], probed);
-    }
+    block_add(&ctl->stat[ST_ROOTS], roots);
+    block_add(&ctl->stat[ST_DEL_PROBED], probed);
 }
 
-// After a repack: point each insertion's slots at an entry (col, w) of its two rows.
-__global__ void k_relocate(UpdParams p) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.k) return;
-    const int4 c = p.chg[i];
-    if (c.w != 1) return;
-    long long* slot = const_cast<long long*>(p.slot);
+// Insertions that no deletion of the batch removes go into row slack, both directions.  An
+// entry that does not fit is written to the overflow list and the batch is deferred to a
+// host-side repack (status 1).
+__global__ void k_append(UpdParams p) {
+    Ctl* ctl = p.g.ctl;
+    if (__ldcg(&ctl->status) < 0) return;  // same for every thread
+    unsigned long long killed = 0, ovf = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.k;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int4 c = p.chg[i];
+        int alive = 0;
+        if (c.w == 1) {
+            if (hash_contains(p, dpair_key((unsigned)c.x, (unsigned)c.y), c.z)) {
+                killed++;
+            } else {
+                alive = 1;
 #pragma unroll
-    for (int side = 0; side < 2; side++) {
-        const int r = side ? c.y : c.x, col = side ? c.x : c.y;
-        const RowDesc rd = p.g.rows[r];
-        const long long sl = rd.start + p.g.sorted_len[r], end = rd.start + rd.deg;
-        long long j = lower_col(p.g.adj, rd.start, sl, col), at = -1;
-        for (; j < sl && p.g.adj[j].x == col && at < 0; j++)
-            if (p.g.adj[j].y == c.z) at = j;
-        for (j = sl; j < end && at < 0; j++)
-            if (p.g.adj[j].x == col && p.g.adj[j].y == c.z) at = j;
-        slot[2 * i + side] = at;
+                for (int side = 0; side < 2; side++) {
+                    const int r = side ? c.y : c.x, col = side ? c.x : c.y;
+                    RowDesc* rd = &p.g.rows[r];
+                    const int pos = atomicAdd(&rd->deg, 1);
+                    if (pos < rd->cap) {
+                        p.g.adj[rd->start + pos] = make_int2(col, c.z);
+                    } else {
+                        const int o = atomicAdd(&ctl->ovf_count, 1);
+                        p.ovf[o] = make_int4(r, col, c.z, (int)i);
+                        ovf++;
+                        atomicCAS(&ctl->status, 0, kStatusOverflowPending);
+                    }
+                }
+            }
+        }
+        p.ins_state[i] = alive;
     }
+    block_add(&ctl->stat[ST_OVF], ovf);
+    unsigned long long kk = warp_sum_u64(killed);
+    if (lane_id() == 0 && kk) atomicAdd(&ctl->killed, (unsigned)kk);
 }
 
 __device__ void update_body(UpdParams& p);
@@ -531,6 +571,7 @@ __device__ void update_body(UpdParams& p) {
     const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned nthreads = gridDim.x * blockDim.x;
     const bool leader = gtid == 0;
+    unsigned* pbuf = s_pbuf[threadIdx.x >> 5];
     LocalStats ls;
     if (leader) ctl->ts[0] = globaltimer();
 
@@ -540,40 +581,55 @@ __device__ void update_body(UpdParams& p) {
         if (!grid_sync(ctl)) return;
         rbase = 1;
     }
+    const unsigned tag0 = rbase + 1;
+    const Out relax0{g.rt0, &ctl->rcT[0], g.tcap, g.rc0, &ctl->rcC[0], g.ccap};
 
     if (p.mode == 1) {
-        if (leader) {
-            g.q0[0] = (unsigned)g.src;
-            g.push_tag[g.src] = rbase + 1;
-            ctl->cq[0] = 1;
+        if (blockIdx.x == 0 && threadIdx.x < 32) {
+            if (lane == 0) g.push_tag[g.src] = tag0;
+            expand(lane == 0, (unsigned)g.src, p, relax0, ls);
+            ls.frontier += lane == 0 ? 1 : 0;
         }
         if (!grid_sync(ctl)) return;
     } else {
-        // ---- A. cut-off subtrees: level-synchronous walk over children -------------------
-        // Level L reads invq[lo, hi) and appends the children it cuts off at invq[hi...]
-        // through its own counter lc[(L+1)%3], so every CTA derives the same level bounds
-        // even while faster CTAs already append the next level.  inv_count (the roots,
-        // written by k_delete) is not written by this kernel.
-        unsigned lo = 0, hi = __ldcg(&ctl->inv_count);
+        // ---- A. cut-off subtrees ------------------------------------------------------------
+        // Level L processes items [lo, hi) of the lists it/ic and appends the items of the
+        // vertices it cuts off after hi through the level's own counters lt*[(L+1)%3], so
+        // every CTA derives the same level bounds while faster CTAs already append.
+        const unsigned nroots = __ldcg(&ctl->inv_count);  // written by k_delete
+        {
+            const Out lvl0{g.it, &ctl->ltT[0], g.tcap, g.ic, &ctl->ltC[0], g.ccap};
+            for (unsigned base = gtid - lane; base < nroots; base += nthreads) {
+                const unsigned i = base + lane;
+                const bool has = i < nroots;
+                expand(has, has ? __ldcg(&g.invq[i]) : 0u, p, lvl0, ls);
+            }
+        }
+        if (leader) ls.marked += nroots;
+        if (!grid_sync(ctl)) return;
+        unsigned loT = 0, loC = 0, hiT = __ldcg(&ctl->ltT[0]), hiC = __ldcg(&ctl->ltC[0]);
         int level = 0;
         bool need_pj = false;
         for (;;) {
-            const unsigned nh = __ldcg(&ctl->bh[level % 3]);
-            if (lo >= hi && nh == 0) break;
+            if (loT >= hiT && loC >= hiC) break;
             if (level >= p.bfs_levels) {
                 need_pj = true;
                 break;
             }
             if (leader) {
-                ctl->bh[(level + 2) % 3] = 0;
-                ctl->lc[(level + 2) % 3] = 0;
+                ctl->ltT[(level + 2) % 3] = 0;
+                ctl->ltC[(level + 2) % 3] = 0;
             }
-            MarkOp op{g.state, g.adj, g.inv_tag, p.epoch, g.invq + hi, &ctl->lc[(level + 1) % 3], &ls};
-            run_items(op, p, g.invq + lo, hi - lo, (level & 1) ? g.h1 : g.h0, nh, (level & 1) ? g.h0 : g.h1,
-                      &ctl->bh[(level + 1) % 3]);
+            MarkOp op{&p,
+                      Out{g.it + hiT, &ctl->ltT[(level + 1) % 3], g.tcap - hiT, g.ic + hiC, &ctl->ltC[(level + 1) % 3],
+                          g.ccap - hiC},
+                      PushBuf{pbuf, 0}, &ls};
+            run_items(op, p, g.it + loT, hiT - loT, g.ic + loC, hiC - loC);
             if (!grid_sync(ctl)) return;
-            lo = hi;
-            hi += __ldcg(&ctl->lc[(level + 1) % 3]);
+            loT = hiT;
+            loC = hiC;
+            hiT += __ldcg(&ctl->ltT[(level + 1) % 3]);
+            hiC += __ldcg(&ctl->ltC[(level + 1) % 3]);
             level++;
         }
         if (leader) ctl->stat[ST_LEVELS] = (unsigned long long)level;
@@ -614,6 +670,7 @@ __device__ void update_body(UpdParams& p) {
                 if (__ldcg(&ctl->pjf[pass % 3]) == 0) break;
             }
             if (leader) ctl->stat[ST_PJ] = (unsigned long long)(pass + 1);
+            const Out pjo{g.it + hiT, &ctl->pjT, g.tcap - hiT, g.ic + hiC, &ctl->pjC, g.ccap - hiC};
             for (unsigned base = gtid - lane; base < (unsigned)g.n; base += nthreads) {
                 const unsigned v = base + lane;
                 bool newinv = false;
@@ -622,82 +679,73 @@ __device__ void update_body(UpdParams& p) {
                     g.state[v] = kInfState;
                     newinv = true;
                 }
-                warp_append(newinv, v, g.invq + hi, &ctl->pj_cnt);
+                ls.marked += newinv ? 1 : 0;
+                expand(newinv, v, p, pjo, ls);
             }
             if (!grid_sync(ctl)) return;
-            hi += __ldcg(&ctl->pj_cnt);
+            hiT += __ldcg(&ctl->pjT);
+            hiC += __ldcg(&ctl->pjC);
         }
-        if (leader) {
-            ctl->ts[1] = globaltimer();
-            ctl->stat[ST_INV] = hi;
-        }
+        if (leader) ctl->ts[1] = globaltimer();
 
-        // ---- B. seeds: surviving insertions relax both ends; cut-off vertices pull -------
-        const unsigned tag0 = rbase + 1;
-        for (long long base = (long long)(gtid - lane); base < p.k; base += nthreads) {
-            const long long i = base + lane;
-            const bool has = i < p.k;
-            const int4 c = has ? p.chg[i] : make_int4(0, 0, 0, -1);
-            bool alive = false;
-            if (has && c.w == 1) {
-                const long long s0 = p.slot[2 * i], s1 = p.slot[2 * i + 1];
-                const long long s = s0 >= 0 ? s0 : s1;
-                alive = s >= 0 && __ldg(&g.adj[s]).y >= 0;
-            }
-            bool pa = false, pb = false;
-            if (alive) {
-                const unsigned a = (unsigned)c.x, b = (unsigned)c.y;
-                const unsigned long long sa = __ldcg(&g.state[a]), sb = __ldcg(&g.state[b]);
-                if ((sa >> 32) != kDistInf) pb = relax_to(g.state, b, (sa >> 32) + (unsigned)c.z, a, c.z, sb, ls);
-                if ((sb >> 32) != kDistInf)
-                    pa = relax_to(g.state, a, (sb >> 32) + (unsigned)c.z, b, c.z, __ldcg(&g.state[a]), ls);
-                ls.edges_relax += 2;
-            }
-            const bool db = pb && claim_push(g.push_tag, (unsigned)c.y, tag0);
-            warp_append(db, (unsigned)c.y, g.q0, &ctl->cq[0]);
-            const bool da = pa && claim_push(g.push_tag, (unsigned)c.x, tag0);
-            warp_append(da, (unsigned)c.x, g.q0, &ctl->cq[0]);
-        }
-        const unsigned ninv = hi;
+        // ---- B. seeds: surviving insertions relax both ends; cut-off vertices pull ---------
         {
-            PullOp op{g.state, g.adj, g.push_tag, tag0, g.q0, &ctl->cq[0], &ls, kInfState, false};
-            run_items(op, p, g.invq, ninv, nullptr, 0, g.h0, &ctl->ph);
+            PushBuf pb{pbuf, 0};
+            for (long long base = (long long)(gtid - lane); base < p.k; base += nthreads) {
+                const long long i = base + lane;
+                const bool has = i < p.k;
+                const int4 c = has ? p.chg[i] : make_int4(0, 0, 0, -1);
+                const bool alive = has && c.w == 1 && p.ins_state[i] == 1;
+                bool pa = false, pbv = false;
+                if (alive) {
+                    const unsigned a = (unsigned)c.x, b = (unsigned)c.y;
+                    const unsigned long long sa = __ldcg(&g.state[a]), sb = __ldcg(&g.state[b]);
+                    if ((sa >> 32) != kDistInf) pbv = relax_to(g.state, b, (sa >> 32) + (unsigned)c.z, a, c.z, sb, ls);
+                    if ((sb >> 32) != kDistInf)
+                        pa = relax_to(g.state, a, (sb >> 32) + (unsigned)c.z, b, c.z, __ldcg(&g.state[a]), ls);
+                    ls.edges_relax += 2;
+                }
+                const bool db = pbv && claim_push(g.push_tag, (unsigned)c.y, tag0);
+                const bool da = pa && claim_push(g.push_tag, (unsigned)c.x, tag0);
+                ls.frontier += (db ? 1 : 0) + (da ? 1 : 0);
+                pb.add(db, (unsigned)c.y);
+                pb.add(da, (unsigned)c.x);
+                pb.flush(p, relax0, ls, false);
+            }
+            pb.flush(p, relax0, ls, true);
+        }
+        {
+            PullOp op{&p, tag0, relax0, PushBuf{pbuf, 0}, &ls, kInfState, false};
+            run_items(op, p, g.it, hiT, g.ic, hiC);
         }
         if (!grid_sync(ctl)) return;
-        const unsigned nph = __ldcg(&ctl->ph);
-        if (nph > 0) {
-            PullOp op{g.state, g.adj, g.push_tag, tag0, g.q0, &ctl->cq[0], &ls, kInfState, false};
-            run_items(op, p, nullptr, 0, g.h0, nph, g.h1, &ctl->ph);
-            if (!grid_sync(ctl)) return;
-        }
     }
     if (leader) ctl->ts[2] = globaltimer();
 
-    // ---- C. relaxation rounds ---------------------------------------------------------
+    // ---- C. relaxation rounds ---------------------------------------------------------------
     long long r = 0;
-    unsigned long long frontier = 0;
     for (;; r++) {
-        const unsigned nq = __ldcg(&ctl->cq[r % 3]), nh = __ldcg(&ctl->ch[r % 3]);
-        if (nq == 0 && nh == 0) break;
+        const unsigned nT = __ldcg(&ctl->rcT[r % 3]), nC = __ldcg(&ctl->rcC[r % 3]);
+        if (nT == 0 && nC == 0) break;
         if (r >= p.max_rounds) {
             if (leader) set_status(ctl, -5 /* NO_CONVERGENCE */);
             break;
         }
-        frontier += (unsigned long long)nq + nh;
         if (leader) {
-            ctl->cq[(r + 2) % 3] = 0;
-            ctl->ch[(r + 2) % 3] = 0;
+            ctl->rcT[(r + 2) % 3] = 0;
+            ctl->rcC[(r + 2) % 3] = 0;
         }
         const bool odd = (r & 1) != 0;
-        RelaxOp op{g.state, g.adj, g.push_tag, rbase + (unsigned)r + 2u, odd ? g.q0 : g.q1,
-                   &ctl->cq[(r + 1) % 3], &ls};
-        run_items(op, p, odd ? g.q1 : g.q0, nq, odd ? g.h1 : g.h0, nh, odd ? g.h0 : g.h1, &ctl->ch[(r + 1) % 3]);
+        RelaxOp op{&p, rbase + (unsigned)r + 2u,
+                   Out{odd ? g.rt0 : g.rt1, &ctl->rcT[(r + 1) % 3], g.tcap, odd ? g.rc0 : g.rc1,
+                       &ctl->rcC[(r + 1) % 3], g.ccap},
+                   PushBuf{pbuf, 0}, &ls};
+        run_items(op, p, odd ? g.rt1 : g.rt0, nT, odd ? g.rc1 : g.rc0, nC);
         if (!grid_sync(ctl)) break;
     }
     flush_stats(ctl, ls);
     if (leader) {
         ctl->stat[ST_ROUNDS] = (unsigned long long)r;
-        ctl->stat[ST_FRONTIER] = frontier;
         ctl->round_base = rbase + (unsigned)r + 4u;
         ctl->ts[3] = globaltimer();
     }
@@ -710,24 +758,14 @@ namespace dsssp {
 
 void count_launch(int n);
 
-cudaError_t launch_front(const UpdParams& p, int4* ovf, bool with_append, cudaStream_t s) {
-    const unsigned grid = (unsigned)((p.k + 255) / 256);
-    if (grid == 0) return cudaSuccess;
-    if (with_append) {
-        k_prepare<<<grid, 256, 0, s>>>(p);
-        k_append<<<grid, 256, 0, s>>>(p, ovf);
-        count_launch(2);
-    }
-    k_delete<<<grid, 256, 0, s>>>(p);
-    count_launch(1);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_relocate(const UpdParams& p, cudaStream_t s) {
-    const unsigned grid = (unsigned)((p.k + 255) / 256);
-    if (grid == 0) return cudaSuccess;
-    k_relocate<<<grid, 256, 0, s>>>(p);
-    count_launch(1);
+cudaError_t launch_front(const UpdParams& p, int grid, cudaStream_t s) {
+    if (p.k <= 0) return cudaSuccess;
+    const long long need = (p.k + 255) / 256;
+    const unsigned g = (unsigned)(need < grid ? need : grid);
+    k_prepare<<<g, 256, 0, s>>>(p);
+    k_delete<<<g, 256, 0, s>>>(p);
+    k_append<<<g, 256, 0, s>>>(p);
+    count_launch(3);
     return cudaGetLastError();
 }
 

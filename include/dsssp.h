@@ -56,9 +56,11 @@ typedef struct {
     int32_t device;       /* CUDA device ordinal */
     int32_t slack_pct;    /* per-row insertion slack, percent of the row's degree */
     int32_t slack_min;    /* minimum free slots per row */
-    int32_t small_deg;    /* frontier vertices with degree <= small_deg: one thread each */
-    int32_t large_deg;    /* degree <= large_deg: one warp each; above: CTA per chunk */
-    int32_t chunk;        /* edges per CTA work item of the large bucket */
+    int32_t small_deg;    /* edges per thread work item (multiple of 4, 4..64): a frontier
+                             vertex of degree d <= small_deg is one thread's item, a longer row
+                             up to large_deg is split into ceil(d/small_deg) thread items */
+    int32_t large_deg;    /* rows above this degree are split into CTA items of `chunk` edges */
+    int32_t chunk;        /* edges per CTA work item */
     int32_t bfs_levels;   /* subtree walk levels before switching to pointer jumping */
     int32_t block;        /* threads per CTA of the update kernel (multiple of 32) */
     int32_t ctas_per_sm;  /* resident CTAs per SM of the update kernel; 0 = occupancy max */
@@ -83,12 +85,14 @@ typedef struct {
     int64_t updates;           /* atomic updates that lowered a distance */
     int64_t overflow_entries;  /* inserted entries that did not fit a row's slack */
     int64_t repacks;           /* adjacency repacks this call triggered */
+    int64_t n_killed;          /* insertions removed again by a deletion of the same batch */
+    int64_t work_items;        /* work items (te-edge thread items + CTA chunks) created */
     double t_step1_ms;         /* insert + delete kernels (CUDA events) */
     double t_inval_ms;         /* subtree invalidation (device timestamps) */
     double t_relax_ms;         /* seeding + relaxation rounds (device timestamps) */
     double t_update_ms;        /* the persistent update kernel (CUDA events) */
     double t_total_ms;         /* the whole batch on the device (CUDA events) */
-    double bytes_alg;          /* algorithmic bytes of the batch (see the design doc byte model) */
+    double bytes_alg;          /* algorithmic bytes of the batch (byte model of the engine) */
     double bytes_alg_update;   /* the part moved by the persistent update kernel */
 } dsssp_stats;
 

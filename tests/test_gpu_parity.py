@@ -56,9 +56,9 @@ OPTION_SETS = [
     {},
     {"bfs_levels": 0},                                     # pointer jumping only
     {"bfs_levels": 1},                                     # walk one level, then pointer jumping
-    {"small_deg": 0, "large_deg": 0, "chunk": 32},          # every row on the CTA-chunk path
-    {"small_deg": 0, "large_deg": 1 << 20},                # every row one warp
-    {"small_deg": 1 << 20, "large_deg": 1 << 20},          # every row one thread
+    {"small_deg": 4, "large_deg": 4, "chunk": 32},          # rows above 4 edges on the CTA-chunk path
+    {"small_deg": 4, "large_deg": 1 << 20},                # every row split into 4-edge thread items
+    {"small_deg": 64, "large_deg": 1 << 20},               # 64-edge thread items
     {"slack_pct": 0, "slack_min": 0},                      # every insertion overflows -> repack
     {"block": 64, "ctas_per_sm": 1},
 ]
@@ -112,8 +112,9 @@ def test_insert_then_delete_same_edge_in_one_batch():
     w = np.array([10, 10, 10], np.int32)
     parent, dist = initial_tree(n, u, v, w)
     ch = D.make_changes([0, 3], [3, 0], [1, 1], [1, 0])
-    p, d, _ = run_engine(n, u, v, w, ch, parent, dist)
+    p, d, st = run_engine(n, u, v, w, ch, parent, dist)
     assert d.tolist() == [0, 10, 20, 30]
+    assert st.n_killed == 1
     check_against_oracle(n, u, v, w, ch, 0, p, d, "insert+delete")
 
 
