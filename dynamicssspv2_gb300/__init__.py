@@ -122,6 +122,10 @@ _sig("dsssp_gen_grid", C.c_int, C.c_int32, C.c_int32, C.c_double, C.c_int64, C.c
 _sig("dsssp_gen_changes", C.c_int, C.c_int32, C.c_int64, _i32p, _i32p, _i32p, C.c_int64, C.c_int64, C.c_int32,
      C.c_int32, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(_P))
 _sig("dsssp_max_degree_vertex", C.c_int32, C.c_int32, C.c_int64, _i32p, _i32p)
+_sig("dsssp_sssp_noalloc", C.c_int, C.c_int32, C.c_int64, _P, _P, C.c_int32, _P, _P, _P)
+
+NOALLOC_MAX_VERTICES = 65536
+NOALLOC_MAX_ENTRIES = 1 << 20
 
 EXPORTED = [
     "dsssp_default_opts", "dsssp_graph_create", "dsssp_graph_destroy", "dsssp_graph_info", "dsssp_tree_load",
@@ -129,7 +133,7 @@ EXPORTED = [
     "dsssp_graph_snapshot", "dsssp_graph_restore", "dsssp_graph_compact", "dsssp_host_alloc", "dsssp_host_free",
     "dsssp_launch_count", "dsssp_last_error", "dsssp_strerror", "dsssp_free", "dsssp_read_graph_file",
     "dsssp_read_changes_file", "dsssp_read_sssp_file", "dsssp_write_sssp_file", "dsssp_gen_er", "dsssp_gen_rmat",
-    "dsssp_gen_grid", "dsssp_gen_changes", "dsssp_max_degree_vertex",
+    "dsssp_gen_grid", "dsssp_gen_changes", "dsssp_max_degree_vertex", "dsssp_sssp_noalloc",
 ]
 
 
@@ -326,3 +330,11 @@ def max_degree_vertex(n: int, u, v) -> int:
     u = np.ascontiguousarray(u, np.int32)
     v = np.ascontiguousarray(v, np.int32)
     return int(_lib.dsssp_max_degree_vertex(n, len(u), u, v))
+
+
+def sssp_noalloc(n: int, nnz: int, d_row_off: int, d_adj: int, src: int, d_parent: int, d_dist: int,
+                 stream: int | None = None) -> None:
+    """Shortest-path tree of a CSR graph in caller device memory (raw device addresses);
+    the engine allocates nothing for it (see dsssp_sssp_noalloc in include/dsssp.h)."""
+    _check(_lib.dsssp_sssp_noalloc(int(n), int(nnz), d_row_off, d_adj, int(src), d_parent, d_dist, stream),
+           "sssp_noalloc")

@@ -30,7 +30,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp"]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-Wno-unused-function"]
 
-CUDA_UNITS = ["update.cu", "graph.cu"]
+CUDA_UNITS = ["update.cu", "graph.cu", "noalloc.cu"]
 HOST_UNITS = ["gen.cpp", "textio.cpp"]
 HEADERS = ["engine.cuh", "host_common.h"]
 

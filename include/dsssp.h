@@ -160,6 +160,35 @@ const char* dsssp_last_error(void);
 const char* dsssp_strerror(int code);
 void dsssp_free(void* p);
 
+/* ---- shortest-path tree without device allocation ---------------------------------- */
+
+/* Largest graph dsssp_sssp_noalloc() accepts: its work space is a fixed static device array
+ * of about 5 MB that every GPU that loads this library keeps until the process exits. */
+#define DSSSP_NOALLOC_MAX_VERTICES 65536
+#define DSSSP_NOALLOC_MAX_ENTRIES 1048576
+
+/* Shortest-path tree from src of a graph held in the caller's device memory, for callers
+ * that must not allocate device memory where they call it (for example a plugin's enqueue
+ * callback inside an inference or streaming runtime that owns the memory budget, or a
+ * pipeline that reserved all device memory up front; cudaMalloc may also synchronize the
+ * device).  No counterpart in the reference: it has no library interface, and its CLI
+ * allocates per run.
+ *   d_row_off  n+1 int64 row offsets (d_row_off[0] == 0, d_row_off[n] == nnz)
+ *   d_adj      nnz (column, weight) int32 pairs, 8-byte aligned, weights >= 0; an
+ *              undirected edge appears in both rows
+ *   d_parent   n int32 outputs (-1 = unreachable, src is its own parent)
+ *   d_dist     n int64 outputs (DSSSP_UNREACHABLE = -1 for unreachable vertices)
+ * All pointers are device addresses on the current device; stream is a cudaStream_t (NULL =
+ * legacy default stream).  n <= DSSSP_NOALLOC_MAX_VERTICES and nnz <=
+ * DSSSP_NOALLOC_MAX_ENTRIES, else DSSSP_E_INVAL.  Waits for the result on stream.
+ * It calls no cudaMalloc, cudaFree or other allocating routine.  The first call on a device
+ * looks up the work space's device address (cudaGetSymbolAddress) and the update kernel's
+ * occupancy; make that first call before any stream capture.  All calls on a device share
+ * the one work space (each call re-initialises what it needs), so calls that overlap on the
+ * GPU, from any thread or stream, race and must be serialised by the caller. */
+int dsssp_sssp_noalloc(int32_t n, int64_t nnz, const int64_t* d_row_off, const int32_t* d_adj,
+                       int32_t src, int32_t* d_parent, int64_t* d_dist, void* stream);
+
 /* ---- reference text formats (all_structure_undir.cuh:89-198, README.md:25-37) ---- */
 
 /* graph file: "u v w" per line, each undirected edge once.  Vertex ids must be < n
