@@ -131,9 +131,11 @@ class ClockSampler:
         self.proc = None
 
     def __enter__(self):
+        if os.environ.get("DSSSP_BENCH_NO_CLOCKS"):
+            return self
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
@@ -261,6 +263,8 @@ def run_engine(args, dist: Dist) -> int:
     n, u, v, w, src, ch = make_inputs(args.workload)
     batch = len(ch)
     opts = D.default_opts(device=dev)
+    for key, val in json.loads(os.environ.get("DSSSP_BENCH_OPTS", "{}")).items():
+        setattr(opts, key, val)
     g = D.Graph(n, u, v, w, opts)
     g.tree_compute(src)
     g.snapshot()
@@ -296,6 +300,9 @@ def run_engine(args, dist: Dist) -> int:
         D._check(D._lib.dsssp_tree_read(g.handle, h_par.data_ptr(), h_dist.data_ptr()), "tree_read")
         return time.perf_counter() - t0, st
 
+    clk = ClockSampler(dev).__enter__()
+    if clk.proc:
+        time.sleep(1.0)  # let nvidia-smi come up before any timed work
     for _ in range(args.warmup):
         reset()
         device_step()
@@ -305,15 +312,14 @@ def run_engine(args, dist: Dist) -> int:
     torch.cuda.synchronize(dev)
     stats = []
     launches0 = D.launch_count()
-    with ClockSampler(dev) as clk:
-        for _ in range(args.steps):
-            reset()
-            stats.append(device_step())
+    for _ in range(args.steps):
+        reset()
+        stats.append(device_step())
     launches = D.launch_count() - launches0
     torch.cuda.synchronize(dev)
     dist.barrier()
     # the resets between steps launch restore copies and the flush (not library kernels);
-    # library kernels per step: prepare, append, delete, update
+    # library kernels per step: prepare, delete, append, update
     t_steps = [s.t_total_ms for s in stats]
     t_total = sum(t_steps) * 1e-3
     t_max = dist.max(t_total)
@@ -325,6 +331,7 @@ def run_engine(args, dist: Dist) -> int:
         reset()
         dt, _ = e2e_step()
         e2e_times.append(dt)
+    clk.__exit__(None, None, None)
     e2e_t = dist.max(sum(e2e_times) / len(e2e_times))
     e2e_value = dist.world * batch / e2e_t
 
@@ -348,7 +355,9 @@ def run_engine(args, dist: Dist) -> int:
         return 0
     cfg = describe(args.workload)
     cfg.update({"parallelism": f"replicas x{dist.world}", "l2": "graph restore (>1 GB written) + 256 MB flush "
-                "between timed steps", "timed": "sum of per-step CUDA-event intervals around the batch kernels"})
+                "between timed steps", "timed": "sum of per-step CUDA-event intervals around the batch kernels",
+                "clocks_window": "nvidia-smi every 50 ms from 1 s before warm-up to the end of the e2e leg",
+                "opts": {k: getattr(opts, k) for k, _ in D.Opts._fields_}})
     line = {
         "metric": "change-edges/s (batch update, exact distances)",
         "value": value,
@@ -389,7 +398,7 @@ def run_engine(args, dist: Dist) -> int:
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["dsssp", "reference"], default="dsssp")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="rmat22")

@@ -7,6 +7,8 @@
 //   rows[n]       16 B {start, deg, cap}          row v = adj[start, start+deg), capacity cap
 //   sorted_len[n] i32  length of the neighbour-sorted prefix of each row
 //   adj[]         8 B  (col, wt) per directed entry; wt < 0 marks a deleted entry
+//   twin[]        u32  per adjacency slot: slot of the reverse entry (v -> u for u -> v), so a
+//                      deletion searches only the shorter of its two rows
 //   inv_tag[n]    u32  batch epoch in which the vertex was cut off
 //   push_tag[n]   u32  round tag of the last frontier push (de-duplication)
 //   jm[n]         u32  pointer-jumping word (ancestor or terminal tag)
@@ -30,7 +32,14 @@ constexpr unsigned kTagOk = 0xFFFFFFFFu;   // pointer jumping: reaches the root 
 constexpr unsigned kTagInv = 0xFFFFFFFEu;  // pointer jumping: below a cut-off vertex
 constexpr int kStatusOverflowPending = 1;  // internal: an insertion did not fit its row
 constexpr unsigned long long kHashEmpty = 0xFFFFFFFFFFFFFFFFull;
-constexpr int kHashNoWeight = (int)0x80808080;  // byte-fill sentinel; deletions with w < 0 are not hashed
+constexpr int kHashNoWeight = -1;  // 0xFF byte fill; deletions with w < 0 are not hashed
+
+// One slot of the batch's deletion set (endpoint pair, weight): one 16-byte sector.
+struct __align__(16) DelSlot {
+    unsigned long long pair;
+    int w;
+    int pad;
+};
 
 struct __align__(16) RowDesc {
     long long start;
@@ -100,6 +109,7 @@ struct DevGraph {
     RowDesc* rows;
     int* sorted_len;
     int2* adj;
+    unsigned* twin;  // nullptr when the slot count does not fit 32 bits
     unsigned* inv_tag;
     unsigned* push_tag;
     unsigned* jm;
@@ -122,8 +132,7 @@ struct UpdParams {
     const int4* chg;  // (u, v, w, op) records
     long long k;
     int* ins_state;   // per record: 1 = insertion that survives the batch
-    unsigned long long* hpair;  // deletion set: endpoint pair -> weight (open addressing)
-    int* hw;
+    DelSlot* hset;    // deletion set: endpoint pair -> weight (open addressing)
     unsigned long long hmask;
     int4* ovf;        // insertions that did not fit their row: (row, col, wt, record)
     unsigned epoch;

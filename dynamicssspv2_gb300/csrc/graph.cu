@@ -74,9 +74,22 @@ __global__ void k_scatter_packed(const int* u, const int* v, const int* w, long 
     keys[poff[b] + atomicAdd(&cursor[b], 1)] = make_key(a, w[i]);
 }
 
+// First index in keys[lo, hi) that is >= key.
+__device__ __forceinline__ long long lower_key(const unsigned long long* keys, long long lo, long long hi,
+                                               unsigned long long key) {
+    while (lo < hi) {
+        const long long mid = (lo + hi) >> 1;
+        if (keys[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
 // Packed (contiguous) sorted rows -> slack layout.  Thread per entry; row by binary search.
+// With twin != nullptr also the slot of the reverse entry: the i-th copy of (c, w) in row r
+// pairs with the i-th copy of (r, w) in row c.
 __global__ void k_spread(const unsigned long long* keys, const long long* poff, const long long* start, int n,
-                         long long total, int2* adj) {
+                         long long total, int2* adj, unsigned* twin) {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= total) return;
     int lo = 0, hi = n;  // last r with poff[r] <= e
@@ -86,7 +99,15 @@ __global__ void k_spread(const unsigned long long* keys, const long long* poff, 
         else hi = mid;
     }
     const unsigned long long k = keys[e];
-    adj[start[lo] + (e - poff[lo])] = make_int2((int)(k >> 32), (int)(unsigned)k);
+    const long long slot = start[lo] + (e - poff[lo]);
+    const int c = (int)(k >> 32), w = (int)(unsigned)k;
+    adj[slot] = make_int2(c, w);
+    if (twin) {
+        const long long rank = e - lower_key(keys, poff[lo], poff[lo + 1], k);
+        const unsigned long long rk = ((unsigned long long)(unsigned)lo << 32) | (unsigned)w;
+        const long long pos = lower_key(keys, poff[c], poff[c + 1], rk);
+        twin[slot] = (unsigned)(start[c] + (pos - poff[c]) + rank);
+    }
 }
 
 __global__ void k_rows_init(const long long* start, const long long* deg, const long long* cap, int n,
@@ -253,8 +274,7 @@ struct dsssp_graph {
     long long chg_cap = 0;
     int* d_ins_state = nullptr;
     int4* d_ovf = nullptr;
-    unsigned long long* d_hpair = nullptr;  // deletion set of the batch
-    int* d_hw = nullptr;
+    DelSlot* d_hset = nullptr;  // deletion set of the batch
     unsigned long long hcap = 0;
     Ctl* h_ctl = nullptr;  // pinned mirror of the control block
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -274,6 +294,7 @@ struct dsssp_graph {
     RowDesc* s_rows = nullptr;
     int* s_sorted = nullptr;
     int2* s_adj = nullptr;
+    unsigned* s_twin = nullptr;
     long long s_cap = 0;
     long long s_entries = 0;
     int s_src = -1;
@@ -328,15 +349,13 @@ int ensure_batch(dsssp_graph* g, long long k) {
     dfree(g->d_chg);
     dfree(g->d_ins_state);
     dfree(g->d_ovf);
-    dfree(g->d_hpair);
-    dfree(g->d_hw);
+    dfree(g->d_hset);
     g->chg_cap = 0;
     g->hcap = 0;
     int rc = dalloc(&g->d_chg, (size_t)cap, "change buffer");
     if (!rc) rc = dalloc(&g->d_ins_state, (size_t)cap, "insertion state");
     if (!rc) rc = dalloc(&g->d_ovf, (size_t)cap * 2, "overflow buffer");
-    if (!rc) rc = dalloc(&g->d_hpair, (size_t)h, "deletion set");
-    if (!rc) rc = dalloc(&g->d_hw, (size_t)h, "deletion set");
+    if (!rc) rc = dalloc(&g->d_hset, (size_t)h, "deletion set");
     if (!rc) {
         g->chg_cap = cap;
         g->hcap = h;
@@ -401,10 +420,12 @@ int layout_rows(dsssp_graph* g, unsigned long long* keys_in, long long total, co
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) rc = cuda_fail(e, "row layout");
     }
+    unsigned* twin = nullptr;
     if (!rc) rc = dalloc(&adj, (size_t)cap_total, "adjacency");
+    if (!rc && cap_total < 0xFFFFFFFFll) rc = dalloc(&twin, (size_t)cap_total, "twin index");
     if (!rc) {
         if (total > 0) {
-            k_spread<<<blocks_for(total), kThreads, 0, s>>>(keys_out, poff, start, n, total, adj);
+            k_spread<<<blocks_for(total), kThreads, 0, s>>>(keys_out, poff, start, n, total, adj, twin);
             count_launch(1);
         }
         if (n > 0) {
@@ -417,8 +438,11 @@ int layout_rows(dsssp_graph* g, unsigned long long* keys_in, long long total, co
     }
     if (!rc) {
         dfree(g->dg.adj);
+        dfree(g->dg.twin);
         g->dg.adj = adj;
+        g->dg.twin = twin;
         adj = nullptr;
+        twin = nullptr;
         g->cap_total = cap_total;
         g->entries = total;
         rc = ensure_work(g);
@@ -428,6 +452,7 @@ int layout_rows(dsssp_graph* g, unsigned long long* keys_in, long long total, co
     dfree(keys_out);
     if (tmp) cudaFree(tmp);
     dfree(adj);
+    dfree(twin);
     return rc;
 }
 
@@ -485,8 +510,7 @@ UpdParams make_params(const dsssp_graph* g, const int4* chg, long long k, int mo
     p.chg = chg;
     p.k = k;
     p.ins_state = g->d_ins_state;
-    p.hpair = g->d_hpair;
-    p.hw = g->d_hw;
+    p.hset = g->d_hset;
     p.hmask = g->hcap ? g->hcap - 1 : 0;
     p.ovf = g->d_ovf;
     p.epoch = g->epoch;
@@ -586,17 +610,16 @@ void fill_stats(const dsssp_graph* g, const Ctl& c, dsssp_stats* st, bool events
 
 // Enqueues one batch (records already on the device).
 int enqueue_batch(dsssp_graph* g, const int4* d_chg, long long k, cudaStream_t s) {
+    const bool ev = g->o.timing != 0;
+    if (ev) CK(cudaEventRecord(g->ev[0], s), "event");
     int rc = clear_ctl(g, s);
     if (rc) return rc;
     const size_t hb = (size_t)(2ull * (unsigned long long)k);
     unsigned long long h = 64;
     while (h < hb) h <<= 1;  // this batch uses the first h slots of the deletion set
-    CK(cudaMemsetAsync(g->d_hpair, 0xFF, sizeof(unsigned long long) * h, s), "deletion set reset");
-    CK(cudaMemsetAsync(g->d_hw, 0x80, sizeof(int) * h, s), "deletion set reset");
+    CK(cudaMemsetAsync(g->d_hset, 0xFF, sizeof(DelSlot) * h, s), "deletion set reset");
     UpdParams p = make_params(g, d_chg, k, 0);
     p.hmask = h - 1;
-    const bool ev = g->o.timing != 0;
-    if (ev) CK(cudaEventRecord(g->ev[0], s), "event");
     CK(launch_front(p, g->num_sms * 8, s), "insert/delete kernels");
     if (ev) CK(cudaEventRecord(g->ev[1], s), "event");
     CK(launch_update(p, g->coop_grid, g->o.block, s), "update kernel");
@@ -654,7 +677,7 @@ void dsssp_default_opts(dsssp_opts* o) {
     o->device = 0;
     o->slack_pct = 25;
     o->slack_min = 4;
-    o->small_deg = 8;
+    o->small_deg = 4;
     o->large_deg = 1024;
     o->chunk = 1024;
     o->bfs_levels = 48;
@@ -706,7 +729,7 @@ void dsssp_graph_destroy(dsssp_graph* g) {
     dfree(d.state); dfree(d.rows); dfree(d.sorted_len); dfree(d.adj); dfree(d.inv_tag);
     dfree(d.push_tag); dfree(d.jm); dfree(d.invq); dfree(d.rt0); dfree(d.rt1); dfree(d.rc0); dfree(d.rc1);
     dfree(d.it); dfree(d.ic); dfree(d.ctl);
-    dfree(g->d_chg); dfree(g->d_ins_state); dfree(g->d_ovf); dfree(g->d_hpair); dfree(g->d_hw);
+    dfree(g->d_chg); dfree(g->d_ins_state); dfree(g->d_ovf); dfree(g->d_hset); dfree(d.twin); dfree(g->s_twin);
     dfree(g->d_par); dfree(g->d_dist);
     dfree(g->s_state); dfree(g->s_rows); dfree(g->s_sorted); dfree(g->s_adj);
     if (g->h_ctl) cudaFreeHost(g->h_ctl);
@@ -844,7 +867,8 @@ int dsssp_graph_info(const dsssp_graph* g, int64_t* n, int64_t* entries, int64_t
     if (device_bytes) {
         const long long N = g->n;
         long long b = N * (8 + 16 + 4 + 4 + 4 + 4 + 4) + g->cap_total * 8 + 3 * g->dg.tcap * 8 +
-                      3 * g->dg.ccap * 8 + g->chg_cap * (16 + 4 + 32) + (long long)g->hcap * 12 +
+                      3 * g->dg.ccap * 8 + g->chg_cap * (16 + 4 + 32) + (long long)g->hcap * 16 +
+                      (g->dg.twin ? g->cap_total * 4 : 0) +
                       (long long)sizeof(Ctl);
         if (g->d_par) b += N * 12;
         if (g->has_snap) b += N * (8 + 16 + 4) + g->s_cap * 8;
@@ -991,9 +1015,12 @@ int dsssp_graph_snapshot(dsssp_graph* g) {
         if (!rc) rc = dalloc(&g->s_sorted, (size_t)g->n, "snapshot");
         if (rc) return rc;
     }
-    if (g->s_cap != g->cap_total) {
+    if (g->s_cap != g->cap_total || (g->dg.twin && !g->s_twin)) {
         dfree(g->s_adj);
+        dfree(g->s_twin);
+        g->s_cap = 0;
         rc = dalloc(&g->s_adj, (size_t)g->cap_total, "snapshot");
+        if (!rc && g->dg.twin) rc = dalloc(&g->s_twin, (size_t)g->cap_total, "snapshot");
         if (rc) return rc;
         g->s_cap = g->cap_total;
     }
@@ -1003,6 +1030,8 @@ int dsssp_graph_snapshot(dsssp_graph* g) {
     CK(cudaMemcpyAsync(g->s_rows, g->dg.rows, N * sizeof(RowDesc), cudaMemcpyDeviceToDevice, s), "snapshot");
     CK(cudaMemcpyAsync(g->s_sorted, g->dg.sorted_len, N * 4, cudaMemcpyDeviceToDevice, s), "snapshot");
     CK(cudaMemcpyAsync(g->s_adj, g->dg.adj, (size_t)g->cap_total * 8, cudaMemcpyDeviceToDevice, s), "snapshot");
+    if (g->dg.twin)
+        CK(cudaMemcpyAsync(g->s_twin, g->dg.twin, (size_t)g->cap_total * 4, cudaMemcpyDeviceToDevice, s), "snapshot");
     CK(cudaStreamSynchronize(s), "snapshot");
     g->s_entries = g->entries;
     g->s_src = g->src;
@@ -1016,10 +1045,12 @@ int dsssp_graph_restore(dsssp_graph* g, void* stream) {
     if (rc) return rc;
     if (g->pending) return fail(DSSSP_E_INVAL, "restore: a batch is still pending");
     cudaStream_t s = stream ? (cudaStream_t)stream : g->stream;
-    if (g->cap_total != g->s_cap) {
+    if (g->cap_total != g->s_cap || (g->s_twin && !g->dg.twin)) {
         CK(cudaStreamSynchronize(s), "restore");
         dfree(g->dg.adj);
+        dfree(g->dg.twin);
         rc = dalloc(&g->dg.adj, (size_t)g->s_cap, "adjacency");
+        if (!rc && g->s_twin) rc = dalloc(&g->dg.twin, (size_t)g->s_cap, "twin index");
         if (rc) return rc;
         g->cap_total = g->s_cap;
         rc = ensure_work(g);
@@ -1030,6 +1061,8 @@ int dsssp_graph_restore(dsssp_graph* g, void* stream) {
     CK(cudaMemcpyAsync(g->dg.rows, g->s_rows, N * sizeof(RowDesc), cudaMemcpyDeviceToDevice, s), "restore");
     CK(cudaMemcpyAsync(g->dg.sorted_len, g->s_sorted, N * 4, cudaMemcpyDeviceToDevice, s), "restore");
     CK(cudaMemcpyAsync(g->dg.adj, g->s_adj, (size_t)g->s_cap * 8, cudaMemcpyDeviceToDevice, s), "restore");
+    if (g->s_twin)
+        CK(cudaMemcpyAsync(g->dg.twin, g->s_twin, (size_t)g->s_cap * 4, cudaMemcpyDeviceToDevice, s), "restore");
     g->entries = g->s_entries;
     g->src = g->s_src;
     return DSSSP_OK;

@@ -40,7 +40,7 @@ constexpr int kMaxWarps = 8;               // update kernel blocks have at most 
 constexpr int kBuf = 160;                  // per-warp push buffer, flushed at >= 32 entries
 
 __shared__ unsigned s_nbar;  // grid barriers this CTA has passed
-__shared__ unsigned s_pbuf[kMaxWarps][kBuf];
+__shared__ uint2 s_pbuf[kMaxWarps][kBuf];  // (vertex, degree) pushed, not yet expanded
 
 struct LocalStats {
     unsigned long long edges_relax = 0, edges_inv = 0, updates = 0, dist_ovf = 0, frontier = 0, items = 0,
@@ -83,11 +83,6 @@ __device__ bool grid_sync(Ctl* ctl) {
     return s_go != 0;
 }
 
-__device__ __forceinline__ bool claim_push(unsigned* push_tag, unsigned c, unsigned tag) {
-    if (__ldcg(&push_tag[c]) == tag) return false;
-    return atomicExch(&push_tag[c], tag) != tag;
-}
-
 // Offers distance nd through parent u to vertex c whose current word is cur.  Returns true
 // when c's distance went down (c must then be pushed).  Zero-weight edges only replace a
 // strictly larger distance, so equal-distance parent swaps can never close a cycle.
@@ -128,9 +123,8 @@ struct Out {
     long long ccap;
 };
 
-// Splits the vertex each lane holds into work items (warp-collective).
-__device__ __forceinline__ void expand(bool valid, unsigned v, const UpdParams& p, const Out& o, LocalStats& ls) {
-    const int deg = valid ? p.g.rows[v].deg : 0;
+// Splits the vertex each lane holds (degree deg, 0 = none) into work items (warp-collective).
+__device__ __forceinline__ void expand(unsigned v, int deg, const UpdParams& p, const Out& o, LocalStats& ls) {
     const bool heavy = deg > p.large_deg;
     const unsigned nt = (!heavy && deg > 0) ? (unsigned)((deg + p.te - 1) / p.te) : 0u;
     const unsigned nc = heavy ? (unsigned)((deg + p.chunk - 1) / p.chunk) : 0u;
@@ -140,14 +134,14 @@ __device__ __forceinline__ void expand(bool valid, unsigned v, const UpdParams& 
     ls.items += nt + nc;
 }
 
-// Per-warp shared-memory buffer of pushed vertices; expanded into items 32 at a time.
+// Per-warp shared-memory buffer of pushed (vertex, degree); expanded into items 32 at a time.
 struct PushBuf {
-    unsigned* buf;
+    uint2* buf;
     int count;  // warp-uniform
 
-    __device__ __forceinline__ void add(bool pred, unsigned v) {
+    __device__ __forceinline__ void add(bool pred, unsigned v, int deg) {
         const unsigned mask = __ballot_sync(kFull, pred);
-        if (pred) buf[count + __popc(mask & ((1u << lane_id()) - 1u))] = v;
+        if (pred) buf[count + __popc(mask & ((1u << lane_id()) - 1u))] = make_uint2(v, (unsigned)deg);
         count += __popc(mask);
         __syncwarp();
     }
@@ -156,13 +150,23 @@ struct PushBuf {
         while (count >= 32 || (all && count > 0)) {
             const int take = count < 32 ? count : 32;
             const bool has = (int)lane_id() < take;
-            const unsigned v = has ? buf[count - take + (int)lane_id()] : 0u;
+            const uint2 e = has ? buf[count - take + (int)lane_id()] : make_uint2(0u, 0u);
             __syncwarp();
             count -= take;
-            expand(has, v, p, o, ls);
+            expand(e.x, (int)e.y, p, o, ls);
         }
     }
 };
+
+// Claims c for the next frontier; the degree load is issued alongside the claim.
+__device__ __forceinline__ bool claim_with_deg(const UpdParams& p, bool want, unsigned c, unsigned tag, int& deg) {
+    deg = 0;
+    if (!want) return false;
+    const int d = p.g.rows[c].deg;
+    const bool won = atomicExch(&p.g.push_tag[c], tag) != tag;
+    deg = d;
+    return won;
+}
 
 // ---- per-edge operations ---------------------------------------------------------------
 // visit4 handles up to four adjacency entries per lane and is called by all 32 lanes.
@@ -195,9 +199,10 @@ struct RelaxOp {
         for (int q = 0; q < 4; q++) {
             bool push = false;
             if (e[q].y >= 0) push = relax_to(state, (unsigned)e[q].x, du + (unsigned)e[q].y, u, e[q].y, cur[q], *ls);
-            const bool doit = push && claim_push(p->g.push_tag, (unsigned)e[q].x, tag);
+            int deg;
+            const bool doit = claim_with_deg(*p, push, (unsigned)e[q].x, tag, deg);
             ls->frontier += doit ? 1 : 0;
-            pb.add(doit, (unsigned)e[q].x);
+            pb.add(doit, (unsigned)e[q].x, deg);
             ls->edges_relax += ok[q] ? 1 : 0;
         }
         pb.flush(*p, out, *ls, false);
@@ -234,7 +239,7 @@ struct MarkOp {
             if (mark) mark = atomicExch(&p->g.inv_tag[c], p->epoch) != p->epoch;
             if (mark) state[c] = kInfState;
             ls->marked += mark ? 1 : 0;
-            pb.add(mark, c);
+            pb.add(mark, c, mark ? p->g.rows[c].deg : 0);
             ls->edges_inv += ok[q] ? 1 : 0;
         }
         pb.flush(*p, out, *ls, false);
@@ -292,9 +297,10 @@ struct PullOp {
                 ls->updates++;
             }
         }
-        const bool doit = valid && (need || improved) && claim_push(p->g.push_tag, x, tag);
+        int deg;
+        const bool doit = claim_with_deg(*p, valid && (need || improved), x, tag, deg);
         ls->frontier += doit ? 1 : 0;
-        pb.add(doit, x);
+        pb.add(doit, x, deg);
         pb.flush(*p, out, *ls, false);
     }
     // an item shared by the warp (part of a CTA item)
@@ -309,9 +315,10 @@ struct PullOp {
                 ls->updates++;
             }
         }
-        const bool doit = lane_id() == 0 && (nd || improved) && claim_push(p->g.push_tag, x, tag);
+        int deg;
+        const bool doit = claim_with_deg(*p, lane_id() == 0 && (nd || improved), x, tag, deg);
         ls->frontier += doit ? 1 : 0;
-        pb.add(doit, x);
+        pb.add(doit, x, deg);
         pb.flush(*p, out, *ls, false);
     }
 };
@@ -420,9 +427,10 @@ __device__ __forceinline__ long long lower_col(const int2* adj, long long lo, lo
 __device__ bool hash_insert(const UpdParams& p, unsigned long long pair, int w) {
     unsigned long long h = dmix64(pair) & p.hmask;
     for (unsigned long long probe = 0; probe <= p.hmask; probe++) {
-        const unsigned long long old = atomicCAS(&p.hpair[h], kHashEmpty, pair);
+        DelSlot* slot = &p.hset[h];
+        const unsigned long long old = atomicCAS(&slot->pair, kHashEmpty, pair);
         if (old == kHashEmpty || old == pair) {
-            const int ow = atomicCAS(&p.hw[h], kHashNoWeight, w);
+            const int ow = atomicCAS(&slot->w, kHashNoWeight, w);
             if (ow == kHashNoWeight || ow == w) return true;
         }
         h = (h + 1) & p.hmask;
@@ -433,12 +441,35 @@ __device__ bool hash_insert(const UpdParams& p, unsigned long long pair, int w) 
 __device__ bool hash_contains(const UpdParams& p, unsigned long long pair, int w) {
     unsigned long long h = dmix64(pair) & p.hmask;
     for (unsigned long long probe = 0; probe <= p.hmask; probe++) {
-        const unsigned long long k = p.hpair[h];
-        if (k == kHashEmpty) return false;
-        if (k == pair && p.hw[h] == w) return true;
+        const DelSlot slot = p.hset[h];
+        if (slot.pair == kHashEmpty) return false;
+        if (slot.pair == pair && slot.w == w) return true;
         h = (h + 1) & p.hmask;
     }
     return false;
+}
+
+// Tombstones every live entry (col, w) of row r; with the twin index also their reverse
+// entries.  Returns the number of entries examined.
+__device__ unsigned long long tombstone_row(const UpdParams& p, const RowDesc& rd, int sorted_len, int col, int w,
+                                            bool with_twin) {
+    int2* adj = p.g.adj;
+    const long long sl = rd.start + sorted_len, end = rd.start + rd.deg;
+    long long j = lower_col(adj, rd.start, sl, col);
+    unsigned long long probed = 1;
+    for (; j < sl && adj[j].x == col; j++, probed++) {
+        if (adj[j].y == w) {
+            adj[j].y = -1;
+            if (with_twin) adj[p.g.twin[j]].y = -1;
+        }
+    }
+    for (j = sl; j < end; j++, probed++) {
+        if (adj[j].x == col && adj[j].y == w) {
+            adj[j].y = -1;
+            if (with_twin) adj[p.g.twin[j]].y = -1;
+        }
+    }
+    return probed;
 }
 
 }  // namespace
@@ -487,17 +518,15 @@ __global__ void k_delete(UpdParams p) {
                 cut = atomicExch(&p.g.inv_tag[cutv], p.epoch) != p.epoch;
                 if (cut) p.g.state[cutv] = kInfState;
             }
-#pragma unroll
-            for (int side = 0; side < 2; side++) {
-                const int r = side ? c.y : c.x, col = side ? c.x : c.y;
-                const RowDesc rd = p.g.rows[r];
-                const long long sl = rd.start + p.g.sorted_len[r], end = rd.start + rd.deg;
-                long long j = lower_col(p.g.adj, rd.start, sl, col);
-                probed += 1;
-                for (; j < sl && p.g.adj[j].x == col; j++, probed++)
-                    if (p.g.adj[j].y == c.z) p.g.adj[j].y = -1;
-                for (j = sl; j < end; j++, probed++)
-                    if (p.g.adj[j].x == col && p.g.adj[j].y == c.z) p.g.adj[j].y = -1;
+            const RowDesc ra = p.g.rows[a], rb = p.g.rows[b];
+            if (p.g.twin) {
+                // search the shorter row; each match's reverse entry is found through twin[]
+                const bool use_a = ra.deg <= rb.deg;
+                probed += tombstone_row(p, use_a ? ra : rb, p.g.sorted_len[use_a ? a : b], (int)(use_a ? b : a), c.z,
+                                        true);
+            } else {
+                probed += tombstone_row(p, ra, p.g.sorted_len[a], (int)b, c.z, false);
+                probed += tombstone_row(p, rb, p.g.sorted_len[b], (int)a, c.z, false);
             }
             if (c.z >= 0 && !hash_insert(p, dpair_key(a, b), c.z)) set_status(ctl, -4 /* deletion set full */);
         }
@@ -524,19 +553,26 @@ __global__ void k_append(UpdParams p) {
                 killed++;
             } else {
                 alive = 1;
+                long long at[2];
 #pragma unroll
                 for (int side = 0; side < 2; side++) {
                     const int r = side ? c.y : c.x, col = side ? c.x : c.y;
                     RowDesc* rd = &p.g.rows[r];
                     const int pos = atomicAdd(&rd->deg, 1);
                     if (pos < rd->cap) {
-                        p.g.adj[rd->start + pos] = make_int2(col, c.z);
+                        at[side] = rd->start + pos;
+                        p.g.adj[at[side]] = make_int2(col, c.z);
                     } else {
+                        at[side] = -1;
                         const int o = atomicAdd(&ctl->ovf_count, 1);
                         p.ovf[o] = make_int4(r, col, c.z, (int)i);
                         ovf++;
                         atomicCAS(&ctl->status, 0, kStatusOverflowPending);
                     }
+                }
+                if (p.g.twin && at[0] >= 0 && at[1] >= 0) {  // an overflow repacks, which rebuilds twins
+                    p.g.twin[at[0]] = (unsigned)at[1];
+                    p.g.twin[at[1]] = (unsigned)at[0];
                 }
             }
         }
@@ -549,7 +585,7 @@ __global__ void k_append(UpdParams p) {
 
 __device__ void update_body(UpdParams& p);
 
-__global__ void __launch_bounds__(256) k_update(UpdParams p) {
+__global__ void __launch_bounds__(256, 4) k_update(UpdParams p) {
     if (threadIdx.x == 0) s_nbar = 0;
     __syncthreads();
     update_body(p);
@@ -571,7 +607,7 @@ __device__ void update_body(UpdParams& p) {
     const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned nthreads = gridDim.x * blockDim.x;
     const bool leader = gtid == 0;
-    unsigned* pbuf = s_pbuf[threadIdx.x >> 5];
+    uint2* pbuf = s_pbuf[threadIdx.x >> 5];
     LocalStats ls;
     if (leader) ctl->ts[0] = globaltimer();
 
@@ -587,7 +623,7 @@ __device__ void update_body(UpdParams& p) {
     if (p.mode == 1) {
         if (blockIdx.x == 0 && threadIdx.x < 32) {
             if (lane == 0) g.push_tag[g.src] = tag0;
-            expand(lane == 0, (unsigned)g.src, p, relax0, ls);
+            expand((unsigned)g.src, lane == 0 ? g.rows[g.src].deg : 0, p, relax0, ls);
             ls.frontier += lane == 0 ? 1 : 0;
         }
         if (!grid_sync(ctl)) return;
@@ -601,8 +637,8 @@ __device__ void update_body(UpdParams& p) {
             const Out lvl0{g.it, &ctl->ltT[0], g.tcap, g.ic, &ctl->ltC[0], g.ccap};
             for (unsigned base = gtid - lane; base < nroots; base += nthreads) {
                 const unsigned i = base + lane;
-                const bool has = i < nroots;
-                expand(has, has ? __ldcg(&g.invq[i]) : 0u, p, lvl0, ls);
+                const unsigned v = i < nroots ? __ldcg(&g.invq[i]) : 0u;
+                expand(v, i < nroots ? g.rows[v].deg : 0, p, lvl0, ls);
             }
         }
         if (leader) ls.marked += nroots;
@@ -680,7 +716,7 @@ __device__ void update_body(UpdParams& p) {
                     newinv = true;
                 }
                 ls.marked += newinv ? 1 : 0;
-                expand(newinv, v, p, pjo, ls);
+                expand(v, newinv ? g.rows[v].deg : 0, p, pjo, ls);
             }
             if (!grid_sync(ctl)) return;
             hiT += __ldcg(&ctl->pjT);
@@ -705,11 +741,12 @@ __device__ void update_body(UpdParams& p) {
                         pa = relax_to(g.state, a, (sb >> 32) + (unsigned)c.z, b, c.z, __ldcg(&g.state[a]), ls);
                     ls.edges_relax += 2;
                 }
-                const bool db = pbv && claim_push(g.push_tag, (unsigned)c.y, tag0);
-                const bool da = pa && claim_push(g.push_tag, (unsigned)c.x, tag0);
+                int degb, dega;
+                const bool db = claim_with_deg(p, pbv, (unsigned)c.y, tag0, degb);
+                const bool da = claim_with_deg(p, pa, (unsigned)c.x, tag0, dega);
                 ls.frontier += (db ? 1 : 0) + (da ? 1 : 0);
-                pb.add(db, (unsigned)c.y);
-                pb.add(da, (unsigned)c.x);
+                pb.add(db, (unsigned)c.y, degb);
+                pb.add(da, (unsigned)c.x, dega);
                 pb.flush(p, relax0, ls, false);
             }
             pb.flush(p, relax0, ls, true);
