@@ -119,6 +119,13 @@ class Dist:
             self.pg.destroy_process_group()
 
 
+def whole_job_rate(dist: "Dist", batch: int, steps: int, local_seconds: float) -> tuple[float, float]:
+    """Replicas: every rank applies `steps` batches of `batch` changes; the job's time is the
+    slowest rank's.  Returns (change-edges/s over all ranks, max seconds)."""
+    t_max = dist.max(local_seconds)
+    return dist.world * batch * steps / t_max, t_max
+
+
 # ---- clocks ---------------------------------------------------------------------------------
 
 class ClockSampler:
@@ -321,9 +328,7 @@ def run_engine(args, dist: Dist) -> int:
     # the resets between steps launch restore copies and the flush (not library kernels);
     # library kernels per step: prepare, delete, append, update
     t_steps = [s.t_total_ms for s in stats]
-    t_total = sum(t_steps) * 1e-3
-    t_max = dist.max(t_total)
-    value = dist.world * batch * args.steps / t_max
+    value, t_max = whole_job_rate(dist, batch, args.steps, sum(t_steps) * 1e-3)
 
     # end-to-end through the C ABI with host buffers
     e2e_times = []
@@ -332,8 +337,7 @@ def run_engine(args, dist: Dist) -> int:
         dt, _ = e2e_step()
         e2e_times.append(dt)
     clk.__exit__(None, None, None)
-    e2e_t = dist.max(sum(e2e_times) / len(e2e_times))
-    e2e_value = dist.world * batch / e2e_t
+    e2e_value, e2e_t = whole_job_rate(dist, batch, 1, sum(e2e_times) / len(e2e_times))
 
     # roofline of the dominant kernel (the persistent update kernel)
     upd_ms = statistics.mean(s.t_update_ms for s in stats)

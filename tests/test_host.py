@@ -1,0 +1,187 @@
+"""Host-side parts of the library, CPU only: the C ABI's exported symbols, the seeded
+generators, the reference text formats, and the drop-in command line's argument handling."""
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import dynamicssspv2_gb300 as D
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def header_functions():
+    text = (ROOT / "include" / "dsssp.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(dsssp_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_every_declared_function_is_exported():
+    names = header_functions()
+    assert len(names) >= 25
+    out = subprocess.run(["nm", "-D", "--defined-only", str(D.LIB_PATH)], capture_output=True, text=True,
+                         check=True).stdout
+    exported = set(re.findall(r" T (dsssp_\w+)", out))
+    missing = [n for n in names if n not in exported]
+    assert not missing, f"declared but not exported: {missing}"
+    for n in names:
+        assert hasattr(D._lib, n)
+    assert set(D.EXPORTED) <= set(names)
+
+
+def test_errors_have_messages():
+    for code in range(0, -13, -1):
+        assert D._lib.dsssp_strerror(code).decode() != "unknown error"
+    assert D._lib.dsssp_strerror(-99).decode() == "unknown error"
+
+
+def _has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_has_gpu(), reason="checks the no-device path")
+def test_no_device_is_reported():
+    with pytest.raises(D.DsssspError) as e:
+        D.Graph(4, [0, 1], [1, 2], [1, 1])
+    assert e.value.code == D.E_NO_DEVICE
+
+
+# ---- generators ---------------------------------------------------------------------------
+
+def _keys(u, v):
+    return np.minimum(u, v).astype(np.int64) * (1 << 32) + np.maximum(u, v)
+
+
+def test_er_exact_distinct_and_deterministic():
+    u, v, w = D.gen_er(1000, 5000, 1, 100, 7)
+    assert len(u) == 5000
+    assert (u != v).all()
+    assert len(np.unique(_keys(u, v))) == 5000
+    assert w.min() >= 1 and w.max() <= 100
+    u2, v2, w2 = D.gen_er(1000, 5000, 1, 100, 7)
+    assert (u == u2).all() and (v == v2).all() and (w == w2).all()
+    u3, _, _ = D.gen_er(1000, 5000, 1, 100, 8)
+    assert not (u == u3).all()
+
+
+def test_rmat_is_skewed_and_exact():
+    u, v, w = D.gen_rmat(12, 30000, seed=3)
+    assert len(np.unique(_keys(u, v))) == 30000 and (u != v).all()
+    assert u.max() < 4096 and v.max() < 4096
+    deg = np.bincount(np.concatenate([u, v]), minlength=4096)
+    assert deg.max() > 20 * deg.mean()  # hubs
+    assert D.max_degree_vertex(4096, u, v) == int(np.argmax(deg))
+
+
+def test_grid_counts():
+    rows, cols = 64, 50
+    u, v, w = D.gen_grid(rows, cols, 0.05, 30, 1, 1000, 1)
+    e4 = rows * (cols - 1) + (rows - 1) * cols
+    assert len(u) == e4 - int(0.05 * e4) + 30
+    ru, cu, rv, cv = u // cols, u % cols, v // cols, v % cols
+    assert (np.maximum(abs(ru - rv), abs(cu - cv)) == 1).all()
+    assert len(np.unique(_keys(u, v))) == len(u)
+
+
+@pytest.mark.parametrize("kind", [D.INS_UNIFORM, D.INS_RMAT, D.INS_LOCAL])
+def test_change_batches(kind):
+    if kind == D.INS_LOCAL:
+        n, cols = 40 * 40, 40
+        u, v, w = D.gen_grid(40, 40, 0.0, 0, 1, 9, 2)
+        ch = D.gen_changes(n, u, v, w, 200, 300, kind, cols, 2.0, 0, 0, 1, 9, seed=5)
+    else:
+        n = 4096
+        u, v, w = D.gen_rmat(12, 20000, seed=2) if kind == D.INS_RMAT else D.gen_er(n, 20000, 1, 9, 2)
+        ch = D.gen_changes(n, u, v, w, 200, 300, kind, 12, 0.57, 0.19, 0.19, 1, 9, seed=5)
+    assert len(ch) == 500
+    ins, dels = ch[ch["op"] == 1], ch[ch["op"] == 0]
+    assert len(ins) == 200 and len(dels) == 300
+    existing = set(_keys(u, v).tolist())
+    ik = _keys(ins["u"], ins["v"])
+    assert len(set(ik.tolist())) == 200 and not (set(ik.tolist()) & existing)
+    assert (ins["u"] != ins["v"]).all()
+    lines = set(zip(u.tolist(), v.tolist(), w.tolist()))
+    assert all((a, b, c) in lines for a, b, c in zip(dels["u"].tolist(), dels["v"].tolist(), dels["w"].tolist()))
+    assert len(set(zip(dels["u"].tolist(), dels["v"].tolist()))) == 300
+    if kind == D.INS_LOCAL:
+        assert (np.maximum(abs(ins["u"] // cols - ins["v"] // cols), abs(ins["u"] % cols - ins["v"] % cols)) <= 2).all()
+    assert not (ch["op"][:200] == 1).all()  # shuffled
+
+
+# ---- text formats -------------------------------------------------------------------------
+
+def test_graph_and_change_files_round_trip(tmp_path):
+    g = tmp_path / "graph.txt"
+    g.write_text("0 1 2\n0  2 6 \n\n1 3 2\nbad line\n1 4\n4 2 2\n")
+    u, v, w = D.read_graph(str(g), 6)
+    assert list(zip(u, v, w)) == [(0, 1, 2), (0, 2, 6), (1, 3, 2), (4, 2, 2)]  # short lines skipped
+    c = tmp_path / "cE.txt"
+    c.write_text("0 1 2 0\n0  4 4 1 \n1 4 0 1\n3 2 1 7\n")  # the reference's generator writes double spaces
+    ch = D.read_changes(str(c), 6)
+    assert ch.tolist() == [(0, 1, 2, 0), (0, 4, 4, 1), (1, 4, 0, 1), (3, 2, 1, 7)]
+
+
+def test_out_of_range_vertex_and_missing_file(tmp_path):
+    g = tmp_path / "graph.txt"
+    g.write_text("0 1 2\n0 9 1\n")
+    with pytest.raises(D.DsssspError) as e:
+        D.read_graph(str(g), 6)
+    assert e.value.code == D.E_BAD_VERTEX
+    with pytest.raises(D.DsssspError) as e:
+        D.read_graph(str(tmp_path / "nope.txt"), 6)
+    assert e.value.code == D.E_IO
+    c = tmp_path / "c.txt"
+    c.write_text("0 7 1 1\n")
+    with pytest.raises(D.DsssspError) as e:
+        D.read_changes(str(c), 6)
+    assert e.value.code == D.E_BAD_VERTEX
+    c.write_text("0 7 1 3\n")  # ignored op: not checked, as in the reference
+    assert len(D.read_changes(str(c), 6)) == 1
+
+
+def test_sssp_file_semantics(tmp_path):
+    """read_SSSP (all_structure_undir.cuh:133-171): gaps and parent -1 are unreachable; the
+    reference's Dijkstra writes distances with cout (%g-like), which is accepted here."""
+    s = tmp_path / "SSSP.txt"
+    s.write_text("0 0 0\n1 0 2\n3 1 1.2e+06\n4 -1 6000\n")
+    parent, dist, lossy = D.read_sssp(str(s), 6)
+    assert parent.tolist() == [0, 0, -1, 1, -1, -1]
+    assert dist.tolist() == [0, 2, -1, 1200000, -1, -1]
+    assert lossy == 1
+
+
+def test_sssp_write_read_round_trip(tmp_path):
+    rng = np.random.default_rng(0)
+    n = 1000
+    parent = rng.integers(-1, n, n).astype(np.int32)
+    dist = np.where(parent == -1, -1, rng.integers(0, 1 << 31, n)).astype(np.int64)
+    out = tmp_path / "out.txt"
+    D.write_sssp(str(out), parent, dist)
+    p2, d2, lossy = D.read_sssp(str(out), n)
+    assert (p2 == parent).all() and (d2 == dist).all() and lossy == 0
+
+
+def test_large_file_parses_in_parallel_chunks(tmp_path):
+    u, v, w = D.gen_er(50000, 300000, 1, 100, 3)
+    g = tmp_path / "big.txt"
+    with open(g, "w") as f:
+        f.write("".join(f"{a} {b} {c}\n" for a, b, c in zip(u.tolist(), v.tolist(), w.tolist())))
+    u2, v2, w2 = D.read_graph(str(g), 50000)
+    assert (u2 == u).all() and (v2 == v).all() and (w2 == w).all()
+
+
+# ---- command line -----------------------------------------------------------------------------
+
+def test_cli_usage_and_errors(tmp_path):
+    r = subprocess.run([str(D.CLI_PATH)], capture_output=True, text=True)
+    assert r.returncode == 2 and "usage" in r.stderr
+    r = subprocess.run([str(D.CLI_PATH), str(tmp_path / "nope.txt"), "6", "6", "x", "y"], capture_output=True,
+                       text=True)
+    assert r.returncode == 1 and "reading the graph" in r.stderr
+    assert r.stdout.startswith("Reading input graph...")
