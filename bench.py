@@ -36,6 +36,8 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 WORKLOADS = {
+    "batch256": dict(kind="batch", count=256, nlo=3.0, nhi=6.0, degree=8, wlo=1, whi=100, flo=-3.0, fhi=-1.0,
+                     slack_pct=50, slack_min=16),
     "rmat22": dict(kind="rmat", scale=22, m=33_554_432, wlo=1, whi=100, n_ins=500_000, n_del=500_000),
     "er10k": dict(kind="er", n=10_000, m=50_000, wlo=1, whi=100, n_ins=500, n_del=500),
     "grid4096": dict(kind="grid", rows=4096, cols=4096, remove=0.05, diag=167_772, wlo=1, whi=1000,
@@ -45,6 +47,12 @@ WORKLOADS = {
 
 def describe(name: str) -> dict:
     w = WORKLOADS[name]
+    if w["kind"] == "batch":
+        return {"workload": name, "graphs": w["count"],
+                "graph": f"Erdos-Renyi, n log-uniform in [1e{w['nlo']:.0f}, 1e{w['nhi']:.0f}], average degree "
+                         f"{w['degree']}, w U[{w['wlo']},{w['whi']}], source vertex 0 of each",
+                "batch": f"per graph ceil(f*m), f log-uniform in [1e{w['flo']:.0f}, 1e{w['fhi']:.0f}], 50% insertions",
+                "seed": 0}
     if w["kind"] == "rmat":
         g = f"RMAT(.57,.19,.19,.05) scale {w['scale']}, {w['m']} edges, w U[{w['wlo']},{w['whi']}], src = max degree"
     elif w["kind"] == "er":
@@ -399,6 +407,161 @@ def run_engine(args, dist: Dist) -> int:
     return 0
 
 
+def make_batch_inputs(name: str):
+    """The batching workload: many independent graphs, each with its own batch."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import dynamicssspv2_gb300 as D
+
+    w = WORKLOADS[name]
+    rng = np.random.default_rng(0)
+    ns = np.round(10 ** rng.uniform(w["nlo"], w["nhi"], w["count"])).astype(np.int64)
+    fs = 10 ** rng.uniform(w["flo"], w["fhi"], w["count"])
+
+    def one(i):
+        n = int(ns[i])
+        m = n * w["degree"] // 2
+        u, v, wt = D.gen_er(n, m, w["wlo"], w["whi"], seed=1000 + i)
+        k = max(2, int(np.ceil(fs[i] * m)))
+        ch = D.gen_changes(n, u, v, wt, k // 2, k - k // 2, seed=2000 + i, wlo=w["wlo"], whi=w["whi"])
+        return n, u, v, wt, ch
+
+    with ThreadPoolExecutor(4) as ex:
+        return list(ex.map(one, range(w["count"])))
+
+
+def run_batching(args, dist: Dist) -> int:
+    """Many graphs: one batch per graph applied one by one with the plain update, against all
+    of them together in one launch sequence on a pooled graph store (autotuned)."""
+    import tempfile
+
+    import torch
+
+    import dynamicssspv2_gb300 as D
+    from dynamicssspv2_gb300.autotune import Autotuner
+    from dynamicssspv2_gb300.pool import GraphPool
+
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    t0 = time.perf_counter()
+    items = make_batch_inputs(args.workload)
+    t_gen = time.perf_counter() - t0
+    total_changes = sum(len(it[4]) for it in items)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+
+    # plain: one graph store per graph, batches applied one after another
+    plain = []
+    wl = WORKLOADS[args.workload]
+    slack = {"slack_pct": wl["slack_pct"], "slack_min": wl["slack_min"]}
+    for n, u, v, wt, ch in items:
+        g = D.Graph(n, u, v, wt, device=dev, **slack)
+        g.tree_compute(0)
+        g.snapshot()
+        d = torch.from_numpy(ch.view(np.int32).reshape(-1)).to(f"cuda:{dev}")
+        plain.append((g, d, len(ch)))
+    # batched: all graphs in one pool, all batches in one union batch
+    pool = GraphPool([(n, u, v, wt) for n, u, v, wt, _ in items], device=dev, **slack)
+    pool.tree_compute([0] * len(items))
+    union = pool.union_batch([(i, it[4]) for i, it in enumerate(items)])
+    d_union = torch.from_numpy(union.view(np.int32).reshape(-1)).to(f"cuda:{dev}")
+    cache = os.environ.get("DSSSP_AUTOTUNE_CACHE") or os.path.join(tempfile.gettempdir(), "dsssp_autotune.json")
+    tuned = Autotuner(cache).tune(pool.graph, union)
+    pool.graph.snapshot()
+
+    def flush_l2():
+        flush.fill_(1)
+        torch.cuda.synchronize(dev)
+
+    def plain_pass():
+        t_dev, t_wall = 0.0, 0.0
+        for g, d, k in plain:
+            g.restore()
+            flush_l2()
+            w0 = time.perf_counter()
+            g.apply_batch_async(d.data_ptr(), k)
+            st = g.batch_finish()
+            t_wall += time.perf_counter() - w0
+            t_dev += st.t_total_ms * 1e-3
+        return t_dev, t_wall
+
+    def pooled_pass():
+        pool.graph.restore()
+        flush_l2()
+        w0 = time.perf_counter()
+        pool.graph.apply_batch_async(d_union.data_ptr(), len(union))
+        st = pool.graph.batch_finish()
+        return st.t_total_ms * 1e-3, time.perf_counter() - w0, st
+
+    for _ in range(args.warmup):
+        plain_pass()
+        pooled_pass()
+    clk = ClockSampler(dev).__enter__()
+    if clk.proc:
+        time.sleep(1.0)
+    dist.barrier()
+    pd, pw, bd, bw, stats, repacks = 0.0, 0.0, 0.0, 0.0, None, 0
+    launches0 = D.launch_count()
+    for _ in range(args.steps):
+        a, b = plain_pass()
+        pd += a
+        pw += b
+        c, d_, stats = pooled_pass()
+        bd += c
+        bw += d_
+        repacks += stats.repacks
+    launches = D.launch_count() - launches0
+    dist.barrier()
+    clk.__exit__(None, None, None)
+    # exactness spot check: pooled result of every graph == its plain result
+    mismatches = 0
+    for i, (g, _, _) in enumerate(plain):
+        p_plain, d_plain = g.tree_read()
+        p_pool, d_pool = pool.tree_read(i)
+        mismatches += int((d_plain != d_pool).sum())
+    value, t_max = whole_job_rate(dist, total_changes, args.steps, bd)
+    plain_value, _ = whole_job_rate(dist, total_changes, args.steps, pd)
+    for g, _, _ in plain:
+        g.close()
+    pool.close()
+    dist.close()
+    if dist.rank != 0:
+        return 0
+    cfg = describe(args.workload)
+    cfg.update({"vertices": int(sum(it[0] for it in items)), "edges": int(sum(len(it[1]) for it in items)),
+                "changes": int(total_changes), "autotuned": tuned["opts"], "autotune_key": tuned["key"],
+                "timed": "sum of CUDA-event intervals of the batch kernels; graph restore + 256 MB flush "
+                         "before each update untimed", "parallelism": f"replicas x{dist.world}",
+                "slack": slack})
+    line = {
+        "metric": "change-edges/s (batched: all graphs' batches in one launch sequence)",
+        "value": value,
+        "unit": "change-edges/s",
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_max / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int32",
+        "data": "synthetic",
+        "config": cfg,
+        "plain": {"value": plain_value, "unit": "change-edges/s", "ms_per_step": 1e3 * pd / args.steps,
+                  "wall_ms_per_step": 1e3 * pw / args.steps},
+        "batched_over_plain": value / plain_value,
+        "batched_wall_ms_per_step": 1e3 * bw / args.steps,
+        "mismatched_distances": mismatches,
+        "pooled_repacks": repacks,
+        "gpu_launches": launches,
+        "detail": {"rounds": stats.rounds, "inv_levels": stats.inv_levels, "invalidated": stats.n_invalidated,
+                   "edges_relaxed": stats.edges_relaxed, "t_step1_ms": stats.t_step1_ms,
+                   "t_update_ms": stats.t_update_ms, "setup_gen_s": t_gen},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -410,7 +573,14 @@ def main() -> int:
     args = ap.parse_args()
     dist = Dist()
     if args.impl == "reference":
+        if WORKLOADS[args.workload]["kind"] == "batch":
+            if dist.rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the batching workload has no CPU reference "
+                                  "arm; see the rmat22 workload"}))
+            return 0
         return run_reference(args, dist)
+    if WORKLOADS[args.workload]["kind"] == "batch":
+        return run_batching(args, dist)
     return run_engine(args, dist)
 
 

@@ -97,10 +97,14 @@ _sig("dsssp_graph_info", C.c_int, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)
      C.POINTER(C.c_int64), C.POINTER(C.c_int32))
 _sig("dsssp_tree_load", C.c_int, _P, _i32p, _i64p)
 _sig("dsssp_tree_compute", C.c_int, _P, C.c_int32, C.POINTER(Stats))
+_sig("dsssp_tree_compute_multi", C.c_int, _P, _i32p, C.c_int32, C.POINTER(Stats))
+_sig("dsssp_forest_load", C.c_int, _P, _i32p, _i64p)
 _sig("dsssp_tree_read", C.c_int, _P, _P, _P)
 _sig("dsssp_apply_batch", C.c_int, _P, _P, C.c_int64, _P, C.POINTER(Stats))
 _sig("dsssp_apply_batch_async", C.c_int, _P, _P, C.c_int64, _P)
 _sig("dsssp_batch_finish", C.c_int, _P, C.POINTER(Stats))
+_sig("dsssp_graph_set_opts", C.c_int, _P, C.POINTER(Opts))
+_sig("dsssp_graph_get_opts", C.c_int, _P, C.POINTER(Opts))
 _sig("dsssp_graph_snapshot", C.c_int, _P)
 _sig("dsssp_graph_restore", C.c_int, _P, _P)
 _sig("dsssp_graph_compact", C.c_int, _P)
@@ -129,8 +133,8 @@ NOALLOC_MAX_ENTRIES = 1 << 20
 
 EXPORTED = [
     "dsssp_default_opts", "dsssp_graph_create", "dsssp_graph_destroy", "dsssp_graph_info", "dsssp_tree_load",
-    "dsssp_tree_compute", "dsssp_tree_read", "dsssp_apply_batch", "dsssp_apply_batch_async", "dsssp_batch_finish",
-    "dsssp_graph_snapshot", "dsssp_graph_restore", "dsssp_graph_compact", "dsssp_host_alloc", "dsssp_host_free",
+    "dsssp_tree_compute", "dsssp_tree_compute_multi", "dsssp_forest_load", "dsssp_tree_read", "dsssp_apply_batch", "dsssp_apply_batch_async", "dsssp_batch_finish",
+    "dsssp_graph_set_opts", "dsssp_graph_get_opts", "dsssp_graph_snapshot", "dsssp_graph_restore", "dsssp_graph_compact", "dsssp_host_alloc", "dsssp_host_free",
     "dsssp_launch_count", "dsssp_last_error", "dsssp_strerror", "dsssp_free", "dsssp_read_graph_file",
     "dsssp_read_changes_file", "dsssp_read_sssp_file", "dsssp_write_sssp_file", "dsssp_gen_er", "dsssp_gen_rmat",
     "dsssp_gen_grid", "dsssp_gen_changes", "dsssp_max_degree_vertex", "dsssp_sssp_noalloc",
@@ -231,6 +235,19 @@ class Graph:
         _check(_lib.dsssp_tree_compute(self._h, int(src), C.byref(st)), "tree_compute")
         return st
 
+    def tree_compute_multi(self, srcs) -> Stats:
+        srcs = np.ascontiguousarray(srcs, np.int32)
+        st = Stats()
+        _check(_lib.dsssp_tree_compute_multi(self._h, srcs, len(srcs), C.byref(st)), "tree_compute_multi")
+        return st
+
+    def forest_load(self, parent, dist) -> None:
+        parent = np.ascontiguousarray(parent, np.int32)
+        dist = np.ascontiguousarray(dist, np.int64)
+        if len(parent) != self.n or len(dist) != self.n:
+            raise ValueError("tree arrays must have n entries")
+        _check(_lib.dsssp_forest_load(self._h, parent, dist), "forest_load")
+
     def tree_read(self, parent: np.ndarray | None = None, dist: np.ndarray | None = None):
         if parent is None:
             parent = np.empty(self.n, np.int32)
@@ -253,6 +270,14 @@ class Graph:
         st = Stats()
         _check(_lib.dsssp_batch_finish(self._h, C.byref(st)), "batch_finish")
         return st
+
+    def set_opts(self, opts: Opts) -> None:
+        _check(_lib.dsssp_graph_set_opts(self._h, C.byref(opts)), "set_opts")
+
+    def get_opts(self) -> Opts:
+        o = Opts()
+        _check(_lib.dsssp_graph_get_opts(self._h, C.byref(o)), "get_opts")
+        return o
 
     def snapshot(self) -> None:
         _check(_lib.dsssp_graph_snapshot(self._h), "snapshot")

@@ -124,7 +124,7 @@ struct DevGraph {
     long long ccap;
     Ctl* ctl;
     int n;
-    int src;
+    int src;  // lowest root (informational; kernels treat any vertex that is its own parent as a root)
 };
 
 struct UpdParams {
@@ -141,6 +141,8 @@ struct UpdParams {
     int chunk;        // edges per CTA item
     int bfs_levels;
     int mode;         // 0 = batch update, 1 = from scratch (state already reset)
+    const int* srcs;  // mode 1: the sources (every root is its own parent)
+    int nsrc;
     long long max_rounds;
 };
 

@@ -6,6 +6,7 @@
 // 42-91): rows live on the device, sorted by neighbour, each with free slots so insertions
 // append in place.  A row that runs out of slots triggers a repack (rows re-sorted, tombstones
 // dropped, slack restored) and the batch resumes after it.
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <cstdlib>
@@ -216,9 +217,18 @@ __global__ void k_tree_unpack(const unsigned long long* state, int n, int* paren
     }
 }
 
-__global__ void k_state_reset(unsigned long long* state, int n, int src) {
+__global__ void k_state_reset(unsigned long long* state, int n) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v < n) state[v] = v == src ? (unsigned long long)(unsigned)src : kInfState;
+    if (v < n) state[v] = kInfState;
+}
+
+// Sources: distance 0, own parent.  Ids are checked; a bad one sets DSSSP_E_BAD_VERTEX.
+__global__ void k_set_sources(unsigned long long* state, int n, const int* srcs, int k, Ctl* ctl) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k) return;
+    const int s = srcs[i];
+    if (s < 0 || s >= n) set_status(ctl, DSSSP_E_BAD_VERTEX);
+    else state[s] = (unsigned long long)(unsigned)s;
 }
 
 // ---- host helpers --------------------------------------------------------------------------
@@ -299,6 +309,10 @@ struct dsssp_graph {
     long long s_entries = 0;
     int s_src = -1;
     bool has_snap = false;
+    bool has_tree = false;
+    bool s_has_tree = false;
+    int* d_srcs = nullptr;  // sources of the last from-scratch computation
+    int srcs_cap = 0;
 };
 
 namespace dsssp {
@@ -519,6 +533,8 @@ UpdParams make_params(const dsssp_graph* g, const int4* chg, long long k, int mo
     p.chunk = g->o.chunk;
     p.bfs_levels = g->o.bfs_levels;
     p.mode = mode;
+    p.srcs = g->d_srcs;
+    p.nsrc = 0;
     p.max_rounds = g->o.max_rounds > 0 ? g->o.max_rounds : 2LL * g->n + 16;
     return p;
 }
@@ -645,10 +661,12 @@ int finish_batch(dsssp_graph* g, dsssp_stats* st) {
         repacks = 1;
         CK(cudaMemsetAsync(&g->dg.ctl->status, 0, sizeof(int), s), "status reset");
         UpdParams p = make_params(g, g->pend_chg, g->pend_k, 0);
+        // the front interval now spans the repack; the update interval is the resumed launch
+        if (g->pend_events) CK(cudaEventRecord(g->ev[1], s), "event");
         CK(launch_update(p, g->coop_grid, g->o.block, s), "update kernel");
+        if (g->pend_events) CK(cudaEventRecord(g->ev[2], s), "event");
         CK(cudaMemcpyAsync(g->h_ctl, g->dg.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s), "status read");
         CK(cudaStreamSynchronize(s), "batch");
-        g->pend_events = false;  // the event interval does not cover the repack
     }
     fill_stats(g, *g->h_ctl, st, g->pend_events, g->pend_k, repacks);
     if (g->h_ctl->status != 0) reset_tags(g, s);
@@ -730,7 +748,7 @@ void dsssp_graph_destroy(dsssp_graph* g) {
     dfree(d.push_tag); dfree(d.jm); dfree(d.invq); dfree(d.rt0); dfree(d.rt1); dfree(d.rc0); dfree(d.rc1);
     dfree(d.it); dfree(d.ic); dfree(d.ctl);
     dfree(g->d_chg); dfree(g->d_ins_state); dfree(g->d_ovf); dfree(g->d_hset); dfree(d.twin); dfree(g->s_twin);
-    dfree(g->d_par); dfree(g->d_dist);
+    dfree(g->d_par); dfree(g->d_dist); dfree(g->d_srcs);
     dfree(g->s_state); dfree(g->s_rows); dfree(g->s_sorted); dfree(g->s_adj);
     if (g->h_ctl) cudaFreeHost(g->h_ctl);
     for (auto& e : g->ev)
@@ -877,7 +895,7 @@ int dsssp_graph_info(const dsssp_graph* g, int64_t* n, int64_t* entries, int64_t
     return DSSSP_OK;
 }
 
-int dsssp_tree_load(dsssp_graph* g, const int32_t* parent, const int64_t* dist) {
+static int tree_load_impl(dsssp_graph* g, const int32_t* parent, const int64_t* dist, bool forest) {
     if (!g || !parent || !dist) return fail(DSSSP_E_INVAL, "tree_load: NULL argument");
     int rc = set_device(g);
     if (rc) return rc;
@@ -898,49 +916,84 @@ int dsssp_tree_load(dsssp_graph* g, const int32_t* parent, const int64_t* dist) 
     count_launch(1);
     CK(cudaMemcpyAsync(g->h_ctl, g->dg.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s), "tree load");
     CK(cudaStreamSynchronize(s), "tree load");
+    const unsigned long long roots = g->h_ctl->stat[0];
+    int bad = 0;
     if (g->h_ctl->status != 0) {
-        cudaMemsetAsync(g->dg.state, 0xFF, sizeof(unsigned long long) * (size_t)g->n, s);
-        cudaStreamSynchronize(s);
-        g->src = -1;
-        return fail(g->h_ctl->status, "tree_load: %s", g->h_ctl->status == DSSSP_E_OVERFLOW
-                                                              ? "a distance does not fit below 2^32-1"
-                                                              : "bad parent id, negative distance or root distance != 0");
+        bad = fail(g->h_ctl->status, "tree_load: %s", g->h_ctl->status == DSSSP_E_OVERFLOW
+                                                          ? "a distance does not fit below 2^32-1"
+                                                          : "bad parent id, negative distance or root distance != 0");
+    } else if (forest ? roots == 0 : roots != 1) {
+        bad = fail(DSSSP_E_BAD_TREE, "tree_load: %llu vertices are their own parent (need %s)", roots,
+                   forest ? "at least one root" : "exactly one root");
     }
-    if (g->h_ctl->stat[0] != 1) {
+    if (bad) {
         cudaMemsetAsync(g->dg.state, 0xFF, sizeof(unsigned long long) * (size_t)g->n, s);
         cudaStreamSynchronize(s);
         g->src = -1;
-        return fail(DSSSP_E_BAD_TREE, "tree_load: %llu vertices are their own parent (need exactly one root)",
-                    (unsigned long long)g->h_ctl->stat[0]);
+        g->has_tree = false;
+        return bad;
     }
     g->src = (int)g->h_ctl->stat[1];
+    g->has_tree = true;
     return DSSSP_OK;
 }
 
-int dsssp_tree_compute(dsssp_graph* g, int32_t src, dsssp_stats* st) {
-    if (!g) return fail(DSSSP_E_INVAL, "tree_compute: NULL graph");
-    if (src < 0 || src >= g->n) return fail(DSSSP_E_BAD_VERTEX, "tree_compute: source %d outside 0..%d", src, g->n - 1);
+int dsssp_tree_load(dsssp_graph* g, const int32_t* parent, const int64_t* dist) {
+    return tree_load_impl(g, parent, dist, false);
+}
+
+int dsssp_forest_load(dsssp_graph* g, const int32_t* parent, const int64_t* dist) {
+    return tree_load_impl(g, parent, dist, true);
+}
+
+int dsssp_tree_compute_multi(dsssp_graph* g, const int32_t* srcs, int32_t k, dsssp_stats* st) {
+    if (!g || k < 1 || !srcs) return fail(DSSSP_E_INVAL, "tree_compute: NULL graph or no source");
     int rc = set_device(g);
     if (rc) return rc;
     if (g->pending) return fail(DSSSP_E_INVAL, "tree_compute: a batch is still pending");
+    for (int32_t i = 0; i < k; i++)
+        if (srcs[i] < 0 || srcs[i] >= g->n)
+            return fail(DSSSP_E_BAD_VERTEX, "tree_compute: source %d outside 0..%d", srcs[i], g->n - 1);
     cudaStream_t s = g->stream;
-    g->src = src;
+    if (k > g->srcs_cap) {
+        dfree(g->d_srcs);
+        g->srcs_cap = 0;
+        rc = dalloc(&g->d_srcs, (size_t)k, "source list");
+        if (rc) return rc;
+        g->srcs_cap = k;
+    }
+    // the sources are de-duplicated so each is pushed once
+    std::vector<int32_t> uniq(srcs, srcs + k);
+    std::sort(uniq.begin(), uniq.end());
+    uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+    const int nsrc = (int)uniq.size();
     rc = clear_ctl(g, s);
     if (rc) return rc;
+    CK(cudaMemcpyAsync(g->d_srcs, uniq.data(), sizeof(int) * (size_t)nsrc, cudaMemcpyHostToDevice, s), "sources");
     const bool ev = g->o.timing != 0;
     if (ev) CK(cudaEventRecord(g->ev[0], s), "event");
-    k_state_reset<<<blocks_for(g->n), kThreads, 0, s>>>(g->dg.state, g->n, src);
-    count_launch(1);
+    k_state_reset<<<blocks_for(g->n), kThreads, 0, s>>>(g->dg.state, g->n);
+    k_set_sources<<<blocks_for(nsrc), kThreads, 0, s>>>(g->dg.state, g->n, g->d_srcs, nsrc, g->dg.ctl);
+    count_launch(2);
     if (ev) CK(cudaEventRecord(g->ev[1], s), "event");
     UpdParams p = make_params(g, nullptr, 0, 1);
+    p.nsrc = nsrc;
     CK(launch_update(p, g->coop_grid, g->o.block, s), "update kernel");
     if (ev) CK(cudaEventRecord(g->ev[2], s), "event");
     CK(cudaMemcpyAsync(g->h_ctl, g->dg.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s), "status read");
     CK(cudaStreamSynchronize(s), "tree compute");
+    g->src = uniq[0];
+    g->has_tree = g->h_ctl->status == 0;
     fill_stats(g, *g->h_ctl, st, ev, 0, 0);
     if (g->h_ctl->status != 0) reset_tags(g, s);
     if (g->h_ctl->stat[ST_DIST_OVF] > 0 && g->h_ctl->status == 0) return status_code(DSSSP_E_OVERFLOW);
     return status_code(g->h_ctl->status);
+}
+
+int dsssp_tree_compute(dsssp_graph* g, int32_t src, dsssp_stats* st) {
+    if (g && (src < 0 || src >= g->n))
+        return fail(DSSSP_E_BAD_VERTEX, "tree_compute: source %d outside 0..%d", src, g->n - 1);
+    return dsssp_tree_compute_multi(g, &src, 1, st);
 }
 
 int dsssp_tree_read(dsssp_graph* g, int32_t* parent, int64_t* dist) {
@@ -967,7 +1020,7 @@ int dsssp_apply_batch_async(dsssp_graph* g, const dsssp_change* d_changes, int64
     int rc = set_device(g);
     if (rc) return rc;
     if (g->pending) return fail(DSSSP_E_INVAL, "apply_batch: previous batch not finished");
-    if (g->src < 0) return fail(DSSSP_E_BAD_TREE, "apply_batch: no tree loaded");
+    if (!g->has_tree) return fail(DSSSP_E_BAD_TREE, "apply_batch: no tree loaded");
     cudaStream_t s = stream ? (cudaStream_t)stream : g->stream;
     if (k == 0) return DSSSP_OK;
     rc = ensure_batch(g, k);
@@ -1004,6 +1057,37 @@ int dsssp_apply_batch(dsssp_graph* g, const dsssp_change* changes, int64_t k, vo
     return finish_batch(g, st);
 }
 
+int dsssp_graph_set_opts(dsssp_graph* g, const dsssp_opts* o) {
+    if (!g || !o) return fail(DSSSP_E_INVAL, "set_opts: NULL argument");
+    int rc = check_opts(*o);
+    if (rc) return rc;
+    if (o->device != g->dev) return fail(DSSSP_E_INVAL, "set_opts: the device of a graph cannot change");
+    rc = set_device(g);
+    if (rc) return rc;
+    if (g->pending) return fail(DSSSP_E_INVAL, "set_opts: a batch is still pending");
+    int per_sm = 0;
+    if (update_occupancy(o->block, &per_sm) != cudaSuccess || per_sm < 1)
+        return fail(DSSSP_E_COOP, "set_opts: update kernel has no occupancy at block %d", o->block);
+    if (o->ctas_per_sm > 0 && o->ctas_per_sm < per_sm) per_sm = o->ctas_per_sm;
+    const dsssp_opts old = g->o;
+    g->o = *o;
+    g->o.slack_pct = old.slack_pct;  // slack is fixed when rows are laid out
+    g->o.slack_min = old.slack_min;
+    rc = ensure_work(g);
+    if (rc) {
+        g->o = old;
+        return rc;
+    }
+    g->coop_grid = per_sm * g->num_sms;
+    return DSSSP_OK;
+}
+
+int dsssp_graph_get_opts(const dsssp_graph* g, dsssp_opts* o) {
+    if (!g || !o) return fail(DSSSP_E_INVAL, "get_opts: NULL argument");
+    *o = g->o;
+    return DSSSP_OK;
+}
+
 int dsssp_graph_snapshot(dsssp_graph* g) {
     if (!g) return fail(DSSSP_E_INVAL, "snapshot: NULL graph");
     int rc = set_device(g);
@@ -1035,6 +1119,7 @@ int dsssp_graph_snapshot(dsssp_graph* g) {
     CK(cudaStreamSynchronize(s), "snapshot");
     g->s_entries = g->entries;
     g->s_src = g->src;
+    g->s_has_tree = g->has_tree;
     g->has_snap = true;
     return DSSSP_OK;
 }
@@ -1065,6 +1150,7 @@ int dsssp_graph_restore(dsssp_graph* g, void* stream) {
         CK(cudaMemcpyAsync(g->dg.twin, g->s_twin, (size_t)g->s_cap * 4, cudaMemcpyDeviceToDevice, s), "restore");
     g->entries = g->s_entries;
     g->src = g->s_src;
+    g->has_tree = g->s_has_tree;
     return DSSSP_OK;
 }
 

@@ -46,7 +46,8 @@ constexpr size_t kOffRt0 = align256(kOffTag + 4 * kMaxV);
 constexpr size_t kOffRt1 = align256(kOffRt0 + 8 * kTcap);
 constexpr size_t kOffRc0 = align256(kOffRt1 + 8 * kTcap);
 constexpr size_t kOffRc1 = align256(kOffRc0 + 8 * kCcap);
-constexpr size_t kScratchBytes = align256(kOffRc1 + 8 * kCcap);
+constexpr size_t kOffSrc = align256(kOffRc1 + 8 * kCcap);
+constexpr size_t kScratchBytes = align256(kOffSrc + sizeof(int));
 
 // The work space.  Shared by every call on a device; kept between calls.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -88,13 +89,14 @@ __global__ void k_noalloc_init(unsigned char* base, int n, long long nnz, const 
     }
 }
 
-__global__ void k_noalloc_ctl(unsigned char* base, const long long* off, int n, long long nnz) {
+__global__ void k_noalloc_ctl(unsigned char* base, const long long* off, int n, long long nnz, int src) {
     Ctl* ctl = reinterpret_cast<Ctl*>(base + kOffCtl);
     unsigned* w = reinterpret_cast<unsigned*>(ctl);
     for (unsigned i = threadIdx.x; i < sizeof(Ctl) / 4; i += blockDim.x) w[i] = 0;
     __syncthreads();
     if (threadIdx.x == 0) {
         ctl->round_base = 1;
+        *reinterpret_cast<int*>(base + kOffSrc) = src;
         if (off[0] != 0 || off[n] != nnz) ctl->diag[7] = 1;
     }
 }
@@ -162,7 +164,7 @@ extern "C" int dsssp_sssp_noalloc(int32_t n, int64_t nnz, const int64_t* d_row_o
     cudaStream_t s = (cudaStream_t)stream;
     const int2* adj = reinterpret_cast<const int2*>(d_adj);
 
-    k_noalloc_ctl<<<1, 256, 0, s>>>(base, reinterpret_cast<const long long*>(d_row_off), n, nnz);
+    k_noalloc_ctl<<<1, 256, 0, s>>>(base, reinterpret_cast<const long long*>(d_row_off), n, nnz, src);
     const long long work = nnz > n ? nnz : n;
     const unsigned blocks = (unsigned)((work + kBlock - 1) / kBlock < 1024 ? (work + kBlock - 1) / kBlock : 1024);
     k_noalloc_init<<<blocks, kBlock, 0, s>>>(base, n, nnz, reinterpret_cast<const long long*>(d_row_off), adj, src);
@@ -188,6 +190,8 @@ extern "C" int dsssp_sssp_noalloc(int32_t n, int64_t nnz, const int64_t* d_row_o
     p.large_deg = kLarge;
     p.chunk = kChunk;
     p.mode = 1;
+    p.srcs = reinterpret_cast<const int*>(base + kOffSrc);
+    p.nsrc = 1;
     p.max_rounds = 2LL * n + 16;
     e = launch_update(p, ds->grid, kBlock, s);
     if (e != cudaSuccess) return fail(DSSSP_E_CUDA, "sssp_noalloc: update kernel: %s", cudaGetErrorString(e));

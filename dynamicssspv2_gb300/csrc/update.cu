@@ -511,9 +511,13 @@ __global__ void k_delete(UpdParams p) {
         unsigned cutv = 0;
         if (c.w == 0) {
             const unsigned a = (unsigned)c.x, b = (unsigned)c.y;
-            // gpuFunctions_undir.cuh:189-198: the child end is checked as b first, then as a
-            if (b != (unsigned)p.g.src && (unsigned)__ldcg(&p.g.state[b]) == a) cutv = b, cut = true;
-            else if (a != (unsigned)p.g.src && (unsigned)__ldcg(&p.g.state[a]) == b) cutv = a, cut = true;
+            // gpuFunctions_undir.cuh:189-198: the child end is checked as b first, then as a.
+            // A self-loop never cuts: its only parent relation is a root's (parent == itself),
+            // and roots are never cut off.
+            if (a != b) {
+                if ((unsigned)__ldcg(&p.g.state[b]) == a) cutv = b, cut = true;
+                else if ((unsigned)__ldcg(&p.g.state[a]) == b) cutv = a, cut = true;
+            }
             if (cut) {
                 cut = atomicExch(&p.g.inv_tag[cutv], p.epoch) != p.epoch;
                 if (cut) p.g.state[cutv] = kInfState;
@@ -621,10 +625,12 @@ __device__ void update_body(UpdParams& p) {
     const Out relax0{g.rt0, &ctl->rcT[0], g.tcap, g.rc0, &ctl->rcC[0], g.ccap};
 
     if (p.mode == 1) {
-        if (blockIdx.x == 0 && threadIdx.x < 32) {
-            if (lane == 0) g.push_tag[g.src] = tag0;
-            expand((unsigned)g.src, lane == 0 ? g.rows[g.src].deg : 0, p, relax0, ls);
-            ls.frontier += lane == 0 ? 1 : 0;
+        for (unsigned base = gtid - lane; base < (unsigned)p.nsrc; base += nthreads) {
+            const unsigned i = base + lane;
+            const unsigned v = i < (unsigned)p.nsrc ? (unsigned)p.srcs[i] : 0u;
+            if (i < (unsigned)p.nsrc) g.push_tag[v] = tag0;
+            expand(v, i < (unsigned)p.nsrc ? g.rows[v].deg : 0, p, relax0, ls);
+            ls.frontier += i < (unsigned)p.nsrc ? 1 : 0;
         }
         if (!grid_sync(ctl)) return;
     } else {
@@ -678,7 +684,7 @@ __device__ void update_body(UpdParams& p) {
                     t = kTagInv;
                 } else {
                     const unsigned par = (unsigned)__ldcg(&g.state[v]);
-                    t = (v == (unsigned)g.src || par == kNone) ? kTagOk : par;
+                    t = (par == v || par == kNone) ? kTagOk : par;  // a root, or unreachable
                 }
                 g.jm[v] = t;
             }

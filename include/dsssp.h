@@ -122,6 +122,16 @@ int dsssp_tree_load(dsssp_graph* g, const int32_t* parent, const int64_t* dist);
  * seqSSSPwithDist_undir.cpp to make the initial SSSP file). */
 int dsssp_tree_compute(dsssp_graph* g, int32_t src, dsssp_stats* st);
 
+/* Several sources at once: each vertex gets its distance to the nearest source.  With one
+ * source per connected component this is one tree per component, as used by the batching
+ * and serving layers (one graph store holding many tenant graphs).  No counterpart in the
+ * reference (its Dijkstra has one hard-coded source, seqSSSPwithDist_undir.cpp:196). */
+int dsssp_tree_compute_multi(dsssp_graph* g, const int32_t* srcs, int32_t k, dsssp_stats* st);
+
+/* Like dsssp_tree_load, but any number (>= 1) of roots: a forest of shortest-path trees,
+ * e.g. one per tenant graph of a pooled graph store. */
+int dsssp_forest_load(dsssp_graph* g, const int32_t* parent, const int64_t* dist);
+
 /* Reads the current tree back into host arrays of n entries (either may be NULL).
  * Replaces printSSSP and the host print of SSSPmainForUndirected.cu:298-312. */
 int dsssp_tree_read(dsssp_graph* g, int32_t* parent, int64_t* dist);
@@ -141,6 +151,12 @@ int dsssp_apply_batch(dsssp_graph* g, const dsssp_change* changes, int64_t k, vo
 int dsssp_apply_batch_async(dsssp_graph* g, const dsssp_change* d_changes, int64_t k,
                             void* stream);
 int dsssp_batch_finish(dsssp_graph* g, dsssp_stats* st);
+
+/* Changes the launch tunables of a graph (all fields but device and the slack, which are
+ * fixed when the rows are laid out); used by the autotuner.  No counterpart in the reference
+ * (its block size is a compile-time macro, SSSPmainForUndirected.cu:11). */
+int dsssp_graph_set_opts(dsssp_graph* g, const dsssp_opts* o);
+int dsssp_graph_get_opts(const dsssp_graph* g, dsssp_opts* o);
 
 /* Device-side copy of the graph and tree, and its restore (benchmark repetition). */
 int dsssp_graph_snapshot(dsssp_graph* g);
