@@ -36,6 +36,8 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 WORKLOADS = {
+    "serve": dict(kind="serve", rmat_scale=24, rmat_m=134_217_728, tenants=32, tnlo=5.0, tnhi=6.30103, degree=8,
+                  wlo=1, whi=100, blo=1.0, bhi=5.0, loads=(0.25, 0.5, 0.75, 0.9, 1.1), requests=2000, checked=4),
     "batch256": dict(kind="batch", count=256, nlo=3.0, nhi=6.0, degree=8, wlo=1, whi=100, flo=-3.0, fhi=-1.0,
                      slack_pct=50, slack_min=16),
     "rmat22": dict(kind="rmat", scale=22, m=33_554_432, wlo=1, whi=100, n_ins=500_000, n_del=500_000),
@@ -47,6 +49,13 @@ WORKLOADS = {
 
 def describe(name: str) -> dict:
     w = WORKLOADS[name]
+    if w["kind"] == "serve":
+        return {"workload": name,
+                "graph": f"resident RMAT(.57,.19,.19,.05) scale {w['rmat_scale']} with {w['rmat_m']} edges + "
+                         f"{w['tenants']} Erdos-Renyi tenants, n log-uniform in [1e{w['tnlo']:.0f}, 2e6], "
+                         f"average degree {w['degree']}, w U[{w['wlo']},{w['whi']}]",
+                "batch": f"Poisson arrivals, sizes log-uniform in [1e{w['blo']:.0f}, 1e{w['bhi']:.0f}], 50% insertions",
+                "loads": list(w["loads"]), "requests_per_load": w["requests"], "seed": 0}
     if w["kind"] == "batch":
         return {"workload": name, "graphs": w["count"],
                 "graph": f"Erdos-Renyi, n log-uniform in [1e{w['nlo']:.0f}, 1e{w['nhi']:.0f}], average degree "
@@ -562,6 +571,112 @@ def run_batching(args, dist: Dist) -> int:
     return 0
 
 
+def run_serving(args, dist: Dist) -> int:
+    """Serving: resident tenants, Poisson request stream, continuous batching; capacity, then
+    p50/p99 latency and throughput at several offered loads; exactness on sampled tenants."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import dynamicssspv2_gb300 as D
+    from dynamicssspv2_gb300.serve import Request, Server, Tenant, random_batch, summarize
+    from oracle import pyoracle as O
+
+    w = WORKLOADS[args.workload]
+    dev = dist.local
+    t0 = time.perf_counter()
+    rng = np.random.default_rng(0)
+    ns = np.round(10 ** rng.uniform(w["tnlo"], w["tnhi"], w["tenants"])).astype(np.int64)
+
+    def er(i):
+        n = int(ns[i])
+        u, v, wt = D.gen_er(n, n * w["degree"] // 2, w["wlo"], w["whi"], seed=3000 + i)
+        return Tenant(f"er{i}", n, u, v, wt, src=0)
+
+    with ThreadPoolExecutor(4) as ex:
+        ers = list(ex.map(er, range(w["tenants"])))
+    n_r = 1 << w["rmat_scale"]
+    ru, rv, rw = D.gen_rmat(w["rmat_scale"], w["rmat_m"], 0.57, 0.19, 0.19, w["wlo"], w["whi"], seed=0)
+    tenants = [Tenant("rmat", n_r, ru, rv, rw, src=D.max_degree_vertex(n_r, ru, rv))] + ers
+    t_gen = time.perf_counter() - t0
+
+    def make_requests(count, rate, seed):
+        g = np.random.default_rng(seed)
+        sizes = np.round(10 ** g.uniform(w["blo"], w["bhi"], count)).astype(int)
+        who = g.integers(0, len(tenants), count)
+        arr = np.cumsum(g.exponential(1.0 / rate, count)) if rate else np.zeros(count)
+        return [Request(int(t), float(a), random_batch(g, tenants[int(t)], int(sz), wlo=w["wlo"], whi=w["whi"]))
+                for t, a, sz in zip(who, arr, sizes)]
+
+    srv = Server(tenants, device=dev, slack_pct=50, slack_min=16)
+    # exactness bookkeeping for the smallest ER tenants: their edge lists follow every request
+    checked = sorted(range(1, len(tenants)), key=lambda t: tenants[t].n)[: w["checked"]]
+    lines = {t: (tenants[t].u, tenants[t].v, tenants[t].w) for t in checked}
+
+    def track(reqs):
+        for r in sorted(reqs, key=lambda r: r.arrival):
+            if r.tenant in lines and not r.refused:
+                _, kept = O.updated_graph(tenants[r.tenant].n, *lines[r.tenant], r.changes, return_kept=True)
+                ins = r.changes[r.changes["op"] == 1]
+                lu = np.concatenate([lines[r.tenant][0], ins["u"]]).astype(np.int32)
+                lv = np.concatenate([lines[r.tenant][1], ins["v"]]).astype(np.int32)
+                lw = np.concatenate([lines[r.tenant][2], ins["w"]]).astype(np.int32)
+                keep = kept[: len(lu)].astype(bool)
+                lines[r.tenant] = (lu[keep], lv[keep], lw[keep])
+
+    warm = make_requests(2 * len(tenants), 0, 1)
+    srv.serve(warm, realtime=False)
+    track(warm)
+    sat = make_requests(w["requests"], 0, 2)
+    srv.serve(sat, realtime=False)
+    track(sat)
+    cap = summarize(sat)
+    cap_rate = cap["served"] / cap["span_s"]
+    loads = []
+    for i, load in enumerate(w["loads"]):
+        reqs = make_requests(w["requests"], load * cap_rate, 10 + i)
+        srv.serve(reqs)
+        track(reqs)
+        st = summarize(reqs)
+        st["offered_load"] = load
+        st["offered_requests_per_s"] = load * cap_rate
+        loads.append(st)
+    mism = 0
+    for t in checked:
+        p, d = srv.tree(t)
+        n = tenants[t].n
+        od, op = O.dijkstra(n, O.csr(n, *lines[t]), tenants[t].src)
+        mism += int((od != d).sum())
+    srv.close()
+    dist.close()
+    if dist.rank != 0:
+        return 0
+    cfg = describe(args.workload)
+    cfg.update({"admitted": len(srv.admitted), "vertices": int(sum(t.n for t in tenants)),
+                "edges": int(sum(len(t.u) for t in tenants)), "setup_gen_s": t_gen,
+                "timed": "host clock from arrival to completion of each request (includes queueing, host batch "
+                         "assembly, copies and the update)", "parallelism": "one pooled graph store, one GPU"})
+    line = {
+        "metric": "change-edges/s and p50/p99 per-batch latency under load (serving, continuous batching)",
+        "value": cap["change_edges_per_s"],
+        "unit": "change-edges/s",
+        "n_gpus": dist.world,
+        "steps": len(w["loads"]),
+        "warmup": 1,
+        "ms_per_step": cap["mean_ms"],
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int32",
+        "data": "synthetic",
+        "config": cfg,
+        "capacity": cap,
+        "loads": loads,
+        "checked_tenants": len(checked),
+        "mismatched_distances": mism,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -573,7 +688,7 @@ def main() -> int:
     args = ap.parse_args()
     dist = Dist()
     if args.impl == "reference":
-        if WORKLOADS[args.workload]["kind"] == "batch":
+        if WORKLOADS[args.workload]["kind"] in ("batch", "serve"):
             if dist.rank == 0:
                 print(json.dumps({"impl": "reference", "unavailable": "the batching workload has no CPU reference "
                                   "arm; see the rmat22 workload"}))
@@ -581,6 +696,8 @@ def main() -> int:
         return run_reference(args, dist)
     if WORKLOADS[args.workload]["kind"] == "batch":
         return run_batching(args, dist)
+    if WORKLOADS[args.workload]["kind"] == "serve":
+        return run_serving(args, dist)
     return run_engine(args, dist)
 
 
