@@ -54,6 +54,8 @@ class Opts(C.Structure):
         ("ctas_per_sm", C.c_int32),
         ("timing", C.c_int32),
         ("max_rounds", C.c_int64),
+        ("spare_pct", C.c_int32),
+        ("reserved0", C.c_int32),
     ]
 
 

@@ -31,6 +31,7 @@ constexpr unsigned long long kDistInf = 0xFFFFFFFFull;
 constexpr unsigned kTagOk = 0xFFFFFFFFu;   // pointer jumping: reaches the root untouched
 constexpr unsigned kTagInv = 0xFFFFFFFEu;  // pointer jumping: below a cut-off vertex
 constexpr int kStatusOverflowPending = 1;  // internal: an insertion did not fit its row
+constexpr unsigned kNoTwin = 0xFFFFFFFFu;   // twin not known yet (the other end overflowed)
 constexpr unsigned long long kHashEmpty = 0xFFFFFFFFFFFFFFFFull;
 constexpr int kHashNoWeight = -1;  // 0xFF byte fill; deletions with w < 0 are not hashed
 
@@ -122,6 +123,7 @@ struct DevGraph {
     uint2* ic;   // cut-off vertices' CTA items
     long long tcap;
     long long ccap;
+    long long cap_total;  // adjacency slots (bounds of twin-derived indices)
     Ctl* ctl;
     int n;
     int src;  // lowest root (informational; kernels treat any vertex that is its own parent as a root)
@@ -135,6 +137,7 @@ struct UpdParams {
     DelSlot* hset;    // deletion set: endpoint pair -> weight (open addressing)
     unsigned long long hmask;
     int4* ovf;        // insertions that did not fit their row: (row, col, wt, record)
+    long long* slot;  // per record, both directions: slot of the appended entry, -1 = overflowed
     unsigned epoch;
     int te;           // edges per thread item
     int large_deg;    // rows above this become CTA items

@@ -168,6 +168,136 @@ __global__ void k_pack_ovf(const int4* ovf, int novf, const long long* poff, int
     keys[poff[o.x] + atomicAdd(&cursor[o.x], 1)] = make_key(o.y, o.z);
 }
 
+// ---- in-place row growth (rows that ran out of slack move to the spare region) ----------
+
+struct GrowParams {
+    RowDesc* rows;
+    int2* adj;
+    unsigned* twin;
+    const int4* ovf;
+    int novf;
+    const int4* chg;
+    long long k;
+    const int* ins_state;
+    long long* slot;
+    int* need;                 // per vertex: overflowed entries of its row (0 = row not growing)
+    int* gidx;                 // per vertex: 1 + index in the grow list (0 = not growing)
+    unsigned* grow_list;       // rows that grow
+    unsigned* grow_count;
+    long long* old_start;      // per grow-list entry
+    int* old_cap;
+    unsigned long long* spare; // {top, end} of the spare region (bump allocator)
+    int* fail;
+    int slack_min;
+    long long cap_total;
+};
+
+__global__ void k_grow_count(GrowParams q) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= q.novf) return;
+    const int r = q.ovf[i].x;
+    if (atomicAdd(&q.need[r], 1) == 0) {
+        const unsigned j = atomicAdd(q.grow_count, 1u);
+        q.grow_list[j] = (unsigned)r;
+        q.gidx[r] = (int)j + 1;
+    }
+}
+
+// Warp per growing row: a region of 2 * (cap + need) + slack_min slots from the spare
+// region, the row's cap stored entries (and their twin words) copied there.
+__global__ void k_grow_move(GrowParams q) {
+    const unsigned j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    if (j >= *q.grow_count) return;
+    const unsigned r = q.grow_list[j];
+    const RowDesc rd = q.rows[r];
+    const long long ncap = 2LL * (rd.cap + q.need[r]) + q.slack_min;
+    unsigned long long pos = 0;
+    if (lane == 0) pos = atomicAdd(&q.spare[0], (unsigned long long)ncap);
+    pos = __shfl_sync(0xFFFFFFFFu, pos, 0);
+    if (pos + (unsigned long long)ncap > q.spare[1] || ncap > 0x7FFFFFFFLL) {
+        if (lane == 0) atomicExch(q.fail, 1);
+        return;
+    }
+    for (int e = (int)lane; e < rd.cap; e += 32) {
+        q.adj[pos + e] = q.adj[rd.start + e];
+        if (q.twin) q.twin[pos + e] = q.twin[rd.start + e];
+    }
+    if (lane == 0) {
+        q.old_start[j] = rd.start;
+        q.old_cap[j] = rd.cap;
+        RowDesc nr;
+        nr.start = (long long)pos;
+        nr.deg = rd.cap;  // the entries actually stored; overflowed ones are placed next
+        nr.cap = (int)ncap;
+        q.rows[r] = nr;
+    }
+}
+
+// Warp per grown row: every live entry re-links with its reverse entry, wherever either moved.
+// Each moved entry reads only its own twin word, which no other thread writes.
+__global__ void k_grow_fix(GrowParams q) {
+    const unsigned j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    if (j >= *q.grow_count || !q.twin) return;
+    const unsigned r = q.grow_list[j];
+    const long long ns = q.rows[r].start;
+    for (int e = (int)lane; e < q.old_cap[j]; e += 32) {
+        const long long at = ns + e;
+        const int2 x = q.adj[at];
+        const unsigned t = q.twin[at];
+        if (x.y < 0 || t == kNoTwin) continue;
+        const int c = x.x;  // the reverse entry lives in row c
+        const int gc = q.gidx[c];
+        // A moved partner re-links itself from its own (old) twin word, so only our own word
+        // is written for it; a partner that stayed gets our new slot.
+        const long long t2 = gc ? q.rows[c].start + ((long long)t - q.old_start[gc - 1]) : (long long)t;
+        if (t2 < 0 || t2 >= q.cap_total) {  // internal error: report, skip the access
+            atomicExch(q.fail, 2);
+            continue;
+        }
+        q.twin[at] = (unsigned)t2;
+        if (!gc) q.twin[t2] = (unsigned)at;
+    }
+}
+
+// Places the overflowed ends of every surviving insertion into its grown row and pairs twins.
+__global__ void k_grow_place(GrowParams q) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= q.k) return;
+    const int4 c = q.chg[i];
+    if (c.w != 1 || q.ins_state[i] != 1) return;
+    long long at[2] = {q.slot[2 * i], q.slot[2 * i + 1]};
+    if (at[0] >= 0 && at[1] >= 0) return;
+#pragma unroll
+    for (int side = 0; side < 2; side++) {
+        if (at[side] >= 0) {
+            // the end that fitted may sit in a row that moved in this growth step
+            const int r = side ? c.y : c.x;
+            const int gr = q.gidx[r];
+            if (gr) at[side] = q.rows[r].start + (at[side] - q.old_start[gr - 1]);
+            continue;
+        }
+        const int r = side ? c.y : c.x, col = side ? c.x : c.y;
+        const int pos = atomicAdd(&q.rows[r].deg, 1);
+        at[side] = q.rows[r].start + pos;
+        q.adj[at[side]] = make_int2(col, c.z);
+        q.slot[2 * i + side] = at[side];
+    }
+    if (q.twin) {
+        q.twin[at[0]] = (unsigned)at[1];
+        q.twin[at[1]] = (unsigned)at[0];
+    }
+}
+
+__global__ void k_grow_reset(GrowParams q) {
+    const unsigned j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= *q.grow_count) return;
+    const unsigned r = q.grow_list[j];
+    q.need[r] = 0;
+    q.gidx[r] = 0;
+}
+
 __global__ void k_int_to_ll(const int* a, int n, long long* b) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v < n) b[v] = a[v];
@@ -284,6 +414,18 @@ struct dsssp_graph {
     long long chg_cap = 0;
     int* d_ins_state = nullptr;
     int4* d_ovf = nullptr;
+    long long* d_slot = nullptr;        // per record: slots of both appended ends
+    // in-place row growth
+    unsigned long long* d_spare = nullptr;  // {top, end} of the spare region
+    int* d_need = nullptr;
+    int* d_gidx = nullptr;
+    unsigned* d_grow_list = nullptr;
+    unsigned* d_grow_count = nullptr;
+    long long* d_old_start = nullptr;
+    int* d_old_cap = nullptr;
+    int* d_fail = nullptr;
+    long long grow_cap = 0;
+    unsigned long long s_spare[2] = {0, 0};  // spare words saved with the snapshot
     DelSlot* d_hset = nullptr;  // deletion set of the batch
     unsigned long long hcap = 0;
     Ctl* h_ctl = nullptr;  // pinned mirror of the control block
@@ -364,12 +506,23 @@ int ensure_batch(dsssp_graph* g, long long k) {
     dfree(g->d_ins_state);
     dfree(g->d_ovf);
     dfree(g->d_hset);
+    dfree(g->d_slot);
+    dfree(g->d_grow_list);
+    dfree(g->d_old_start);
+    dfree(g->d_old_cap);
+    g->grow_cap = 0;
     g->chg_cap = 0;
     g->hcap = 0;
     int rc = dalloc(&g->d_chg, (size_t)cap, "change buffer");
     if (!rc) rc = dalloc(&g->d_ins_state, (size_t)cap, "insertion state");
     if (!rc) rc = dalloc(&g->d_ovf, (size_t)cap * 2, "overflow buffer");
     if (!rc) rc = dalloc(&g->d_hset, (size_t)h, "deletion set");
+    if (!rc) rc = dalloc(&g->d_slot, (size_t)cap * 2, "slot buffer");
+    const long long gl = 2 * cap < g->n ? 2 * cap : g->n;
+    if (!rc) rc = dalloc(&g->d_grow_list, (size_t)gl, "grow list");
+    if (!rc) rc = dalloc(&g->d_old_start, (size_t)gl, "grow list");
+    if (!rc) rc = dalloc(&g->d_old_cap, (size_t)gl, "grow list");
+    if (!rc) g->grow_cap = gl;
     if (!rc) {
         g->chg_cap = cap;
         g->hcap = h;
@@ -433,6 +586,15 @@ int layout_rows(dsssp_graph* g, unsigned long long* keys_in, long long total, co
         if (e == cudaSuccess) e = cudaMemcpyAsync(&cap_total, start + n, sizeof(long long), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) rc = cuda_fail(e, "row layout");
+    }
+    // rows take [0, main); [main, cap_total) is the spare region that rows running out of
+    // slack move into (bump allocator, reset by the next layout)
+    const long long main_slots = cap_total;
+    cap_total = main_slots + main_slots * g->o.spare_pct / 100 + 1024;
+    if (!rc) {
+        const unsigned long long sp[2] = {(unsigned long long)main_slots, (unsigned long long)cap_total};
+        cudaError_t e = cudaMemcpyAsync(g->d_spare, sp, sizeof(sp), cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) rc = cuda_fail(e, "spare region");
     }
     unsigned* twin = nullptr;
     if (!rc) rc = dalloc(&adj, (size_t)cap_total, "adjacency");
@@ -521,12 +683,14 @@ UpdParams make_params(const dsssp_graph* g, const int4* chg, long long k, int mo
     p.g = g->dg;
     p.g.n = g->n;
     p.g.src = g->src;
+    p.g.cap_total = g->cap_total;
     p.chg = chg;
     p.k = k;
     p.ins_state = g->d_ins_state;
     p.hset = g->d_hset;
     p.hmask = g->hcap ? g->hcap - 1 : 0;
     p.ovf = g->d_ovf;
+    p.slot = g->d_slot;
     p.epoch = g->epoch;
     p.te = g->o.small_deg;
     p.large_deg = g->o.large_deg;
@@ -624,6 +788,66 @@ void fill_stats(const dsssp_graph* g, const Ctl& c, dsssp_stats* st, bool events
     st->bytes_alg = upd + front;
 }
 
+constexpr int kSpareExhausted = 1;
+
+// Moves every row that overflowed in this batch into the spare region and places its
+// overflowed entries; kSpareExhausted if the region is too small (nothing lost: the caller
+// repacks, which folds the overflow list in).
+int grow_rows(dsssp_graph* g, int novf, cudaStream_t s) {
+    if (novf <= 0) return DSSSP_OK;
+    if (!g->d_need) {
+        int rc = dalloc(&g->d_need, (size_t)g->n, "row growth");
+        if (!rc) rc = dalloc(&g->d_gidx, (size_t)g->n, "row growth");
+        if (rc) return rc;
+        CK(cudaMemsetAsync(g->d_need, 0, sizeof(int) * (size_t)g->n, s), "row growth");
+        CK(cudaMemsetAsync(g->d_gidx, 0, sizeof(int) * (size_t)g->n, s), "row growth");
+    }
+    GrowParams q;
+    q.rows = g->dg.rows;
+    q.adj = g->dg.adj;
+    q.twin = g->dg.twin;
+    q.ovf = g->d_ovf;
+    q.novf = novf;
+    q.chg = g->pend_chg;
+    q.k = g->pend_k;
+    q.ins_state = g->d_ins_state;
+    q.slot = g->d_slot;
+    q.need = g->d_need;
+    q.gidx = g->d_gidx;
+    q.grow_list = g->d_grow_list;
+    q.grow_count = g->d_grow_count;
+    q.old_start = g->d_old_start;
+    q.old_cap = g->d_old_cap;
+    q.spare = g->d_spare;
+    q.fail = g->d_fail;
+    q.slack_min = g->o.slack_min > 4 ? g->o.slack_min : 4;
+    q.cap_total = g->cap_total;
+    CK(cudaMemsetAsync(g->d_grow_count, 0, sizeof(unsigned), s), "row growth");
+    CK(cudaMemsetAsync(g->d_fail, 0, sizeof(int), s), "row growth");
+    const long long rows_max = novf < g->grow_cap ? novf : g->grow_cap;
+    const unsigned wb = (unsigned)((rows_max * 32 + kThreads - 1) / kThreads);
+    k_grow_count<<<blocks_for(novf), kThreads, 0, s>>>(q);
+    k_grow_move<<<wb, kThreads, 0, s>>>(q);
+    count_launch(2);
+    int fail = 0;
+    CK(cudaMemcpyAsync(&fail, g->d_fail, sizeof(int), cudaMemcpyDeviceToHost, s), "row growth");
+    CK(cudaStreamSynchronize(s), "row growth");
+    if (fail) {
+        k_grow_reset<<<blocks_for(rows_max), kThreads, 0, s>>>(q);
+        count_launch(1);
+        CK(cudaStreamSynchronize(s), "row growth");
+        return kSpareExhausted;
+    }
+    k_grow_fix<<<wb, kThreads, 0, s>>>(q);
+    k_grow_place<<<blocks_for(g->pend_k), kThreads, 0, s>>>(q);
+    k_grow_reset<<<blocks_for(rows_max), kThreads, 0, s>>>(q);
+    count_launch(3);
+    CK(cudaMemcpyAsync(&fail, g->d_fail, sizeof(int), cudaMemcpyDeviceToHost, s), "row growth");
+    CK(cudaStreamSynchronize(s), "row growth");
+    if (fail) return dsssp::fail(DSSSP_E_CUDA, "row growth: twin index out of range (internal error)");
+    return DSSSP_OK;
+}
+
 // Enqueues one batch (records already on the device).
 int enqueue_batch(dsssp_graph* g, const int4* d_chg, long long k, cudaStream_t s) {
     const bool ev = g->o.timing != 0;
@@ -654,11 +878,15 @@ int finish_batch(dsssp_graph* g, dsssp_stats* st) {
     CK(cudaStreamSynchronize(s), "batch");
     int repacks = 0;
     if (g->h_ctl->status == kStatusOverflowPending) {
-        // insertions are placed and deletions applied; the rows that ran out of slack are
-        // rebuilt with the overflow entries folded in, then the update kernel runs
-        int rc = repack(g, g->d_ovf, g->h_ctl->ovf_count, s);
+        // deletions are applied and the insertions that fit are placed.  The rows that ran
+        // out of slack move to the spare region with room to grow; only when that region is
+        // used up is the whole adjacency repacked.  Then the update kernel runs.
+        int rc = grow_rows(g, g->h_ctl->ovf_count, s);
+        if (rc == kSpareExhausted) {
+            rc = repack(g, g->d_ovf, g->h_ctl->ovf_count, s);
+            repacks = 1;
+        }
         if (rc) return rc;
-        repacks = 1;
         CK(cudaMemsetAsync(&g->dg.ctl->status, 0, sizeof(int), s), "status reset");
         UpdParams p = make_params(g, g->pend_chg, g->pend_k, 0);
         // the front interval now spans the repack; the update interval is the resumed launch
@@ -703,6 +931,7 @@ void dsssp_default_opts(dsssp_opts* o) {
     o->ctas_per_sm = 0;
     o->timing = 1;
     o->max_rounds = 0;
+    o->spare_pct = 12;
 }
 
 const char* dsssp_strerror(int code) {
@@ -748,7 +977,9 @@ void dsssp_graph_destroy(dsssp_graph* g) {
     dfree(d.push_tag); dfree(d.jm); dfree(d.invq); dfree(d.rt0); dfree(d.rt1); dfree(d.rc0); dfree(d.rc1);
     dfree(d.it); dfree(d.ic); dfree(d.ctl);
     dfree(g->d_chg); dfree(g->d_ins_state); dfree(g->d_ovf); dfree(g->d_hset); dfree(d.twin); dfree(g->s_twin);
-    dfree(g->d_par); dfree(g->d_dist); dfree(g->d_srcs);
+    dfree(g->d_par); dfree(g->d_dist); dfree(g->d_srcs); dfree(g->d_slot); dfree(g->d_spare);
+    dfree(g->d_need); dfree(g->d_gidx); dfree(g->d_grow_list); dfree(g->d_grow_count); dfree(g->d_old_start);
+    dfree(g->d_old_cap); dfree(g->d_fail);
     dfree(g->s_state); dfree(g->s_rows); dfree(g->s_sorted); dfree(g->s_adj);
     if (g->h_ctl) cudaFreeHost(g->h_ctl);
     for (auto& e : g->ev)
@@ -760,7 +991,8 @@ void dsssp_graph_destroy(dsssp_graph* g) {
 static int check_opts(const dsssp_opts& o) {
     if (o.slack_pct < 0 || o.slack_min < 0 || o.small_deg < 4 || o.small_deg > 64 || o.small_deg % 4 ||
         o.large_deg < o.small_deg || o.chunk < 32 ||
-        o.bfs_levels < 0 || o.block < 32 || o.block > 256 || o.block % 32 || o.ctas_per_sm < 0 || o.max_rounds < 0)
+        o.bfs_levels < 0 || o.block < 32 || o.block > 256 || o.block % 32 || o.ctas_per_sm < 0 || o.max_rounds < 0 ||
+        o.spare_pct < 0 || o.spare_pct > 400)
         return fail(DSSSP_E_INVAL, "invalid dsssp_opts");
     return DSSSP_OK;
 }
@@ -816,6 +1048,9 @@ int dsssp_graph_create(int32_t n, int64_t m, const int32_t* u, const int32_t* v,
     if (!rc) rc = dalloc(&d.jm, N, "jm");
     if (!rc) rc = dalloc(&d.invq, N, "invq");
     if (!rc) rc = dalloc(&d.ctl, 1, "control block");
+    if (!rc) rc = dalloc(&g->d_spare, 2, "spare region words");
+    if (!rc) rc = dalloc(&g->d_grow_count, 1, "row growth");
+    if (!rc) rc = dalloc(&g->d_fail, 1, "row growth");
     if (rc) { dsssp_graph_destroy(g); return rc; }
     cudaStream_t s = g->stream;
     cudaMemsetAsync(d.state, 0xFF, sizeof(unsigned long long) * N, s);
@@ -1116,6 +1351,7 @@ int dsssp_graph_snapshot(dsssp_graph* g) {
     CK(cudaMemcpyAsync(g->s_adj, g->dg.adj, (size_t)g->cap_total * 8, cudaMemcpyDeviceToDevice, s), "snapshot");
     if (g->dg.twin)
         CK(cudaMemcpyAsync(g->s_twin, g->dg.twin, (size_t)g->cap_total * 4, cudaMemcpyDeviceToDevice, s), "snapshot");
+    CK(cudaMemcpyAsync(g->s_spare, g->d_spare, sizeof(g->s_spare), cudaMemcpyDeviceToHost, s), "snapshot");
     CK(cudaStreamSynchronize(s), "snapshot");
     g->s_entries = g->entries;
     g->s_src = g->src;
@@ -1148,6 +1384,7 @@ int dsssp_graph_restore(dsssp_graph* g, void* stream) {
     CK(cudaMemcpyAsync(g->dg.adj, g->s_adj, (size_t)g->s_cap * 8, cudaMemcpyDeviceToDevice, s), "restore");
     if (g->s_twin)
         CK(cudaMemcpyAsync(g->dg.twin, g->s_twin, (size_t)g->s_cap * 4, cudaMemcpyDeviceToDevice, s), "restore");
+    CK(cudaMemcpyAsync(g->d_spare, g->s_spare, sizeof(g->s_spare), cudaMemcpyHostToDevice, s), "restore");
     g->entries = g->s_entries;
     g->src = g->s_src;
     g->has_tree = g->s_has_tree;

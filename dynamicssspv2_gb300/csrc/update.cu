@@ -449,6 +449,14 @@ __device__ bool hash_contains(const UpdParams& p, unsigned long long pair, int w
     return false;
 }
 
+// Tombstones the reverse entry of slot j.  A twin word outside the adjacency is an internal
+// error: it is reported in the status word and the access is skipped.
+__device__ __forceinline__ void tombstone_twin(const UpdParams& p, long long j) {
+    const unsigned t = p.g.twin[j];
+    if ((long long)t < p.g.cap_total) p.g.adj[t].y = -1;
+    else set_status(p.g.ctl, -4 /* twin index out of range: internal error */);
+}
+
 // Tombstones every live entry (col, w) of row r; with the twin index also their reverse
 // entries.  Returns the number of entries examined.
 __device__ unsigned long long tombstone_row(const UpdParams& p, const RowDesc& rd, int sorted_len, int col, int w,
@@ -460,13 +468,13 @@ __device__ unsigned long long tombstone_row(const UpdParams& p, const RowDesc& r
     for (; j < sl && adj[j].x == col; j++, probed++) {
         if (adj[j].y == w) {
             adj[j].y = -1;
-            if (with_twin) adj[p.g.twin[j]].y = -1;
+            if (with_twin) tombstone_twin(p, j);
         }
     }
     for (j = sl; j < end; j++, probed++) {
         if (adj[j].x == col && adj[j].y == w) {
             adj[j].y = -1;
-            if (with_twin) adj[p.g.twin[j]].y = -1;
+            if (with_twin) tombstone_twin(p, j);
         }
     }
     return probed;
@@ -573,10 +581,11 @@ __global__ void k_append(UpdParams p) {
                         ovf++;
                         atomicCAS(&ctl->status, 0, kStatusOverflowPending);
                     }
+                    p.slot[2 * i + side] = at[side];
                 }
-                if (p.g.twin && at[0] >= 0 && at[1] >= 0) {  // an overflow repacks, which rebuilds twins
-                    p.g.twin[at[0]] = (unsigned)at[1];
-                    p.g.twin[at[1]] = (unsigned)at[0];
+                if (p.g.twin) {  // an overflowed end is placed (and paired) by the row growth
+                    if (at[0] >= 0) p.g.twin[at[0]] = at[1] >= 0 ? (unsigned)at[1] : kNoTwin;
+                    if (at[1] >= 0) p.g.twin[at[1]] = at[0] >= 0 ? (unsigned)at[0] : kNoTwin;
                 }
             }
         }

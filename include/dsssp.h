@@ -65,7 +65,10 @@ typedef struct {
     int32_t block;        /* threads per CTA of the update kernel (multiple of 32) */
     int32_t ctas_per_sm;  /* resident CTAs per SM of the update kernel; 0 = occupancy max */
     int32_t timing;       /* 1 = record CUDA events and phase timestamps into the stats */
-    int64_t max_rounds;   /* relaxation round cap; 0 = n + 1 */
+    int64_t max_rounds;   /* relaxation round cap; 0 = 2n + 16 */
+    int32_t spare_pct;    /* extra adjacency slots, percent of the laid-out rows, into which a
+                             row that runs out of slack moves (no full repack); 0..400 */
+    int32_t reserved0;
 } dsssp_opts;
 
 /* Counters of one batch (or one tree computation), read back from the device. */

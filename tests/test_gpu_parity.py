@@ -59,7 +59,8 @@ OPTION_SETS = [
     {"small_deg": 4, "large_deg": 4, "chunk": 32},          # rows above 4 edges on the CTA-chunk path
     {"small_deg": 4, "large_deg": 1 << 20},                # every row split into 4-edge thread items
     {"small_deg": 64, "large_deg": 1 << 20},               # 64-edge thread items
-    {"slack_pct": 0, "slack_min": 0},                      # every insertion overflows -> repack
+    {"slack_pct": 0, "slack_min": 0, "spare_pct": 300},    # every insertion overflows -> rows grow in place
+    {"slack_pct": 0, "slack_min": 0, "spare_pct": 0},      # ... and no spare region -> full repack
     {"block": 64, "ctas_per_sm": 1},
 ]
 
@@ -76,7 +77,8 @@ def test_random_er_batches(opts, seed):
     p, d, st = run_engine(n, u, v, w, ch, parent, dist, **opts)
     check_against_oracle(n, u, v, w, ch, 0, p, d, f"seed {seed} {opts}")
     if opts.get("slack_pct") == 0:
-        assert st.repacks == 1 and st.overflow_entries > 0
+        assert st.overflow_entries > 0
+        assert st.repacks == (1 if opts.get("spare_pct") == 0 else 0)
 
 
 def test_zero_weights_multiedges_selfloops():
@@ -188,6 +190,79 @@ def test_sequence_of_batches():
         g.apply_batch(ch)
         p, d = g.tree_read()
         check_against_oracle(n, cu, cv, cw, ch, 0, p, d, "after compact")
+
+
+def test_rows_grow_over_many_batches():
+    """Small slack: rows overflow again and again and move into the spare region; deletions
+    then find entries of moved rows through the twin index."""
+    n, m = 2000, 6000
+    u, v, w = D.gen_er(n, m, 1, 30, 21)
+    parent, dist = initial_tree(n, u, v, w)
+    cu, cv, cw = u.copy(), v.copy(), w.copy()
+    rng = np.random.default_rng(5)
+    grew = 0
+    with D.Graph(n, u, v, w, slack_pct=0, slack_min=1, spare_pct=200) as g:
+        g.tree_load(parent, dist)
+        for b in range(6):
+            hub = rng.integers(0, 50, 300)  # insertions concentrated on a few rows
+            other = rng.integers(0, n, 300)
+            ins = D.make_changes(hub, np.where(other == hub, (other + 1) % n, other), rng.integers(1, 30, 300),
+                                 np.ones(300))
+            idx = rng.choice(len(cu), 200, replace=False)
+            dels = D.make_changes(cu[idx], cv[idx], cw[idx], np.zeros(200))
+            ch = np.concatenate([ins, dels])[rng.permutation(500)]
+            st = g.apply_batch(ch)
+            grew += st.overflow_entries
+            p, d = g.tree_read()
+            check_against_oracle(n, cu, cv, cw, ch, 0, p, d, f"growth batch {b}")
+            _, kept = O.updated_graph(n, cu, cv, cw, ch, return_kept=True)
+            ins_ = ch[ch["op"] == 1]
+            lu = np.concatenate([cu, ins_["u"]]).astype(np.int32)
+            lv = np.concatenate([cv, ins_["v"]]).astype(np.int32)
+            lw = np.concatenate([cw, ins_["w"]]).astype(np.int32)
+            keep = kept[: len(lu)].astype(bool)
+            cu, cv, cw = lu[keep], lv[keep], lw[keep]
+        assert grew > 0 and st.repacks == 0
+
+
+def test_both_ends_grow_in_one_batch():
+    """Edges whose two rows both overflow in one batch: both rows move, and the twin words of
+    the pair must be re-linked from each side's own old value."""
+    n = 400
+    rng = np.random.default_rng(8)
+    u = rng.integers(0, 40, 3000).astype(np.int32)  # a dense core of 40 rows
+    v = rng.integers(0, 40, 3000).astype(np.int32)
+    keep = u != v
+    u, v = u[keep], v[keep]
+    u = np.concatenate([u, np.arange(40, n, dtype=np.int32)])
+    v = np.concatenate([v, rng.integers(0, 40, n - 40).astype(np.int32)])
+    w = rng.integers(1, 20, len(u)).astype(np.int32)
+    parent, dist = initial_tree(n, u, v, w)
+    cu, cv, cw = u, v, w
+    overflowed = 0
+    with D.Graph(n, u, v, w, slack_pct=0, slack_min=0, spare_pct=400) as g:
+        g.tree_load(parent, dist)
+        for b in range(4):
+            a = rng.integers(0, 40, 400)
+            c = rng.integers(0, 40, 400)
+            c = np.where(a == c, (c + 1) % 40, c)
+            ins = D.make_changes(a, c, rng.integers(1, 20, 400), np.ones(400))
+            idx = rng.choice(len(cu), 150, replace=False)
+            dels = D.make_changes(cu[idx], cv[idx], cw[idx], np.zeros(150))
+            ch = np.concatenate([ins, dels])[rng.permutation(550)]
+            st = g.apply_batch(ch)
+            assert st.repacks == 0
+            overflowed += st.overflow_entries
+            p, d = g.tree_read()
+            check_against_oracle(n, cu, cv, cw, ch, 0, p, d, f"core batch {b}")
+            _, kept = O.updated_graph(n, cu, cv, cw, ch, return_kept=True)
+            ins_ = ch[ch["op"] == 1]
+            lu = np.concatenate([cu, ins_["u"]]).astype(np.int32)
+            lv = np.concatenate([cv, ins_["v"]]).astype(np.int32)
+            lw = np.concatenate([cw, ins_["w"]]).astype(np.int32)
+            kp = kept[: len(lu)].astype(bool)
+            cu, cv, cw = lu[kp], lv[kp], lw[kp]
+    assert overflowed > 0
 
 
 def test_config_small_er_exact():
