@@ -347,14 +347,15 @@ def run_engine(args, dist: Dist) -> int:
     t_steps = [s.t_total_ms for s in stats]
     value, t_max = whole_job_rate(dist, batch, args.steps, sum(t_steps) * 1e-3)
 
-    # end-to-end through the C ABI with host buffers
+    # end-to-end through the C ABI with host buffers (median over the steps: host-side
+    # copies see more run-to-run noise than the device)
     e2e_times = []
-    for _ in range(max(3, min(args.steps, 10))):
+    for _ in range(max(5, min(args.steps, 20))):
         reset()
         dt, _ = e2e_step()
         e2e_times.append(dt)
     clk.__exit__(None, None, None)
-    e2e_value, e2e_t = whole_job_rate(dist, batch, 1, sum(e2e_times) / len(e2e_times))
+    e2e_value, e2e_t = whole_job_rate(dist, batch, 1, statistics.median(e2e_times))
 
     # roofline of the dominant kernel (the persistent update kernel)
     upd_ms = statistics.mean(s.t_update_ms for s in stats)
@@ -394,7 +395,8 @@ def run_engine(args, dist: Dist) -> int:
         "data": "synthetic",
         "config": cfg,
         "e2e": {"value": e2e_value, "unit": "change-edges/s", "h2d_bytes_per_step": nbytes,
-                "d2h_bytes_per_step": n * (4 + 8) + 320, "ms_per_step": 1e3 * e2e_t},
+                "d2h_bytes_per_step": n * (4 + 8) + 320, "ms_per_step": 1e3 * e2e_t,
+                "ms_all_steps": [round(1e3 * t, 4) for t in e2e_times], "timed": "host clock per step, median"},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": profiled_traffic(args.workload),
