@@ -405,7 +405,7 @@ def run_engine(args, dist: Dist) -> int:
         "cpu_baseline": cpu,
         "clocks": clocks,
         "detail": {
-            "rounds": s0.rounds, "frontier_total": s0.frontier_total, "edges_relaxed": s0.edges_relaxed,
+            "rounds": s0.rounds, "advances": s0.advances, "frontier_total": s0.frontier_total, "edges_relaxed": s0.edges_relaxed,
             "edges_inval": s0.edges_inval, "invalidated": s0.n_invalidated, "roots": s0.n_roots,
             "inv_levels": s0.inv_levels, "pj_passes": s0.pj_passes, "updates": s0.updates,
             "repacks": sum(s.repacks for s in stats), "t_step1_ms": s0.t_step1_ms, "t_update_ms": s0.t_update_ms,

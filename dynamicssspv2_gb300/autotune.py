@@ -2,10 +2,10 @@
 
 For a graph and a representative change batch it times a short list of candidate settings
 (edges per thread item, CTA-chunk thresholds, subtree-walk depth before pointer jumping, CTA
-size and residency), each on the same batch from the same starting state (device snapshot
-and restore), keeps the fastest, and caches it per size class -- (log2 vertices, log2
-adjacency entries, log2 batch size) -- in a JSON file, so later graphs of the same class
-skip the search.  The reference has no tunables (THREADS_PER_BLOCK is a compile-time macro,
+size and residency, near-far bucket width), each on the same batch from the same starting
+state (device snapshot and restore), keeps the fastest, and caches it per size class --
+(log2 vertices, log2 adjacency entries, log2 batch size) -- in a JSON file, so later graphs
+of the same class skip the search.  The reference has no tunables (THREADS_PER_BLOCK is a compile-time macro,
 SSSPmainForUndirected.cu:11).
 
 Tuning takes a device snapshot of the graph (replacing any snapshot taken before) and leaves
@@ -33,7 +33,7 @@ CANDIDATES = [
     {"ctas_per_sm": 2},
 ]
 
-TUNED_FIELDS = ("small_deg", "large_deg", "chunk", "bfs_levels", "block", "ctas_per_sm")
+TUNED_FIELDS = ("small_deg", "large_deg", "chunk", "bfs_levels", "block", "ctas_per_sm", "delta")
 
 
 def default_cache_path() -> Path:
@@ -73,6 +73,17 @@ class Autotuner:
             setattr(o, k, v)
         return o
 
+    @staticmethod
+    def near_far_candidates(changes: np.ndarray) -> list:
+        """Near-far bucket widths scaled by the batch's mean edge weight (a multiple of the
+        typical edge keeps a few hops per bucket)."""
+        ch = np.asarray(changes)
+        live = ch[(ch["op"] == 0) | (ch["op"] == 1)] if len(ch) else ch
+        wbar = float(np.mean(live["w"])) if len(live) else 0.0
+        if wbar <= 0:
+            return []
+        return [{"delta": max(1, int(round(f * wbar)))} for f in (4.0, 12.0)]
+
     def tune(self, graph: Graph, changes: np.ndarray, force: bool = False) -> dict:
         """Picks the fastest candidate for (graph, changes), sets it on the graph and returns
         {"key", "opts", "ms", "trials"}; a cached class is applied without timing."""
@@ -85,7 +96,10 @@ class Autotuner:
             return {"key": key, "opts": best["opts"], "ms": best["ms"], "trials": [], "cached": True}
         graph.snapshot()
         trials = []
-        for cand in self.candidates:
+        cands = list(self.candidates)
+        if self.candidates is CANDIDATES:
+            cands += self.near_far_candidates(changes)
+        for cand in cands:
             o = self._apply(base, cand)
             try:
                 graph.set_opts(o)

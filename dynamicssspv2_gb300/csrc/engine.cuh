@@ -65,6 +65,7 @@ enum StatIdx {
     ST_OVF,
     ST_ITEMS,
     ST_DIST_OVF,
+    ST_ADVANCES,
     ST_COUNT
 };
 
@@ -93,7 +94,11 @@ struct __align__(128) Ctl {
     unsigned pjT;
     unsigned pjC;
     unsigned pjf[3];
-    unsigned pad4[21];
+    unsigned fc[2];  // near-far: far-list counts (double buffer)
+    unsigned pad4[19];
+    // line 4b: near-far threshold reduction (double buffer)
+    unsigned long long fmin[2];
+    unsigned long long pad4b[14];
     // line 5: barrier diagnostics (first timed-out barrier, arrivals then, CTAs that timed
     // out, max barrier count at exit, 0xFFFFFFFF - min barrier count at exit)
     unsigned diag[8];
@@ -121,6 +126,9 @@ struct DevGraph {
     uint2* rc1;
     uint2* it;   // cut-off vertices' thread items
     uint2* ic;   // cut-off vertices' CTA items
+    unsigned* far0;     // near-far: vertices whose distance is at or above the threshold
+    unsigned* far1;
+    unsigned* far_tag;  // far-list membership tag (de-duplication)
     long long tcap;
     long long ccap;
     long long cap_total;  // adjacency slots (bounds of twin-derived indices)
@@ -144,6 +152,7 @@ struct UpdParams {
     int chunk;        // edges per CTA item
     int bfs_levels;
     int mode;         // 0 = batch update, 1 = from scratch (state already reset)
+    unsigned long long delta;  // near-far bucket width; 0 = plain frontier relaxation
     const int* srcs;  // mode 1: the sources (every root is its own parent)
     int nsrc;
     long long max_rounds;
@@ -216,6 +225,15 @@ __device__ __forceinline__ bool warp_append_chunks(unsigned val, unsigned cnt, u
     const unsigned first = base + incl - cnt;
     for (unsigned k = 0; k < cnt; k++) list[first + k] = make_uint2(val, k);
     return true;
+}
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long w = __shfl_xor_sync(0xFFFFFFFFu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
 }
 
 __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {

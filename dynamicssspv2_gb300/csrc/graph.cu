@@ -481,6 +481,16 @@ int ensure_work(dsssp_graph* g) {
     const long long nt = thread_item_capacity(g->cap_total, g->n, g->o);
     const long long nc = cta_item_capacity(g->cap_total, g->o);
     DevGraph& d = g->dg;
+    if (g->o.delta > 0 && !d.far_tag) {  // near-far lists: one entry per vertex at most
+        int rc = dalloc(&d.far0, (size_t)g->n, "far list");
+        if (!rc) rc = dalloc(&d.far1, (size_t)g->n, "far list");
+        if (!rc) rc = dalloc(&d.far_tag, (size_t)g->n, "far tags");
+        if (rc) {
+            dfree(d.far0); dfree(d.far1); dfree(d.far_tag);
+            return rc;
+        }
+        CK(cudaMemsetAsync(d.far_tag, 0, sizeof(unsigned) * (size_t)g->n, g->stream), "far tags");
+    }
     if (d.tcap >= nt && d.ccap >= nc && d.rt0) return DSSSP_OK;
     dfree(d.rt0); dfree(d.rt1); dfree(d.rc0); dfree(d.rc1); dfree(d.it); dfree(d.ic);
     d.tcap = d.ccap = 0;
@@ -697,6 +707,7 @@ UpdParams make_params(const dsssp_graph* g, const int4* chg, long long k, int mo
     p.chunk = g->o.chunk;
     p.bfs_levels = g->o.bfs_levels;
     p.mode = mode;
+    p.delta = g->o.delta > 0 ? (unsigned long long)g->o.delta : 0ull;
     p.srcs = g->d_srcs;
     p.nsrc = 0;
     p.max_rounds = g->o.max_rounds > 0 ? g->o.max_rounds : 2LL * g->n + 16;
@@ -722,6 +733,7 @@ int next_epoch(dsssp_graph* g, cudaStream_t s) {
 // tags and restart the tag sequence so no stale tag can suppress a later push.
 void reset_tags(dsssp_graph* g, cudaStream_t s) {
     cudaMemsetAsync(g->dg.push_tag, 0, sizeof(unsigned) * (size_t)g->n, s);
+    if (g->dg.far_tag) cudaMemsetAsync(g->dg.far_tag, 0, sizeof(unsigned) * (size_t)g->n, s);
     const unsigned one = 1;
     cudaMemcpyAsync(&g->dg.ctl->round_base, &one, sizeof(one), cudaMemcpyHostToDevice, s);
     cudaStreamSynchronize(s);
@@ -769,6 +781,7 @@ void fill_stats(const dsssp_graph* g, const Ctl& c, dsssp_stats* st, bool events
     }
     st->n_killed = (int64_t)c.killed;
     st->work_items = (int64_t)c.stat[ST_ITEMS];
+    st->advances = (int64_t)c.stat[ST_ADVANCES];
     // algorithmic bytes (byte model: each item is touched once by this algorithm)
     //   per adjacency entry scanned 16 (entry + neighbour state), per work item 40 (item write
     //   + read, row descriptor, owner state), per pushed vertex 20 (push tag, degree), per
@@ -932,6 +945,7 @@ void dsssp_default_opts(dsssp_opts* o) {
     o->timing = 1;
     o->max_rounds = 0;
     o->spare_pct = 12;
+    o->delta = 0;
 }
 
 const char* dsssp_strerror(int code) {
@@ -975,7 +989,7 @@ void dsssp_graph_destroy(dsssp_graph* g) {
     DevGraph& d = g->dg;
     dfree(d.state); dfree(d.rows); dfree(d.sorted_len); dfree(d.adj); dfree(d.inv_tag);
     dfree(d.push_tag); dfree(d.jm); dfree(d.invq); dfree(d.rt0); dfree(d.rt1); dfree(d.rc0); dfree(d.rc1);
-    dfree(d.it); dfree(d.ic); dfree(d.ctl);
+    dfree(d.it); dfree(d.ic); dfree(d.ctl); dfree(d.far0); dfree(d.far1); dfree(d.far_tag);
     dfree(g->d_chg); dfree(g->d_ins_state); dfree(g->d_ovf); dfree(g->d_hset); dfree(d.twin); dfree(g->s_twin);
     dfree(g->d_par); dfree(g->d_dist); dfree(g->d_srcs); dfree(g->d_slot); dfree(g->d_spare);
     dfree(g->d_need); dfree(g->d_gidx); dfree(g->d_grow_list); dfree(g->d_grow_count); dfree(g->d_old_start);
@@ -992,7 +1006,7 @@ static int check_opts(const dsssp_opts& o) {
     if (o.slack_pct < 0 || o.slack_min < 0 || o.small_deg < 4 || o.small_deg > 64 || o.small_deg % 4 ||
         o.large_deg < o.small_deg || o.chunk < 32 ||
         o.bfs_levels < 0 || o.block < 32 || o.block > 256 || o.block % 32 || o.ctas_per_sm < 0 || o.max_rounds < 0 ||
-        o.spare_pct < 0 || o.spare_pct > 400)
+        o.spare_pct < 0 || o.spare_pct > 400 || o.delta < 0)
         return fail(DSSSP_E_INVAL, "invalid dsssp_opts");
     return DSSSP_OK;
 }

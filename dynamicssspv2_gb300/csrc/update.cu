@@ -21,7 +21,13 @@
 //               C. frontier relaxation rounds with 64-bit atomicMin on the packed
 //                  (dist, parent) word until the frontier is empty (replaces
 //                  filterAllAffected + updateNeighbors and its host loop,
-//                  gpuFunctions_undir.cuh:162-174, 370-433, MAIN:263-281)
+//                  gpuFunctions_undir.cuh:162-174, 370-433, MAIN:263-281).  With a bucket
+//                  width delta > 0 the rounds are near-far ordered: a vertex whose new
+//                  distance is at or above the threshold T waits in a de-duplicated far list;
+//                  when the near frontier runs dry, T moves to (least far distance) + delta
+//                  and the far list is split again.  High-diameter graphs then settle most
+//                  vertices once instead of once per improving wave.  The result is the same
+//                  fixpoint: exact distances, the same parents.
 // Load balance: a vertex entering a frontier is split by degree into work items -- rows of
 // at most te edges are one thread's item, longer rows up to large_deg become ceil(deg/te)
 // thread items (a warp's worth for a few hundred edges), longer ones become CTA items of
@@ -168,6 +174,34 @@ __device__ __forceinline__ bool claim_with_deg(const UpdParams& p, bool want, un
     return won;
 }
 
+// Near-far ordering: pushes whose new distance is at or above the threshold T go to a far
+// list, each vertex at most once per list generation (far_tag).  T = ~0 turns it off.
+struct Far {
+    unsigned* list;
+    unsigned* cnt;
+    unsigned* tag;
+    unsigned gen;
+    unsigned cap;
+    unsigned long long T;
+};
+
+// Appends c to the far list for every lane with pred (warp-collective).
+__device__ __forceinline__ void far_push(const UpdParams& p, const Far& f, bool pred, unsigned c) {
+    if (pred) pred = atomicExch(&f.tag[c], f.gen) != f.gen;
+    const unsigned mask = __ballot_sync(kFull, pred);
+    if (mask == 0) return;
+    const unsigned lane = lane_id();
+    const unsigned leader = __ffs(mask) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(f.cnt, (unsigned)__popc(mask));
+    base = __shfl_sync(kFull, base, leader);
+    if ((unsigned long long)base + __popc(mask) > f.cap) {  // cannot happen: one entry per vertex
+        if (lane == leader) set_status(p.g.ctl, -4);
+        return;
+    }
+    if (pred) f.list[base + __popc(mask & ((1u << lane) - 1u))] = c;
+}
+
 // ---- per-edge operations ---------------------------------------------------------------
 // visit4 handles up to four adjacency entries per lane and is called by all 32 lanes.
 
@@ -177,6 +211,7 @@ struct RelaxOp {
     Out out;
     PushBuf pb;
     LocalStats* ls;
+    Far far;
 
     __device__ __forceinline__ unsigned long long prep(unsigned v) const { return __ldcg(&p->g.state[v]) >> 32; }
     __device__ __forceinline__ bool skip(unsigned long long du) const { return du >= kDistInf; }
@@ -198,9 +233,12 @@ struct RelaxOp {
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             bool push = false;
-            if (e[q].y >= 0) push = relax_to(state, (unsigned)e[q].x, du + (unsigned)e[q].y, u, e[q].y, cur[q], *ls);
+            const unsigned long long nd = du + (unsigned)e[q].y;
+            if (e[q].y >= 0) push = relax_to(state, (unsigned)e[q].x, nd, u, e[q].y, cur[q], *ls);
+            const bool later = push && nd >= far.T;
+            far_push(*p, far, later, (unsigned)e[q].x);
             int deg;
-            const bool doit = claim_with_deg(*p, push, (unsigned)e[q].x, tag, deg);
+            const bool doit = claim_with_deg(*p, push && !later, (unsigned)e[q].x, tag, deg);
             ls->frontier += doit ? 1 : 0;
             pb.add(doit, (unsigned)e[q].x, deg);
             ls->edges_relax += ok[q] ? 1 : 0;
@@ -252,8 +290,20 @@ struct PullOp {
     Out out;
     PushBuf pb;
     LocalStats* ls;
+    Far far;
     unsigned long long best;
     bool need;
+
+    // pushes x (pred) to the next round or, at or above the threshold, to the far list
+    __device__ __forceinline__ void route(bool pred, unsigned x) {
+        const bool later = pred && (__ldcg(&p->g.state[x]) >> 32) >= far.T;
+        far_push(*p, far, later, x);
+        int deg;
+        const bool doit = claim_with_deg(*p, pred && !later, x, tag, deg);
+        ls->frontier += doit ? 1 : 0;
+        pb.add(doit, x, deg);
+        pb.flush(*p, out, *ls, false);
+    }
 
     __device__ __forceinline__ unsigned long long prep(unsigned) const { return 0; }
     __device__ __forceinline__ bool skip(unsigned long long) const { return false; }
@@ -297,11 +347,7 @@ struct PullOp {
                 ls->updates++;
             }
         }
-        int deg;
-        const bool doit = claim_with_deg(*p, valid && (need || improved), x, tag, deg);
-        ls->frontier += doit ? 1 : 0;
-        pb.add(doit, x, deg);
-        pb.flush(*p, out, *ls, false);
+        route(valid && (need || improved), x);
     }
     // an item shared by the warp (part of a CTA item)
     __device__ __forceinline__ void end_group(unsigned x) {
@@ -315,11 +361,7 @@ struct PullOp {
                 ls->updates++;
             }
         }
-        int deg;
-        const bool doit = claim_with_deg(*p, lane_id() == 0 && (nd || improved), x, tag, deg);
-        ls->frontier += doit ? 1 : 0;
-        pb.add(doit, x, deg);
-        pb.flush(*p, out, *ls, false);
+        route(lane_id() == 0 && (nd || improved), x);
     }
 };
 
@@ -397,6 +439,17 @@ __device__ void flush_stats(Ctl* ctl, const LocalStats& ls) {
     __syncthreads();
     const int idx[7] = {ST_EDGES_RELAX, ST_EDGES_INV, ST_UPDATES, ST_DIST_OVF, ST_FRONTIER, ST_ITEMS, ST_INV};
     if (threadIdx.x < 7 && s_acc[threadIdx.x]) atomicAdd(&ctl->stat[idx[threadIdx.x]], s_acc[threadIdx.x]);
+}
+
+__device__ void block_max(unsigned long long* dst, unsigned long long x) {
+    __shared__ unsigned long long s_max;
+    __syncthreads();
+    if (threadIdx.x == 0) s_max = 0;
+    __syncthreads();
+    x = warp_max_u64(x);
+    if (lane_id() == 0 && x) atomicMax(&s_max, x);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_max) atomicMax(dst, s_max);
 }
 
 __device__ void block_add(unsigned long long* dst, unsigned long long x) {
@@ -625,13 +678,29 @@ __device__ void update_body(UpdParams& p) {
     if (leader) ctl->ts[0] = globaltimer();
 
     unsigned rbase = __ldcg(&ctl->round_base);
-    if (rbase > 0xF0000000u) {  // push tags would wrap: clear them
-        for (unsigned v = gtid; v < (unsigned)g.n; v += nthreads) g.push_tag[v] = 0;
+    if (rbase > 0xF0000000u) {  // push and far tags would wrap: clear them
+        for (unsigned v = gtid; v < (unsigned)g.n; v += nthreads) {
+            g.push_tag[v] = 0;
+            if (g.far_tag) g.far_tag[v] = 0;
+        }
         if (!grid_sync(ctl)) return;
         rbase = 1;
     }
     const unsigned tag0 = rbase + 1;
     const Out relax0{g.rt0, &ctl->rcT[0], g.tcap, g.rc0, &ctl->rcC[0], g.ccap};
+    // Near-far state (identical in every thread).  A batch update starts with T = 0, so every
+    // seed waits in the far list and the first advance picks the threshold; a computation
+    // from scratch starts with the sources (distance 0) near and T = delta.  Far generations
+    // of this call are rbase, rbase + 1, ... (at most one per round, so below the next
+    // call's round base).
+    const bool nf = p.delta != 0 && g.far0 != nullptr && g.far1 != nullptr && g.far_tag != nullptr;
+    unsigned long long T = nf ? (p.mode == 1 ? p.delta : 0ull) : ~0ull;
+    unsigned fgen = rbase;
+    int cf = 0;
+    unsigned adv = 0;
+    auto far_of = [&](int which, unsigned gen, unsigned long long thr) {
+        return Far{which ? g.far1 : g.far0, &ctl->fc[which], g.far_tag, gen, (unsigned)g.n, thr};
+    };
 
     if (p.mode == 1) {
         for (unsigned base = gtid - lane; base < (unsigned)p.nsrc; base += nthreads) {
@@ -742,23 +811,29 @@ __device__ void update_body(UpdParams& p) {
         // ---- B. seeds: surviving insertions relax both ends; cut-off vertices pull ---------
         {
             PushBuf pb{pbuf, 0};
+            const Far far = far_of(cf, fgen, T);
             for (long long base = (long long)(gtid - lane); base < p.k; base += nthreads) {
                 const long long i = base + lane;
                 const bool has = i < p.k;
                 const int4 c = has ? p.chg[i] : make_int4(0, 0, 0, -1);
                 const bool alive = has && c.w == 1 && p.ins_state[i] == 1;
                 bool pa = false, pbv = false;
+                unsigned long long nda = 0, ndb = 0;
                 if (alive) {
                     const unsigned a = (unsigned)c.x, b = (unsigned)c.y;
                     const unsigned long long sa = __ldcg(&g.state[a]), sb = __ldcg(&g.state[b]);
-                    if ((sa >> 32) != kDistInf) pbv = relax_to(g.state, b, (sa >> 32) + (unsigned)c.z, a, c.z, sb, ls);
-                    if ((sb >> 32) != kDistInf)
-                        pa = relax_to(g.state, a, (sb >> 32) + (unsigned)c.z, b, c.z, __ldcg(&g.state[a]), ls);
+                    ndb = (sa >> 32) + (unsigned)c.z;
+                    nda = (sb >> 32) + (unsigned)c.z;
+                    if ((sa >> 32) != kDistInf) pbv = relax_to(g.state, b, ndb, a, c.z, sb, ls);
+                    if ((sb >> 32) != kDistInf) pa = relax_to(g.state, a, nda, b, c.z, __ldcg(&g.state[a]), ls);
                     ls.edges_relax += 2;
                 }
+                const bool lb = pbv && ndb >= far.T, la = pa && nda >= far.T;
+                far_push(p, far, lb, (unsigned)c.y);
+                far_push(p, far, la, (unsigned)c.x);
                 int degb, dega;
-                const bool db = claim_with_deg(p, pbv, (unsigned)c.y, tag0, degb);
-                const bool da = claim_with_deg(p, pa, (unsigned)c.x, tag0, dega);
+                const bool db = claim_with_deg(p, pbv && !lb, (unsigned)c.y, tag0, degb);
+                const bool da = claim_with_deg(p, pa && !la, (unsigned)c.x, tag0, dega);
                 ls.frontier += (db ? 1 : 0) + (da ? 1 : 0);
                 pb.add(db, (unsigned)c.y, degb);
                 pb.add(da, (unsigned)c.x, dega);
@@ -767,7 +842,7 @@ __device__ void update_body(UpdParams& p) {
             pb.flush(p, relax0, ls, true);
         }
         {
-            PullOp op{&p, tag0, relax0, PushBuf{pbuf, 0}, &ls, kInfState, false};
+            PullOp op{&p, tag0, relax0, PushBuf{pbuf, 0}, &ls, far_of(cf, fgen, T), kInfState, false};
             run_items(op, p, g.it, hiT, g.ic, hiC);
         }
         if (!grid_sync(ctl)) return;
@@ -777,8 +852,53 @@ __device__ void update_body(UpdParams& p) {
     // ---- C. relaxation rounds ---------------------------------------------------------------
     long long r = 0;
     for (;; r++) {
-        const unsigned nT = __ldcg(&ctl->rcT[r % 3]), nC = __ldcg(&ctl->rcC[r % 3]);
-        if (nT == 0 && nC == 0) break;
+        unsigned nT = __ldcg(&ctl->rcT[r % 3]), nC = __ldcg(&ctl->rcC[r % 3]);
+        if (nT == 0 && nC == 0) {
+            if (!nf) break;
+            // near frontier empty: advance the threshold past the least waiting distance
+            const unsigned nfar = __ldcg(&ctl->fc[cf]);
+            if (nfar == 0) break;
+            const unsigned* fl = cf ? g.far1 : g.far0;
+            unsigned long long mn = ~0ull;
+            for (unsigned i = gtid; i < nfar; i += nthreads) {
+                const unsigned long long d = __ldcg(&g.state[__ldcg(&fl[i])]) >> 32;
+                if (d >= T && d < mn) mn = d;  // below T: settled by an earlier near phase
+            }
+            block_max(&ctl->fmin[adv & 1], ~mn);  // max of ~d = min of d; 0 = nothing waits
+            if (leader) {
+                ctl->fmin[(adv + 1) & 1] = 0;  // read by every CTA before the last barrier
+                ctl->fc[cf ^ 1] = 0;           // the previous advance's source list
+            }
+            if (!grid_sync(ctl)) break;
+            const unsigned long long fm = __ldcg(&ctl->fmin[adv & 1]);
+            if (fm == 0) break;
+            const unsigned long long tn = ~fm + p.delta;
+            const Far nxt = far_of(cf ^ 1, fgen + 1, tn);
+            const Out near{(r & 1) ? g.rt1 : g.rt0, &ctl->rcT[r % 3], g.tcap, (r & 1) ? g.rc1 : g.rc0,
+                           &ctl->rcC[r % 3], g.ccap};
+            const unsigned tagr = rbase + (unsigned)r + 1u;  // the tag of round r's list
+            PushBuf pb{pbuf, 0};
+            for (unsigned base = gtid - lane; base < nfar; base += nthreads) {
+                const unsigned i = base + lane;
+                const unsigned v = i < nfar ? __ldcg(&fl[i]) : 0u;
+                const unsigned long long d = i < nfar ? __ldcg(&g.state[v]) >> 32 : 0ull;
+                const bool live = i < nfar && d >= T;
+                far_push(p, nxt, live && d >= tn, v);
+                int deg;
+                const bool doit = claim_with_deg(p, live && d < tn, v, tagr, deg);
+                ls.frontier += doit ? 1 : 0;
+                pb.add(doit, v, deg);
+                pb.flush(p, near, ls, false);
+            }
+            pb.flush(p, near, ls, true);
+            T = tn;
+            fgen++;
+            cf ^= 1;
+            adv++;
+            if (!grid_sync(ctl)) break;
+            nT = __ldcg(&ctl->rcT[r % 3]);
+            nC = __ldcg(&ctl->rcC[r % 3]);
+        }
         if (r >= p.max_rounds) {
             if (leader) set_status(ctl, -5 /* NO_CONVERGENCE */);
             break;
@@ -791,13 +911,14 @@ __device__ void update_body(UpdParams& p) {
         RelaxOp op{&p, rbase + (unsigned)r + 2u,
                    Out{odd ? g.rt0 : g.rt1, &ctl->rcT[(r + 1) % 3], g.tcap, odd ? g.rc0 : g.rc1,
                        &ctl->rcC[(r + 1) % 3], g.ccap},
-                   PushBuf{pbuf, 0}, &ls};
+                   PushBuf{pbuf, 0}, &ls, far_of(cf, fgen, T)};
         run_items(op, p, odd ? g.rt1 : g.rt0, nT, odd ? g.rc1 : g.rc0, nC);
         if (!grid_sync(ctl)) break;
     }
     flush_stats(ctl, ls);
     if (leader) {
         ctl->stat[ST_ROUNDS] = (unsigned long long)r;
+        ctl->stat[ST_ADVANCES] = (unsigned long long)adv;
         ctl->round_base = rbase + (unsigned)r + 4u;
         ctl->ts[3] = globaltimer();
     }

@@ -68,7 +68,12 @@ typedef struct {
     int64_t max_rounds;   /* relaxation round cap; 0 = 2n + 16 */
     int32_t spare_pct;    /* extra adjacency slots, percent of the laid-out rows, into which a
                              row that runs out of slack moves (no full repack); 0..400 */
-    int32_t reserved0;
+    int32_t delta;        /* near-far bucket width of the relaxation rounds: 0 = plain frontier
+                             rounds; > 0 = a round relaxes only vertices whose distance is below
+                             a threshold T, the others wait until the near frontier is empty and
+                             T moves to (least waiting distance) + delta.  Same results; far
+                             fewer rounds and relaxations on high-diameter graphs.  Costs 12
+                             bytes per vertex, allocated when first enabled. */
 } dsssp_opts;
 
 /* Counters of one batch (or one tree computation), read back from the device. */
@@ -97,6 +102,7 @@ typedef struct {
     double t_total_ms;         /* the whole batch on the device (CUDA events) */
     double bytes_alg;          /* algorithmic bytes of the batch (byte model of the engine) */
     double bytes_alg_update;   /* the part moved by the persistent update kernel */
+    int64_t advances;          /* near-far threshold advances (0 when delta = 0) */
 } dsssp_stats;
 
 /* ---- engine ------------------------------------------------------------------------ */

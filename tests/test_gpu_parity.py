@@ -62,6 +62,9 @@ OPTION_SETS = [
     {"slack_pct": 0, "slack_min": 0, "spare_pct": 300},    # every insertion overflows -> rows grow in place
     {"slack_pct": 0, "slack_min": 0, "spare_pct": 0},      # ... and no spare region -> full repack
     {"block": 64, "ctas_per_sm": 1},
+    {"delta": 1},                                          # near-far rounds, narrowest buckets
+    {"delta": 25},
+    {"delta": 25, "bfs_levels": 0, "small_deg": 4, "large_deg": 4, "chunk": 32},
 ]
 
 
@@ -100,7 +103,7 @@ def test_zero_weights_multiedges_selfloops():
     ch = D.make_changes(np.concatenate([u[idx], ins_u]), np.concatenate([v[idx], ins_v]),
                         np.concatenate([w[idx], rng.integers(0, 3, 200)]), np.concatenate([np.zeros(300), np.ones(200)]))
     ch = ch[rng.permutation(len(ch))]
-    for opts in ({}, {"bfs_levels": 0}):
+    for opts in ({}, {"bfs_levels": 0}, {"delta": 1}, {"delta": 2, "bfs_levels": 0}):
         p, d, _ = run_engine(n, u, v, w, ch, parent, dist, **opts)
         check_against_oracle(n, u, v, w, ch, 0, p, d, f"zero weights {opts}")
 
@@ -147,8 +150,9 @@ def test_source_never_invalidated():
     assert d.tolist() == [0, 2, 4]
 
 
+@pytest.mark.parametrize("delta", [0, 30])
 @pytest.mark.parametrize("kind", ["rmat", "grid"])
-def test_tree_compute_from_scratch(kind):
+def test_tree_compute_from_scratch(kind, delta):
     if kind == "rmat":
         n = 1 << 13
         u, v, w = D.gen_rmat(13, 8 * n, seed=3)
@@ -157,20 +161,47 @@ def test_tree_compute_from_scratch(kind):
         n = 64 * 64
         u, v, w = D.gen_grid(64, 64, 0.05, 40, 1, 1000, seed=3)
         src = 0
-    with D.Graph(n, u, v, w) as g:
+    with D.Graph(n, u, v, w, delta=delta) as g:
         st = g.tree_compute(src)
         p, d = g.tree_read()
     check_against_oracle(n, u, v, w, None, src, p, d, kind)
     assert st.rounds > 0
+    assert (st.advances > 0) == (delta > 0)
 
 
-def test_sequence_of_batches():
+@pytest.mark.parametrize("delta", [1, 40, 1000])
+def test_near_far_same_tree_on_grid(delta):
+    """High-diameter grid with a cut near the source: near-far rounds give the same distances
+    and, with positive weights, the same parents as plain rounds, in fewer relaxations."""
+    n = 96 * 96
+    u, v, w = D.gen_grid(96, 96, 0.02, 40, 1, 1000, seed=5)
+    parent, dist = initial_tree(n, u, v, w)
+    # delete the tree edges of 40 vertices a little away from the source: about half of the
+    # grid is cut off and must be reached again around the cuts
+    order = np.argsort(dist)
+    near = order[200:240]
+    pu = np.asarray(parent)[near]
+    ch = D.make_changes(near, pu, np.asarray(dist)[near] - np.asarray(dist)[pu], np.zeros(len(near)))
+    ins = D.gen_changes(n, u, v, w, 300, 0, seed=6)
+    ch = np.concatenate([ch, ins])
+    p0, d0, st0 = run_engine(n, u, v, w, ch, parent, dist)
+    p1, d1, st1 = run_engine(n, u, v, w, ch, parent, dist, delta=delta)
+    check_against_oracle(n, u, v, w, ch, 0, p1, d1, f"near-far delta {delta}")
+    assert np.array_equal(d0, d1) and np.array_equal(p0, p1)
+    assert st1.advances > 0 and st0.advances == 0
+    assert st0.n_invalidated > n // 4 and (d1 >= 0).all()
+    if delta <= 40:
+        assert st1.edges_relaxed < st0.edges_relaxed
+
+
+@pytest.mark.parametrize("delta", [0, 16])
+def test_sequence_of_batches(delta):
     """Five batches in a row on one resident graph, each checked against a full recompute."""
     n, m = 4000, 16000
     u, v, w = D.gen_er(n, m, 1, 100, 11)
     parent, dist = initial_tree(n, u, v, w)
     cu, cv, cw = u.copy(), v.copy(), w.copy()
-    with D.Graph(n, u, v, w, slack_pct=5, slack_min=1) as g:
+    with D.Graph(n, u, v, w, slack_pct=5, slack_min=1, delta=delta) as g:
         g.tree_load(parent, dist)
         for b in range(5):
             ch = D.gen_changes(n, cu, cv, cw, 400, 600, seed=200 + b)
