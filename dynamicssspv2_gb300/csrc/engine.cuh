@@ -80,7 +80,8 @@ struct __align__(128) Ctl {
     int ovf_count;
     unsigned inv_count;  // roots appended by k_delete
     unsigned killed;     // insertions removed by a deletion of the same batch
-    unsigned pad1[28];
+    unsigned seed_count;  // vertices k_append seeded into the first frontier
+    unsigned pad1[27];
     // line 2
     unsigned bar_count;
     unsigned pad2[31];
@@ -153,6 +154,7 @@ struct UpdParams {
     int bfs_levels;
     int mode;         // 0 = batch update, 1 = from scratch (state already reset)
     unsigned long long delta;  // near-far bucket width; 0 = plain frontier relaxation
+    unsigned* seedq;  // vertices seeded by k_append (claimed, expanded by k_update)
     const int* srcs;  // mode 1: the sources (every root is its own parent)
     int nsrc;
     long long max_rounds;
@@ -226,6 +228,10 @@ __device__ __forceinline__ bool warp_append_chunks(unsigned val, unsigned cnt, u
     for (unsigned k = 0; k < cnt; k++) list[first + k] = make_uint2(val, k);
     return true;
 }
+
+// Adjacency entries are read once per push: streaming loads (evict-first in L1 and L2) keep
+// the randomly accessed per-vertex arrays (state, row descriptors, tags) resident in L2.
+__device__ __forceinline__ int2 ld_stream(const int2* a) { return __ldcs(a); }
 
 __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
 #pragma unroll

@@ -415,6 +415,7 @@ struct dsssp_graph {
     int* d_ins_state = nullptr;
     int4* d_ovf = nullptr;
     long long* d_slot = nullptr;        // per record: slots of both appended ends
+    unsigned* d_seedq = nullptr;        // vertices seeded by the insertions of a batch
     // in-place row growth
     unsigned long long* d_spare = nullptr;  // {top, end} of the spare region
     int* d_need = nullptr;
@@ -517,6 +518,7 @@ int ensure_batch(dsssp_graph* g, long long k) {
     dfree(g->d_ovf);
     dfree(g->d_hset);
     dfree(g->d_slot);
+    dfree(g->d_seedq);
     dfree(g->d_grow_list);
     dfree(g->d_old_start);
     dfree(g->d_old_cap);
@@ -530,6 +532,7 @@ int ensure_batch(dsssp_graph* g, long long k) {
     if (!rc) rc = dalloc(&g->d_slot, (size_t)cap * 2, "slot buffer");
     const long long gl = 2 * cap < g->n ? 2 * cap : g->n;
     if (!rc) rc = dalloc(&g->d_grow_list, (size_t)gl, "grow list");
+    if (!rc) rc = dalloc(&g->d_seedq, (size_t)gl, "seed list");
     if (!rc) rc = dalloc(&g->d_old_start, (size_t)gl, "grow list");
     if (!rc) rc = dalloc(&g->d_old_cap, (size_t)gl, "grow list");
     if (!rc) g->grow_cap = gl;
@@ -708,6 +711,7 @@ UpdParams make_params(const dsssp_graph* g, const int4* chg, long long k, int mo
     p.bfs_levels = g->o.bfs_levels;
     p.mode = mode;
     p.delta = g->o.delta > 0 ? (unsigned long long)g->o.delta : 0ull;
+    p.seedq = g->d_seedq;
     p.srcs = g->d_srcs;
     p.nsrc = 0;
     p.max_rounds = g->o.max_rounds > 0 ? g->o.max_rounds : 2LL * g->n + 16;
@@ -737,6 +741,7 @@ void reset_tags(dsssp_graph* g, cudaStream_t s) {
     const unsigned one = 1;
     cudaMemcpyAsync(&g->dg.ctl->round_base, &one, sizeof(one), cudaMemcpyHostToDevice, s);
     cudaStreamSynchronize(s);
+    g->h_ctl->round_base = 1;
 }
 
 int status_code(int st) {
@@ -863,6 +868,9 @@ int grow_rows(dsssp_graph* g, int novf, cudaStream_t s) {
 
 // Enqueues one batch (records already on the device).
 int enqueue_batch(dsssp_graph* g, const int4* d_chg, long long k, cudaStream_t s) {
+    // k_append already claims frontier tags: restart the tag sequence before it could wrap
+    // (the mirror holds the round base the last kernel left)
+    if (g->h_ctl->round_base > 0xF0000000u) reset_tags(g, g->stream);
     const bool ev = g->o.timing != 0;
     if (ev) CK(cudaEventRecord(g->ev[0], s), "event");
     int rc = clear_ctl(g, s);
@@ -991,7 +999,7 @@ void dsssp_graph_destroy(dsssp_graph* g) {
     dfree(d.push_tag); dfree(d.jm); dfree(d.invq); dfree(d.rt0); dfree(d.rt1); dfree(d.rc0); dfree(d.rc1);
     dfree(d.it); dfree(d.ic); dfree(d.ctl); dfree(d.far0); dfree(d.far1); dfree(d.far_tag);
     dfree(g->d_chg); dfree(g->d_ins_state); dfree(g->d_ovf); dfree(g->d_hset); dfree(d.twin); dfree(g->s_twin);
-    dfree(g->d_par); dfree(g->d_dist); dfree(g->d_srcs); dfree(g->d_slot); dfree(g->d_spare);
+    dfree(g->d_par); dfree(g->d_dist); dfree(g->d_srcs); dfree(g->d_slot); dfree(g->d_seedq); dfree(g->d_spare);
     dfree(g->d_need); dfree(g->d_gidx); dfree(g->d_grow_list); dfree(g->d_grow_count); dfree(g->d_old_start);
     dfree(g->d_old_cap); dfree(g->d_fail);
     dfree(g->s_state); dfree(g->s_rows); dfree(g->s_sorted); dfree(g->s_adj);

@@ -10,14 +10,16 @@
 //               degree bump, both directions).  The reference appends every insertion and
 //               then tombstones matches (all_structure_undir.cuh:106-117 before
 //               gpuFunctions_undir.cuh:201-213); skipping the removed ones gives the same graph.
+//               Each surviving insertion then relaxes both ends and seeds the first frontier
+//               (replaces insertEdge, gpuFunctions_undir.cuh:217-251)
 //   k_update    one persistent cooperative kernel with a bounded grid barrier:
 //               A. cut-off subtrees are walked level by level from the roots (replaces
 //                  filterAffectedNodes + updateNeighbors_del and its host loop,
 //                  gpuFunctions_undir.cuh:125-144, 312-349, MAIN:219-239); after bfs_levels
-//                  levels it switches to pointer jumping over the parent array
-//               B. surviving insertions relax their endpoints (replaces insertEdge,
-//                  gpuFunctions_undir.cuh:217-251) and every cut-off vertex pulls its best
-//                  live neighbour
+//                  levels it switches to pointer jumping over the parent array.  The walk
+//                  follows the parent words as k_append left them, so an end relaxed from a
+//                  vertex that turns out to be cut off is cut off with it.
+//               B. every cut-off vertex pulls its best live neighbour
 //               C. frontier relaxation rounds with 64-bit atomicMin on the packed
 //                  (dist, parent) word until the frontier is empty (replaces
 //                  filterAllAffected + updateNeighbors and its host loop,
@@ -43,7 +45,9 @@ namespace {
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr unsigned kSpinLimit = 1u << 24;  // x ~200 ns sleeps: a barrier gives up after ~3 s
 constexpr int kMaxWarps = 8;               // update kernel blocks have at most 256 threads
-constexpr int kBuf = 160;                  // per-warp push buffer, flushed at >= 32 entries
+constexpr int kBuf = 256;                  // per-warp push buffer (vertex, degree) entries
+constexpr int kAddsPerCheck = 128;         // entries a warp may add between two flush checks
+                                           // (visit4: 4 adds of up to 32 lanes)
 
 __shared__ unsigned s_nbar;  // grid barriers this CTA has passed
 __shared__ uint2 s_pbuf[kMaxWarps][kBuf];  // (vertex, degree) pushed, not yet expanded
@@ -140,7 +144,46 @@ __device__ __forceinline__ void expand(unsigned v, int deg, const UpdParams& p, 
     ls.items += nt + nc;
 }
 
-// Per-warp shared-memory buffer of pushed (vertex, degree); expanded into items 32 at a time.
+// Work items of the entries a lane holds in a push buffer (entries lane, lane + 32, ...).
+__device__ __forceinline__ void buf_counts(const uint2* buf, int count, const UpdParams& p, unsigned& nt,
+                                           unsigned& nc) {
+    nt = nc = 0;
+    for (int e = (int)lane_id(); e < count; e += 32) {
+        const int deg = (int)buf[e].y;
+        if (deg > p.large_deg) nc += (unsigned)((deg + p.chunk - 1) / p.chunk);
+        else if (deg > 0) nt += (unsigned)((deg + p.te - 1) / p.te);
+    }
+}
+
+// Writes those items from list positions ft (thread items) and fc (CTA items) on.
+__device__ __forceinline__ void buf_write(const uint2* buf, int count, const UpdParams& p, const Out& o, unsigned ft,
+                                          unsigned fc) {
+    for (int e = (int)lane_id(); e < count; e += 32) {
+        const uint2 x = buf[e];
+        const int deg = (int)x.y;
+        if (deg > p.large_deg) {
+            const unsigned n = (unsigned)((deg + p.chunk - 1) / p.chunk);
+            for (unsigned k = 0; k < n; k++) o.cl[fc++] = make_uint2(x.x, k);
+        } else if (deg > 0) {
+            const unsigned n = (unsigned)((deg + p.te - 1) / p.te);
+            for (unsigned k = 0; k < n; k++) o.tl[ft++] = make_uint2(x.x, k);
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned warp_incl_scan(unsigned x) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned t = __shfl_up_sync(kFull, x, o);
+        if (lane_id() >= (unsigned)o) x += t;
+    }
+    return x;
+}
+
+// Per-warp shared-memory buffer of pushed (vertex, degree).  Entries are split into work
+// items when the buffer is nearly full (one list-counter atomic per warp for up to kBuf
+// vertices) and at the end of a phase (one atomic per CTA): the list counters are single
+// words that every CTA appends to, so their atomics are kept few.
 struct PushBuf {
     uint2* buf;
     int count;  // warp-uniform
@@ -152,15 +195,61 @@ struct PushBuf {
         __syncwarp();
     }
 
-    __device__ __forceinline__ void flush(const UpdParams& p, const Out& o, LocalStats& ls, bool all) {
-        while (count >= 32 || (all && count > 0)) {
-            const int take = count < 32 ? count : 32;
-            const bool has = (int)lane_id() < take;
-            const uint2 e = has ? buf[count - take + (int)lane_id()] : make_uint2(0u, 0u);
-            __syncwarp();
-            count -= take;
-            expand(e.x, (int)e.y, p, o, ls);
+    // warp-collective: expands the buffer once it could not take another kAddsPerCheck
+    __device__ __forceinline__ void flush(const UpdParams& p, const Out& o, LocalStats& ls) {
+        if (count <= kBuf - kAddsPerCheck) return;
+        unsigned nt, nc;
+        buf_counts(buf, count, p, nt, nc);
+        const unsigned it = warp_incl_scan(nt), ic = warp_incl_scan(nc);
+        const unsigned tt = __shfl_sync(kFull, it, 31), tc = __shfl_sync(kFull, ic, 31);
+        unsigned bt = 0, bc = 0;
+        if (lane_id() == 0) {
+            if (tt) bt = atomicAdd(o.tcnt, tt);
+            if (tc) bc = atomicAdd(o.ccnt, tc);
         }
+        bt = __shfl_sync(kFull, bt, 0);
+        bc = __shfl_sync(kFull, bc, 0);
+        if ((long long)bt + tt > o.tcap || (long long)bc + tc > o.ccap) {
+            if (lane_id() == 0) set_status(p.g.ctl, -4 /* work list capacity: internal error */);
+        } else {
+            buf_write(buf, count, p, o, bt + it - nt, bc + ic - nc);
+        }
+        ls.items += nt + nc;
+        count = 0;
+        __syncwarp();
+    }
+
+    // CTA-collective (every thread of the CTA): expands what every warp still holds
+    __device__ void flush_cta(const UpdParams& p, const Out& o, LocalStats& ls) {
+        __shared__ unsigned s_t[kMaxWarps], s_c[kMaxWarps], s_bt, s_bc, s_ok;
+        const unsigned w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        unsigned nt, nc;
+        buf_counts(buf, count, p, nt, nc);
+        const unsigned it = warp_incl_scan(nt), ic = warp_incl_scan(nc);
+        if (lane_id() == 31) {
+            s_t[w] = it;
+            s_c[w] = ic;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned tt = 0, tc = 0;
+            for (unsigned k = 0; k < nw; k++) {
+                const unsigned a = s_t[k], b = s_c[k];
+                s_t[k] = tt;
+                s_c[k] = tc;
+                tt += a;
+                tc += b;
+            }
+            s_bt = tt ? atomicAdd(o.tcnt, tt) : 0u;
+            s_bc = tc ? atomicAdd(o.ccnt, tc) : 0u;
+            s_ok = (long long)s_bt + tt <= o.tcap && (long long)s_bc + tc <= o.ccap;
+            if (!s_ok) set_status(p.g.ctl, -4 /* work list capacity: internal error */);
+        }
+        __syncthreads();
+        if (s_ok) buf_write(buf, count, p, o, s_bt + s_t[w] + it - nt, s_bc + s_c[w] + ic - nc);
+        ls.items += nt + nc;
+        count = 0;
+        __syncthreads();
     }
 };
 
@@ -219,14 +308,14 @@ struct RelaxOp {
     __device__ __forceinline__ void end_lane(unsigned, bool) {}
     __device__ __forceinline__ void begin_group(unsigned) {}
     __device__ __forceinline__ void end_group(unsigned) {}
-    __device__ __forceinline__ void finish() { pb.flush(*p, out, *ls, true); }
+    __device__ __forceinline__ void finish() { pb.flush_cta(*p, out, *ls); }
 
     __device__ __forceinline__ void visit4(unsigned u, unsigned long long du, const long long (&j)[4],
                                            const bool (&ok)[4]) {
         unsigned long long* state = p->g.state;
         int2 e[4];
 #pragma unroll
-        for (int q = 0; q < 4; q++) e[q] = ok[q] ? __ldg(&p->g.adj[j[q]]) : make_int2(0, -1);
+        for (int q = 0; q < 4; q++) e[q] = ok[q] ? ld_stream(&p->g.adj[j[q]]) : make_int2(0, -1);
         unsigned long long cur[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) cur[q] = e[q].y >= 0 ? __ldcg(&state[e[q].x]) : 0ull;
@@ -243,7 +332,7 @@ struct RelaxOp {
             pb.add(doit, (unsigned)e[q].x, deg);
             ls->edges_relax += ok[q] ? 1 : 0;
         }
-        pb.flush(*p, out, *ls, false);
+        pb.flush(*p, out, *ls);
     }
 };
 
@@ -259,28 +348,30 @@ struct MarkOp {
     __device__ __forceinline__ void end_lane(unsigned, bool) {}
     __device__ __forceinline__ void begin_group(unsigned) {}
     __device__ __forceinline__ void end_group(unsigned) {}
-    __device__ __forceinline__ void finish() { pb.flush(*p, out, *ls, true); }
+    __device__ __forceinline__ void finish() { pb.flush_cta(*p, out, *ls); }
 
     __device__ __forceinline__ void visit4(unsigned x, unsigned long long, const long long (&j)[4],
                                            const bool (&ok)[4]) {
         unsigned long long* state = p->g.state;
         int2 e[4];
 #pragma unroll
-        for (int q = 0; q < 4; q++) e[q] = ok[q] ? __ldg(&p->g.adj[j[q]]) : make_int2(0, -1);
+        for (int q = 0; q < 4; q++) e[q] = ok[q] ? ld_stream(&p->g.adj[j[q]]) : make_int2(0, -1);
         unsigned long long s[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) s[q] = e[q].y >= 0 ? __ldcg(&state[e[q].x]) : kInfState;
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const unsigned c = (unsigned)e[q].x;
-            bool mark = e[q].y >= 0 && (unsigned)s[q] == x;
-            if (mark) mark = atomicExch(&p->g.inv_tag[c], p->epoch) != p->epoch;
-            if (mark) state[c] = kInfState;
+            // a child is cut off even when already tagged: a root that an insertion of this
+            // batch re-parented onto a vertex of a cut-off subtree must lose that distance
+            const bool child = e[q].y >= 0 && (unsigned)s[q] == x;
+            if (child) state[c] = kInfState;
+            const bool mark = child && atomicExch(&p->g.inv_tag[c], p->epoch) != p->epoch;
             ls->marked += mark ? 1 : 0;
             pb.add(mark, c, mark ? p->g.rows[c].deg : 0);
             ls->edges_inv += ok[q] ? 1 : 0;
         }
-        pb.flush(*p, out, *ls, false);
+        pb.flush(*p, out, *ls);
     }
 };
 
@@ -302,21 +393,21 @@ struct PullOp {
         const bool doit = claim_with_deg(*p, pred && !later, x, tag, deg);
         ls->frontier += doit ? 1 : 0;
         pb.add(doit, x, deg);
-        pb.flush(*p, out, *ls, false);
+        pb.flush(*p, out, *ls);
     }
 
     __device__ __forceinline__ unsigned long long prep(unsigned) const { return 0; }
     __device__ __forceinline__ bool skip(unsigned long long) const { return false; }
     __device__ __forceinline__ void begin_lane(unsigned) { best = kInfState; need = false; }
     __device__ __forceinline__ void begin_group(unsigned) { best = kInfState; need = false; }
-    __device__ __forceinline__ void finish() { pb.flush(*p, out, *ls, true); }
+    __device__ __forceinline__ void finish() { pb.flush_cta(*p, out, *ls); }
 
     __device__ __forceinline__ void visit4(unsigned x, unsigned long long, const long long (&j)[4],
                                            const bool (&ok)[4]) {
         unsigned long long* state = p->g.state;
         int2 e[4];
 #pragma unroll
-        for (int q = 0; q < 4; q++) e[q] = ok[q] ? __ldg(&p->g.adj[j[q]]) : make_int2(0, -1);
+        for (int q = 0; q < 4; q++) e[q] = ok[q] ? ld_stream(&p->g.adj[j[q]]) : make_int2(0, -1);
         unsigned long long s[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) s[q] = e[q].y >= 0 ? __ldcg(&state[e[q].x]) : kInfState;
@@ -463,6 +554,38 @@ __device__ void block_add(unsigned long long* dst, unsigned long long x) {
     if (threadIdx.x == 0 && s_sum) atomicAdd(dst, s_sum);
 }
 
+// CTA-level staging of appends to a plain u32 list: entries gather in shared memory and go
+// out with one atomic on the list counter per CTA flush.  stage_flush is CTA-collective; it
+// writes when `all` is set or when fewer than `room` free entries are left.
+struct Stage {
+    unsigned* buf;  // shared memory, cap entries
+    unsigned cap;
+    unsigned* n;    // shared counter
+
+    __device__ __forceinline__ void add(bool pred, unsigned v) const {
+        if (pred) buf[atomicAdd(n, 1u)] = v;
+    }
+};
+
+__device__ void stage_flush(const Stage& st, unsigned* list, unsigned* counter, unsigned list_cap, bool all,
+                            unsigned room, Ctl* ctl) {
+    __shared__ unsigned s_base;
+    __syncthreads();
+    const unsigned cnt = *st.n;
+    if (cnt == 0 || (!all && cnt + room <= st.cap)) return;  // same for every thread
+    if (threadIdx.x == 0) s_base = atomicAdd(counter, cnt);
+    __syncthreads();
+    const unsigned b = s_base;
+    if ((unsigned long long)b + cnt > list_cap) {
+        if (threadIdx.x == 0) set_status(ctl, -4 /* list capacity: internal error */);
+    } else {
+        for (unsigned j = threadIdx.x; j < cnt; j += blockDim.x) list[b + j] = st.buf[j];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *st.n = 0;
+    __syncthreads();
+}
+
 // ---- row search and the deletion set -------------------------------------------------------
 
 // First index in adj[lo, hi) whose column is >= c (the prefix is sorted by column).
@@ -562,11 +685,15 @@ __global__ void k_prepare(UpdParams p) {
 __global__ void k_delete(UpdParams p) {
     Ctl* ctl = p.g.ctl;
     if (__ldcg(&ctl->status) != 0) return;  // set by k_prepare: same for every thread
-    const unsigned lane = lane_id();
     const long long nthreads = (long long)gridDim.x * blockDim.x;
     unsigned long long probed = 0, roots = 0;
-    for (long long base = (long long)blockIdx.x * blockDim.x + threadIdx.x - lane; base < p.k; base += nthreads) {
-        const long long i = base + lane;
+    __shared__ unsigned s_nroots;
+    if (threadIdx.x == 0) s_nroots = 0;
+    __syncthreads();
+    const Stage roots_stage{reinterpret_cast<unsigned*>(&s_pbuf[0][0]), 2u * kMaxWarps * kBuf, &s_nroots};
+    // the loop is uniform over the CTA (the root staging flushes are CTA-collective)
+    for (long long cbase = (long long)blockIdx.x * blockDim.x; cbase < p.k; cbase += nthreads) {
+        const long long i = cbase + threadIdx.x;
         const int4 c = i < p.k ? p.chg[i] : make_int4(0, 0, 0, -1);
         bool cut = false;
         unsigned cutv = 0;
@@ -576,8 +703,9 @@ __global__ void k_delete(UpdParams p) {
             // A self-loop never cuts: its only parent relation is a root's (parent == itself),
             // and roots are never cut off.
             if (a != b) {
-                if ((unsigned)__ldcg(&p.g.state[b]) == a) cutv = b, cut = true;
-                else if ((unsigned)__ldcg(&p.g.state[a]) == b) cutv = a, cut = true;
+                const unsigned pb = (unsigned)__ldcg(&p.g.state[b]), pa = (unsigned)__ldcg(&p.g.state[a]);
+                if (pb == a) cutv = b, cut = true;
+                else if (pa == b) cutv = a, cut = true;
             }
             if (cut) {
                 cut = atomicExch(&p.g.inv_tag[cutv], p.epoch) != p.epoch;
@@ -595,25 +723,55 @@ __global__ void k_delete(UpdParams p) {
             }
             if (c.z >= 0 && !hash_insert(p, dpair_key(a, b), c.z)) set_status(ctl, -4 /* deletion set full */);
         }
-        warp_append(cut, cutv, p.g.invq, &ctl->inv_count);
+        roots_stage.add(cut, cutv);
         roots += cut ? 1 : 0;
+        stage_flush(roots_stage, p.g.invq, &ctl->inv_count, (unsigned)p.g.n, false, blockDim.x, ctl);
     }
+    stage_flush(roots_stage, p.g.invq, &ctl->inv_count, (unsigned)p.g.n, true, 0, ctl);
     block_add(&ctl->stat[ST_ROOTS], roots);
     block_add(&ctl->stat[ST_DEL_PROBED], probed);
 }
 
 // Insertions that no deletion of the batch removes go into row slack, both directions.  An
 // entry that does not fit is written to the overflow list and the batch is deferred to a
-// host-side repack (status 1).
+// host-side row growth (status 1).  Every surviving insertion then relaxes both of its ends
+// (replaces insertEdge, gpuFunctions_undir.cuh:217-251); an improved end is claimed for the
+// first frontier and listed in seedq (k_update splits it into work items once every row has
+// its final degree) or, in near-far mode, put in the far list.  Doing this before the
+// subtree walk is exact: k_delete has already cut off the roots (their distance is
+// infinite, so nothing relaxes from them), an end relaxed from a vertex that the walk later
+// cuts off takes that vertex as its parent and is cut off with it, and every other relaxed
+// distance is the length of a live path.
 __global__ void k_append(UpdParams p) {
     Ctl* ctl = p.g.ctl;
     if (__ldcg(&ctl->status) < 0) return;  // same for every thread
+    DevGraph& g = p.g;
+    const unsigned lane = lane_id();
+    const long long nthreads = (long long)gridDim.x * blockDim.x;
+    const unsigned rbase = __ldcg(&ctl->round_base);
+    const unsigned tag0 = rbase + 1;
+    // near-far: a batch starts with threshold 0, so every seed waits in the far list
+    const bool nf = p.delta != 0 && g.far0 != nullptr && g.far1 != nullptr && g.far_tag != nullptr;
+    const unsigned long long T = nf ? 0ull : ~0ull;
+    // seeds are staged per CTA (half of the push-buffer storage each for near and far)
+    __shared__ unsigned s_nn, s_nf;
+    if (threadIdx.x == 0) s_nn = s_nf = 0;
+    __syncthreads();
+    unsigned* stage_mem = reinterpret_cast<unsigned*>(&s_pbuf[0][0]);
+    const Stage near_stage{stage_mem, kMaxWarps * kBuf, &s_nn};
+    const Stage far_stage{stage_mem + kMaxWarps * kBuf, kMaxWarps * kBuf, &s_nf};
+    const unsigned seed_cap = (unsigned)min(2 * p.k, (long long)g.n);  // distinct claimed ends
+    LocalStats ls;
     unsigned long long killed = 0, ovf = 0;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.k;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int4 c = p.chg[i];
+    // the loop is uniform over the CTA (the staging flushes are CTA-collective)
+    for (long long cbase = (long long)blockIdx.x * blockDim.x; cbase < p.k; cbase += nthreads) {
+        const long long i = cbase + threadIdx.x;
+        const int4 c = i < p.k ? p.chg[i] : make_int4(0, 0, 0, -1);
         int alive = 0;
+        unsigned long long sa = kInfState, sb = kInfState;
         if (c.w == 1) {
+            sa = __ldcg(&g.state[c.x]);  // issued alongside the deletion-set probe
+            sb = __ldcg(&g.state[c.y]);
             if (hash_contains(p, dpair_key((unsigned)c.x, (unsigned)c.y), c.z)) {
                 killed++;
             } else {
@@ -622,11 +780,11 @@ __global__ void k_append(UpdParams p) {
 #pragma unroll
                 for (int side = 0; side < 2; side++) {
                     const int r = side ? c.y : c.x, col = side ? c.x : c.y;
-                    RowDesc* rd = &p.g.rows[r];
+                    RowDesc* rd = &g.rows[r];
                     const int pos = atomicAdd(&rd->deg, 1);
                     if (pos < rd->cap) {
                         at[side] = rd->start + pos;
-                        p.g.adj[at[side]] = make_int2(col, c.z);
+                        g.adj[at[side]] = make_int2(col, c.z);
                     } else {
                         at[side] = -1;
                         const int o = atomicAdd(&ctl->ovf_count, 1);
@@ -636,14 +794,38 @@ __global__ void k_append(UpdParams p) {
                     }
                     p.slot[2 * i + side] = at[side];
                 }
-                if (p.g.twin) {  // an overflowed end is placed (and paired) by the row growth
-                    if (at[0] >= 0) p.g.twin[at[0]] = at[1] >= 0 ? (unsigned)at[1] : kNoTwin;
-                    if (at[1] >= 0) p.g.twin[at[1]] = at[0] >= 0 ? (unsigned)at[0] : kNoTwin;
+                if (g.twin) {  // an overflowed end is placed (and paired) by the row growth
+                    if (at[0] >= 0) g.twin[at[0]] = at[1] >= 0 ? (unsigned)at[1] : kNoTwin;
+                    if (at[1] >= 0) g.twin[at[1]] = at[0] >= 0 ? (unsigned)at[0] : kNoTwin;
                 }
             }
         }
-        p.ins_state[i] = alive;
+        if (i < p.k) p.ins_state[i] = alive;
+        // seed: relax both ends through the new edge
+        bool pa = false, pbv = false;
+        const unsigned long long ndb = (sa >> 32) + (unsigned)c.z, nda = (sb >> 32) + (unsigned)c.z;
+        if (alive) {
+            if ((sa >> 32) != kDistInf) pbv = relax_to(g.state, (unsigned)c.y, ndb, (unsigned)c.x, c.z, sb, ls);
+            if ((sb >> 32) != kDistInf)
+                pa = relax_to(g.state, (unsigned)c.x, nda, (unsigned)c.y, c.z, __ldcg(&g.state[c.x]), ls);
+            ls.edges_relax += 2;
+        }
+        const bool lb = pbv && ndb >= T, la = pa && nda >= T;
+        const bool fb = lb && atomicExch(&g.far_tag[c.y], rbase) != rbase;
+        const bool fa = la && atomicExch(&g.far_tag[c.x], rbase) != rbase;
+        const bool db = pbv && !lb && atomicExch(&g.push_tag[c.y], tag0) != tag0;
+        const bool da = pa && !la && atomicExch(&g.push_tag[c.x], tag0) != tag0;
+        ls.frontier += (db ? 1 : 0) + (da ? 1 : 0);
+        near_stage.add(db, (unsigned)c.y);  // claimed: one entry per vertex
+        near_stage.add(da, (unsigned)c.x);
+        far_stage.add(fb, (unsigned)c.y);  // far-tagged: one entry per vertex
+        far_stage.add(fa, (unsigned)c.x);
+        stage_flush(near_stage, p.seedq, &ctl->seed_count, seed_cap, false, 2 * blockDim.x, ctl);
+        stage_flush(far_stage, g.far0, &ctl->fc[0], (unsigned)g.n, false, 2 * blockDim.x, ctl);
     }
+    stage_flush(near_stage, p.seedq, &ctl->seed_count, seed_cap, true, 0, ctl);
+    stage_flush(far_stage, g.far0, &ctl->fc[0], (unsigned)g.n, true, 0, ctl);
+    flush_stats(ctl, ls);
     block_add(&ctl->stat[ST_OVF], ovf);
     unsigned long long kk = warp_sum_u64(killed);
     if (lane_id() == 0 && kk) atomicAdd(&ctl->killed, (unsigned)kk);
@@ -719,11 +901,14 @@ __device__ void update_body(UpdParams& p) {
         const unsigned nroots = __ldcg(&ctl->inv_count);  // written by k_delete
         {
             const Out lvl0{g.it, &ctl->ltT[0], g.tcap, g.ic, &ctl->ltC[0], g.ccap};
+            PushBuf pb{pbuf, 0};
             for (unsigned base = gtid - lane; base < nroots; base += nthreads) {
                 const unsigned i = base + lane;
                 const unsigned v = i < nroots ? __ldcg(&g.invq[i]) : 0u;
-                expand(v, i < nroots ? g.rows[v].deg : 0, p, lvl0, ls);
+                pb.add(i < nroots, v, i < nroots ? g.rows[v].deg : 0);
+                pb.flush(p, lvl0, ls);
             }
+            pb.flush_cta(p, lvl0, ls);
         }
         if (leader) ls.marked += nroots;
         if (!grid_sync(ctl)) return;
@@ -791,55 +976,41 @@ __device__ void update_body(UpdParams& p) {
             }
             if (leader) ctl->stat[ST_PJ] = (unsigned long long)(pass + 1);
             const Out pjo{g.it + hiT, &ctl->pjT, g.tcap - hiT, g.ic + hiC, &ctl->pjC, g.ccap - hiC};
+            PushBuf pb{pbuf, 0};
             for (unsigned base = gtid - lane; base < (unsigned)g.n; base += nthreads) {
                 const unsigned v = base + lane;
                 bool newinv = false;
-                if (v < (unsigned)g.n && __ldcg(&g.jm[v]) == kTagInv && __ldcg(&g.inv_tag[v]) != p.epoch) {
+                const bool inv = v < (unsigned)g.n && __ldcg(&g.jm[v]) == kTagInv;
+                if (inv && __ldcg(&g.inv_tag[v]) != p.epoch) {
                     g.inv_tag[v] = p.epoch;
-                    g.state[v] = kInfState;
                     newinv = true;
                 }
+                // also the roots: one that an insertion re-parented may hold a distance
+                // through a cut-off vertex (the pull gives it its best live value again)
+                if (inv) g.state[v] = kInfState;
                 ls.marked += newinv ? 1 : 0;
-                expand(v, newinv ? g.rows[v].deg : 0, p, pjo, ls);
+                pb.add(newinv, v, newinv ? g.rows[v].deg : 0);
+                pb.flush(p, pjo, ls);
             }
+            pb.flush_cta(p, pjo, ls);
             if (!grid_sync(ctl)) return;
             hiT += __ldcg(&ctl->pjT);
             hiC += __ldcg(&ctl->pjC);
         }
         if (leader) ctl->ts[1] = globaltimer();
 
-        // ---- B. seeds: surviving insertions relax both ends; cut-off vertices pull ---------
+        // ---- B. the seeds of k_append become work items; cut-off vertices pull their best
+        // live neighbour --------------------------------------------------------------------
         {
+            const unsigned ns = __ldcg(&ctl->seed_count);
             PushBuf pb{pbuf, 0};
-            const Far far = far_of(cf, fgen, T);
-            for (long long base = (long long)(gtid - lane); base < p.k; base += nthreads) {
-                const long long i = base + lane;
-                const bool has = i < p.k;
-                const int4 c = has ? p.chg[i] : make_int4(0, 0, 0, -1);
-                const bool alive = has && c.w == 1 && p.ins_state[i] == 1;
-                bool pa = false, pbv = false;
-                unsigned long long nda = 0, ndb = 0;
-                if (alive) {
-                    const unsigned a = (unsigned)c.x, b = (unsigned)c.y;
-                    const unsigned long long sa = __ldcg(&g.state[a]), sb = __ldcg(&g.state[b]);
-                    ndb = (sa >> 32) + (unsigned)c.z;
-                    nda = (sb >> 32) + (unsigned)c.z;
-                    if ((sa >> 32) != kDistInf) pbv = relax_to(g.state, b, ndb, a, c.z, sb, ls);
-                    if ((sb >> 32) != kDistInf) pa = relax_to(g.state, a, nda, b, c.z, __ldcg(&g.state[a]), ls);
-                    ls.edges_relax += 2;
-                }
-                const bool lb = pbv && ndb >= far.T, la = pa && nda >= far.T;
-                far_push(p, far, lb, (unsigned)c.y);
-                far_push(p, far, la, (unsigned)c.x);
-                int degb, dega;
-                const bool db = claim_with_deg(p, pbv && !lb, (unsigned)c.y, tag0, degb);
-                const bool da = claim_with_deg(p, pa && !la, (unsigned)c.x, tag0, dega);
-                ls.frontier += (db ? 1 : 0) + (da ? 1 : 0);
-                pb.add(db, (unsigned)c.y, degb);
-                pb.add(da, (unsigned)c.x, dega);
-                pb.flush(p, relax0, ls, false);
+            for (unsigned base = gtid - lane; base < ns; base += nthreads) {
+                const unsigned i = base + lane;
+                const unsigned v = i < ns ? __ldcg(&p.seedq[i]) : 0u;
+                pb.add(i < ns, v, i < ns ? g.rows[v].deg : 0);
+                pb.flush(p, relax0, ls);
             }
-            pb.flush(p, relax0, ls, true);
+            pb.flush_cta(p, relax0, ls);
         }
         {
             PullOp op{&p, tag0, relax0, PushBuf{pbuf, 0}, &ls, far_of(cf, fgen, T), kInfState, false};
@@ -888,9 +1059,9 @@ __device__ void update_body(UpdParams& p) {
                 const bool doit = claim_with_deg(p, live && d < tn, v, tagr, deg);
                 ls.frontier += doit ? 1 : 0;
                 pb.add(doit, v, deg);
-                pb.flush(p, near, ls, false);
+                pb.flush(p, near, ls);
             }
-            pb.flush(p, near, ls, true);
+            pb.flush_cta(p, near, ls);
             T = tn;
             fgen++;
             cf ^= 1;

@@ -368,3 +368,24 @@ def test_parent_cycle_is_reported():
         with pytest.raises(D.DsssspError) as e:
             g.apply_batch(D.make_changes([0], [1], [1], [0]))
         assert e.value.code == D.E_BAD_TREE
+
+
+@pytest.mark.parametrize("opts", [{}, {"bfs_levels": 0}, {"bfs_levels": 1}, {"delta": 2}])
+def test_insertion_into_cut_off_root(opts):
+    """Insertions are relaxed before the subtree walk.  A cut-off root re-parented by an
+    insertion onto a vertex of its own subtree (0-1-2-3-4-5, delete 1-2, insert 2-5) must end
+    unreachable; a vertex re-parented onto a cut-off subtree (insert 3-9 below) must be cut off
+    with it and recomputed."""
+    # path 0-1-2-3-4-5 (w 1) and path 0-6-7-8-9 (w 10)
+    u = np.array([0, 1, 2, 3, 4, 0, 6, 7, 8], np.int32)
+    v = np.array([1, 2, 3, 4, 5, 6, 7, 8, 9], np.int32)
+    w = np.array([1, 1, 1, 1, 1, 10, 10, 10, 10], np.int32)
+    parent, dist = initial_tree(10, u, v, w)
+    ch = D.make_changes([1, 2], [2, 5], [1, 1], [0, 1])
+    p, d, _ = run_engine(10, u, v, w, ch, parent, dist, **opts)
+    check_against_oracle(10, u, v, w, ch, 0, p, d, f"cycle {opts}")
+    assert (d[2:6] == -1).all()
+    ch = D.make_changes([0, 3], [1, 9], [1, 1], [0, 1])
+    p, d, _ = run_engine(10, u, v, w, ch, parent, dist, **opts)
+    check_against_oracle(10, u, v, w, ch, 0, p, d, f"cross {opts}")
+    assert d[9] == 40 and d[3] == 41
