@@ -128,6 +128,14 @@ _sig("dsssp_gen_grid", C.c_int, C.c_int32, C.c_int32, C.c_double, C.c_int64, C.c
 _sig("dsssp_gen_changes", C.c_int, C.c_int32, C.c_int64, _i32p, _i32p, _i32p, C.c_int64, C.c_int64, C.c_int32,
      C.c_int32, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(_P))
 _sig("dsssp_max_degree_vertex", C.c_int32, C.c_int32, C.c_int64, _i32p, _i32p)
+_sig("dsssp_gen_changes_ref", C.c_int, C.c_int32, C.c_int64, _i32p, _i32p, _i32p, C.c_int64, C.c_int32, C.c_int32,
+     C.c_int32, C.c_uint64, C.POINTER(_P))
+_sig("dsssp_write_changes_file", C.c_int, C.c_char_p, _P, C.c_int64)
+_sig("dsssp_write_graph_binary", C.c_int, C.c_char_p, C.c_int32, C.c_int64, _i32p, _i32p, _i32p)
+_sig("dsssp_read_graph_binary", C.c_int, C.c_char_p, C.c_int32, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P),
+     C.POINTER(C.c_int64))
+_sig("dsssp_write_sssp_binary", C.c_int, C.c_char_p, C.c_int32, _i32p, _i64p)
+_sig("dsssp_read_sssp_binary", C.c_int, C.c_char_p, C.c_int32, _i32p, _i64p)
 _sig("dsssp_sssp_noalloc", C.c_int, C.c_int32, C.c_int64, _P, _P, C.c_int32, _P, _P, _P)
 
 NOALLOC_MAX_VERTICES = 65536
@@ -140,6 +148,8 @@ EXPORTED = [
     "dsssp_launch_count", "dsssp_last_error", "dsssp_strerror", "dsssp_free", "dsssp_read_graph_file",
     "dsssp_read_changes_file", "dsssp_read_sssp_file", "dsssp_write_sssp_file", "dsssp_gen_er", "dsssp_gen_rmat",
     "dsssp_gen_grid", "dsssp_gen_changes", "dsssp_max_degree_vertex", "dsssp_sssp_noalloc",
+    "dsssp_gen_changes_ref", "dsssp_write_changes_file", "dsssp_write_graph_binary", "dsssp_read_graph_binary",
+    "dsssp_write_sssp_binary", "dsssp_read_sssp_binary",
 ]
 
 
@@ -320,6 +330,40 @@ def write_sssp(path: str, parent, dist) -> None:
     _check(_lib.dsssp_write_sssp_file(str(path).encode(), len(parent), parent, dist), "write_sssp")
 
 
+def write_changes(path: str, changes: np.ndarray) -> None:
+    """Change records in the reference generator's line format (createChangedEdges.cpp:104, 116)."""
+    changes = np.ascontiguousarray(changes, CHANGE_DTYPE)
+    _check(_lib.dsssp_write_changes_file(str(path).encode(), changes.ctypes.data if len(changes) else None,
+                                         len(changes)), "write_changes")
+
+
+def write_graph_binary(path: str, n: int, u, v, w) -> None:
+    u = np.ascontiguousarray(u, np.int32)
+    v = np.ascontiguousarray(v, np.int32)
+    w = np.ascontiguousarray(w, np.int32)
+    _check(_lib.dsssp_write_graph_binary(str(path).encode(), int(n), len(u), u, v, w), "write_graph_binary")
+
+
+def read_graph_binary(path: str, n: int):
+    u, v, w, m = _P(), _P(), _P(), C.c_int64()
+    _check(_lib.dsssp_read_graph_binary(str(path).encode(), int(n), C.byref(u), C.byref(v), C.byref(w),
+                                        C.byref(m)), "read_graph_binary")
+    return _take_i32(u, m.value), _take_i32(v, m.value), _take_i32(w, m.value)
+
+
+def write_sssp_binary(path: str, parent, dist) -> None:
+    parent = np.ascontiguousarray(parent, np.int32)
+    dist = np.ascontiguousarray(dist, np.int64)
+    _check(_lib.dsssp_write_sssp_binary(str(path).encode(), len(parent), parent, dist), "write_sssp_binary")
+
+
+def read_sssp_binary(path: str, n: int):
+    parent = np.empty(n, np.int32)
+    dist = np.empty(n, np.int64)
+    _check(_lib.dsssp_read_sssp_binary(str(path).encode(), int(n), parent, dist), "read_sssp_binary")
+    return parent, dist
+
+
 # ---- generators -----------------------------------------------------------------------------
 
 def gen_er(n: int, m: int, wlo: int = 1, whi: int = 100, seed: int = 0):
@@ -351,6 +395,20 @@ def gen_changes(n: int, u, v, w, n_ins: int, n_del: int, kind: int = INS_UNIFORM
     _check(_lib.dsssp_gen_changes(n, len(u), u, v, w, n_ins, n_del, kind, scale, p0, p1, p2, wlo, whi, seed,
                                   C.byref(p)), "gen_changes")
     return _take_changes(p, n_ins + n_del)
+
+
+def gen_changes_ref(n: int, u, v, w, num_changes: int, ins_pct: int, wlo: int = 0, whi: int = 99,
+                    seed: int = 0) -> np.ndarray:
+    """The reference generator's sampling (createChangedEdges.cpp:75-122), seeded: coin-flip
+    interleaving, insertions of any pair u<v with w in [wlo, whi] (default [0, 99] as the
+    reference), deletions drawn from the edge list with replacement."""
+    u = np.ascontiguousarray(u, np.int32)
+    v = np.ascontiguousarray(v, np.int32)
+    w = np.ascontiguousarray(w, np.int32)
+    p = _P()
+    _check(_lib.dsssp_gen_changes_ref(n, len(u), u, v, w, num_changes, ins_pct, wlo, whi, seed, C.byref(p)),
+           "gen_changes_ref")
+    return _take_changes(p, num_changes)
 
 
 def max_degree_vertex(n: int, u, v) -> int:

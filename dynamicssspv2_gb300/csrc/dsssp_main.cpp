@@ -1,6 +1,11 @@
 // dsssp_main.cpp -- drop-in command line for SSSPmainForUndirected.cu (README.md:13-18):
 //
 //   dsssp_main <graph> <N> <M> <SSSP> <changes> [--out FILE] [--json FILE] [--device D]
+//              [--delta W] [--cache]
+//
+// --cache keeps a binary image of the graph and of the SSSP file next to them (<file>.dsssp.bin,
+// include/dsssp.h binary cache) and reads it instead of the text when it is at least as new as
+// the text; --delta sets the near-far bucket width of the relaxation rounds.
 //
 // Reads the three text formats, builds the device graph, loads the tree, applies the change
 // batch through the C ABI and prints the reference's stdout lines (SSSPmainForUndirected.cu:
@@ -9,6 +14,8 @@
 // reference stops its STEP1 clock without a sync), "Total affected nodes" is the real number
 // of cut-off vertices (the reference always prints 0), and --out writes the updated tree,
 // which the reference never does.  Exit status is 0 on success, 1 on any error.
+#include <sys/stat.h>
+
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -24,6 +31,13 @@ static long long us_since(clk::time_point t0) {
     return std::chrono::duration_cast<std::chrono::microseconds>(clk::now() - t0).count();
 }
 
+// true when `cache` exists and is not older than `text`
+static bool cache_fresh(const std::string& cache, const char* text) {
+    struct stat a, b;
+    if (stat(cache.c_str(), &a) != 0 || stat(text, &b) != 0) return false;
+    return a.st_mtime >= b.st_mtime;
+}
+
 static int die(const char* what, int rc) {
     fprintf(stderr, "dsssp_main: %s failed: %s (%s)\n", what, dsssp_strerror(rc), dsssp_last_error());
     return 1;
@@ -33,18 +47,21 @@ int main(int argc, char** argv) {
     if (argc < 6) {
         fprintf(stderr,
                 "usage: %s <graph> <number_of_nodes> <number_of_edges> <SSSP> <change_edges> "
-                "[--out FILE] [--json FILE] [--device D]\n",
+                "[--out FILE] [--json FILE] [--device D] [--delta W] [--cache]\n",
                 argv[0]);
         return 2;
     }
     const char* out_path = nullptr;
     const char* json_path = nullptr;
+    bool use_cache = false;
     dsssp_opts opts;
     dsssp_default_opts(&opts);
     for (int i = 6; i < argc; i++) {
         if (!strcmp(argv[i], "--out") && i + 1 < argc) out_path = argv[++i];
         else if (!strcmp(argv[i], "--json") && i + 1 < argc) json_path = argv[++i];
         else if (!strcmp(argv[i], "--device") && i + 1 < argc) opts.device = atoi(argv[++i]);
+        else if (!strcmp(argv[i], "--delta") && i + 1 < argc) opts.delta = atoi(argv[++i]);
+        else if (!strcmp(argv[i], "--cache")) use_cache = true;
         else {
             fprintf(stderr, "dsssp_main: unknown option %s\n", argv[i]);
             return 2;
@@ -61,8 +78,18 @@ int main(int argc, char** argv) {
     auto t0 = clk::now();
     int32_t *eu = nullptr, *ev = nullptr, *ew = nullptr;
     int64_t m = 0;
-    int rc = dsssp_read_graph_file(argv[1], nodes, &eu, &ev, &ew, &m);
-    if (rc) return die("reading the graph", rc);
+    const std::string gcache = std::string(argv[1]) + ".dsssp.bin";
+    int rc = 1;
+    if (use_cache && cache_fresh(gcache, argv[1])) {
+        rc = dsssp_read_graph_binary(gcache.c_str(), nodes, &eu, &ev, &ew, &m);
+        if (rc) fprintf(stderr, "dsssp_main: note: ignoring the graph cache: %s\n", dsssp_last_error());
+    }
+    if (rc) {
+        rc = dsssp_read_graph_file(argv[1], nodes, &eu, &ev, &ew, &m);
+        if (rc) return die("reading the graph", rc);
+        if (use_cache && dsssp_write_graph_binary(gcache.c_str(), nodes, m, eu, ev, ew) != DSSSP_OK)
+            fprintf(stderr, "dsssp_main: note: could not write the graph cache: %s\n", dsssp_last_error());
+    }
     printf("Reading input graph completed\n");
     printf("Time taken to read input graph: %lld microseconds\n", us_since(t0));
     if (edges_arg < m)
@@ -94,8 +121,18 @@ int main(int argc, char** argv) {
     printf("Reading input SSSP tree data...\n");
     t0 = clk::now();
     int64_t lossy = 0;
-    rc = dsssp_read_sssp_file(argv[4], nodes, parent.data(), dist.data(), &lossy);
-    if (rc) return die("reading the SSSP tree", rc);
+    const std::string tcache = std::string(argv[4]) + ".dsssp.bin";
+    rc = 1;
+    if (use_cache && cache_fresh(tcache, argv[4])) {
+        rc = dsssp_read_sssp_binary(tcache.c_str(), nodes, parent.data(), dist.data());
+        if (rc) fprintf(stderr, "dsssp_main: note: ignoring the tree cache: %s\n", dsssp_last_error());
+    }
+    if (rc) {
+        rc = dsssp_read_sssp_file(argv[4], nodes, parent.data(), dist.data(), &lossy);
+        if (rc) return die("reading the SSSP tree", rc);
+        if (use_cache && dsssp_write_sssp_binary(tcache.c_str(), nodes, parent.data(), dist.data()) != DSSSP_OK)
+            fprintf(stderr, "dsssp_main: note: could not write the tree cache: %s\n", dsssp_last_error());
+    }
     printf("Reading input SSSP tree data completed\n");
     printf("Time taken to read input input SSSP tree: %lld microseconds\n", us_since(t0));
     if (lossy)

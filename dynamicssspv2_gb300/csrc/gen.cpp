@@ -347,4 +347,47 @@ int dsssp_gen_changes(int32_t n, int64_t m, const int32_t* eu, const int32_t* ev
     return DSSSP_OK;
 }
 
+// The reference generator's sampling (createChangedEdges.cpp:75-122) with a seeded stream in
+// place of rand(): num_changes records, (int)(num_changes * ins_pct / 100) of them insertions.
+// Each step flips a coin; heads draws an insertion -- a uniform pair, redrawn when both ends
+// are equal, ordered u < v, weight uniform in [wlo, whi] (the reference: rand() % 100, i.e.
+// [0, 99]), possibly an existing edge or a repeat -- and tails a deletion of a uniform line of
+// the edge list, with replacement.  Records come out in draw order.  Allocates *changes.
+int dsssp_gen_changes_ref(int32_t n, int64_t m, const int32_t* eu, const int32_t* ev, const int32_t* ew,
+                          int64_t num_changes, int32_t ins_pct, int32_t wlo, int32_t whi, uint64_t seed,
+                          dsssp_change** changes) {
+    if (n < 2 || m < 0 || num_changes < 0 || ins_pct < 0 || ins_pct > 100 || wlo < 0 || whi < wlo || !changes)
+        return fail(DSSSP_E_INVAL, "gen_changes_ref: bad arguments");
+    const int64_t n_ins = (int64_t)((double)num_changes * ((double)ins_pct / 100.0));
+    const int64_t n_del = num_changes - n_ins;
+    if (n_del > 0 && (m == 0 || !eu || !ev || !ew)) return fail(DSSSP_E_INVAL, "gen_changes_ref: no lines to delete");
+    Stream coin(seed, 41), pick(seed, 42), wt(seed, 43), del(seed, 44);
+    std::vector<dsssp_change> out;
+    out.reserve((size_t)num_changes);
+    int64_t ii = 0, id = 0;
+    uint64_t step = 0;
+    const uint64_t cap = (uint64_t)(num_changes + 16) * 64;
+    while (ii < n_ins || id < n_del) {
+        if (step > cap) return fail(DSSSP_E_INVAL, "gen_changes_ref: too many redraws");
+        const uint64_t s = step++;
+        if (coin.at(s) & 1) {
+            if (ii >= n_ins) continue;
+            const int32_t x = (int32_t)pick.range(2 * s, 0, n - 1), y = (int32_t)pick.range(2 * s + 1, 0, n - 1);
+            if (x == y) continue;
+            out.push_back(dsssp_change{x < y ? x : y, x < y ? y : x, (int32_t)wt.range(s, wlo, whi), 1});
+            ii++;
+        } else {
+            if (id >= n_del) continue;
+            const int64_t li = del.range(s, 0, m - 1);
+            out.push_back(dsssp_change{eu[li], ev[li], ew[li], 0});
+            id++;
+        }
+    }
+    dsssp_change* res = (dsssp_change*)malloc(sizeof(dsssp_change) * (out.size() ? out.size() : 1));
+    if (!res) return fail(DSSSP_E_OOM, "gen_changes_ref: host allocation failed");
+    memcpy(res, out.data(), sizeof(dsssp_change) * out.size());
+    *changes = res;
+    return DSSSP_OK;
+}
+
 }  // extern "C"

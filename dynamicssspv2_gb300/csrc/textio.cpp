@@ -246,4 +246,29 @@ int dsssp_write_sssp_file(const char* path, int32_t n, const int32_t* parent, co
     return DSSSP_OK;
 }
 
+// Change records in the line format the reference's generator prints (createChangedEdges.cpp:
+// 104 for insertions, 116 for deletions): "u  v w 1 " and "u v w 0 ", each with a trailing
+// space.  Records with another op keep the deletion layout with their op.
+int dsssp_write_changes_file(const char* path, const dsssp_change* changes, int64_t k) {
+    if (!path || k < 0 || (k > 0 && !changes)) return fail(DSSSP_E_INVAL, "write_changes: bad arguments");
+    FILE* f = fopen(path, "wb");
+    if (!f) return fail(DSSSP_E_IO, "cannot create %s: %s", path, strerror(errno));
+    std::vector<char> buf;
+    buf.reserve(1 << 22);
+    char tmp[96];
+    for (int64_t i = 0; i < k; i++) {
+        const dsssp_change& c = changes[i];
+        const int len = c.op == 1 ? snprintf(tmp, sizeof(tmp), "%d  %d %d 1 \n", c.u, c.v, c.w)
+                                  : snprintf(tmp, sizeof(tmp), "%d %d %d %d \n", c.u, c.v, c.w, c.op);
+        buf.insert(buf.end(), tmp, tmp + len);
+        if (buf.size() > (1 << 22) - 128) {
+            if (fwrite(buf.data(), 1, buf.size(), f) != buf.size()) { fclose(f); return fail(DSSSP_E_IO, "write to %s failed", path); }
+            buf.clear();
+        }
+    }
+    if (!buf.empty() && fwrite(buf.data(), 1, buf.size(), f) != buf.size()) { fclose(f); return fail(DSSSP_E_IO, "write to %s failed", path); }
+    if (fclose(f) != 0) return fail(DSSSP_E_IO, "closing %s failed", path);
+    return DSSSP_OK;
+}
+
 }  // extern "C"

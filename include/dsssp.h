@@ -236,6 +236,28 @@ int dsssp_read_sssp_file(const char* path, int32_t n, int32_t* parent, int64_t* 
 int dsssp_write_sssp_file(const char* path, int32_t n, const int32_t* parent,
                           const int64_t* dist);
 
+/* Writes change records in the reference generator's line format (createChangedEdges.cpp:104,
+ * 116): "u  v w 1 " for an insertion, "u v w 0 " for a deletion; readable by
+ * dsssp_read_changes_file and by the reference's readin_changes. */
+int dsssp_write_changes_file(const char* path, const dsssp_change* changes, int64_t k);
+
+/* ---- binary cache ------------------------------------------------------------------
+ * Binary images of an edge list and of a tree (32-byte header with magic, sizes and a
+ * checksum, then the arrays) that load at file-system speed instead of being parsed.  A
+ * reader fails with DSSSP_E_IO on another magic, other sizes than expected, a short file or a
+ * checksum mismatch.  Replaces nothing in the reference (it parses text on every run,
+ * all_structure_undir.cuh:133-198). */
+int dsssp_write_graph_binary(const char* path, int32_t n, int64_t m, const int32_t* u,
+                             const int32_t* v, const int32_t* w);
+/* Allocates *u, *v, *w (free with dsssp_free); vertex ids are range-checked like the text
+ * reader's (DSSSP_E_BAD_VERTEX). */
+int dsssp_read_graph_binary(const char* path, int32_t n, int32_t** u, int32_t** v, int32_t** w,
+                            int64_t* m);
+int dsssp_write_sssp_binary(const char* path, int32_t n, const int32_t* parent,
+                            const int64_t* dist);
+/* parent[n] and dist[n] are caller-owned. */
+int dsssp_read_sssp_binary(const char* path, int32_t n, int32_t* parent, int64_t* dist);
+
 /* ---- seeded synthetic inputs (SplitMix64-based counter PRNG, same result on any host) --- */
 
 /* Erdos-Renyi: exactly m distinct undirected pairs u<v, w uniform in [wlo, whi]. */
@@ -265,6 +287,16 @@ int dsssp_gen_changes(int32_t n, int64_t m, const int32_t* eu, const int32_t* ev
                       const int32_t* ew, int64_t n_ins, int64_t n_del, int32_t ins_kind,
                       int32_t scale, double p0, double p1, double p2, int32_t wlo, int32_t whi,
                       uint64_t seed, dsssp_change** changes);
+
+/* The reference generator's sampling (createChangedEdges.cpp:49-125: `op_cE graph N k pct`)
+ * with a seeded stream instead of rand(): num_changes records of which
+ * (int)(num_changes*ins_pct/100) are insertions, interleaved by coin flips; insertions are
+ * uniform pairs u<v (u != v) with w uniform in [wlo, whi] (the reference uses [0, 99]) and
+ * may repeat or duplicate existing edges; deletions are lines of the edge list drawn with
+ * replacement.  Allocates *changes (num_changes records). */
+int dsssp_gen_changes_ref(int32_t n, int64_t m, const int32_t* eu, const int32_t* ev,
+                          const int32_t* ew, int64_t num_changes, int32_t ins_pct, int32_t wlo,
+                          int32_t whi, uint64_t seed, dsssp_change** changes);
 
 /* Vertex of maximum degree (lowest id on ties) of an edge list. */
 int32_t dsssp_max_degree_vertex(int32_t n, int64_t m, const int32_t* u, const int32_t* v);

@@ -185,3 +185,81 @@ def test_cli_usage_and_errors(tmp_path):
                        text=True)
     assert r.returncode == 1 and "reading the graph" in r.stderr
     assert r.stdout.startswith("Reading input graph...")
+
+
+# ---- binary cache, the reference generator's format and sampling -----------------------------
+
+def test_graph_binary_round_trip_and_rejections(tmp_path):
+    u, v, w = D.gen_rmat(12, 30001, seed=4)  # odd edge count: a padded checksum tail word
+    path = tmp_path / "g.bin"
+    D.write_graph_binary(str(path), 1 << 12, u, v, w)
+    u2, v2, w2 = D.read_graph_binary(str(path), 1 << 12)
+    assert (u2 == u).all() and (v2 == v).all() and (w2 == w).all()
+    with pytest.raises(D.DsssspError) as e:  # other vertex count than the cache holds
+        D.read_graph_binary(str(path), 1 << 11)
+    assert e.value.code == D.E_IO
+    data = bytearray(path.read_bytes())
+    data[32 + 4 * 12345] ^= 0x10  # one flipped payload bit
+    bad = tmp_path / "bad.bin"
+    bad.write_bytes(bytes(data))
+    with pytest.raises(D.DsssspError) as e:
+        D.read_graph_binary(str(bad), 1 << 12)
+    assert e.value.code == D.E_IO and "checksum" in str(e.value)
+    bad.write_bytes(path.read_bytes()[:-8])  # truncated
+    with pytest.raises(D.DsssspError) as e:
+        D.read_graph_binary(str(bad), 1 << 12)
+    assert e.value.code == D.E_IO
+    txt = tmp_path / "g.txt"
+    txt.write_text("0 1 2\n")
+    with pytest.raises(D.DsssspError) as e:  # a text file is not a cache
+        D.read_graph_binary(str(txt), 6)
+    assert e.value.code == D.E_IO
+    empty = tmp_path / "e.bin"
+    D.write_graph_binary(str(empty), 5, [], [], [])
+    assert all(len(a) == 0 for a in D.read_graph_binary(str(empty), 5))
+
+
+def test_tree_binary_round_trip(tmp_path):
+    rng = np.random.default_rng(1)
+    n = 777
+    parent = rng.integers(-1, n, n).astype(np.int32)
+    dist = np.where(parent == -1, -1, rng.integers(0, 1 << 40, n)).astype(np.int64)
+    path = tmp_path / "t.bin"
+    D.write_sssp_binary(str(path), parent, dist)
+    p2, d2 = D.read_sssp_binary(str(path), n)
+    assert (p2 == parent).all() and (d2 == dist).all()
+    with pytest.raises(D.DsssspError):
+        D.read_sssp_binary(str(path), n + 1)
+    with pytest.raises(D.DsssspError):  # a graph image is not a tree image
+        D.write_graph_binary(str(path), n, [0], [1], [2])
+        D.read_sssp_binary(str(path), n)
+
+
+def test_changes_file_in_the_reference_generator_format(tmp_path):
+    ch = D.make_changes([0, 0, 1], [1, 4, 4], [2, 4, 0], [0, 1, 1])
+    path = tmp_path / "cE.txt"
+    D.write_changes(str(path), ch)
+    # createChangedEdges.cpp:104 ("%d  %d %d 1 \n") and :116 ("%d %d %d 0 \n")
+    assert path.read_text() == "0 1 2 0 \n0  4 4 1 \n1  4 0 1 \n"
+    assert D.read_changes(str(path), 6).tolist() == ch.tolist()
+    big = D.gen_changes(1000, *D.gen_er(1000, 5000, seed=2), 300, 300, seed=3)
+    D.write_changes(str(path), big)
+    assert D.read_changes(str(path), 1000).tolist() == big.tolist()
+
+
+def test_reference_style_change_sampling():
+    n = 500
+    u, v, w = D.gen_er(n, 2000, 1, 100, seed=7)
+    ch = D.gen_changes_ref(n, u, v, w, 5000, 30, seed=11)
+    ins, dels = ch[ch["op"] == 1], ch[ch["op"] == 0]
+    assert len(ch) == 5000 and len(ins) == int(5000 * 0.30) and len(dels) == 5000 - len(ins)
+    assert (ins["u"] < ins["v"]).all() and (ins["w"] >= 0).all() and (ins["w"] <= 99).all()
+    assert (ins["w"] == 0).any()  # the reference's rand() % 100 includes weight 0
+    lines = set(zip(u.tolist(), v.tolist(), w.tolist()))
+    assert all(t in lines for t in zip(dels["u"].tolist(), dels["v"].tolist(), dels["w"].tolist()))
+    assert len(set(zip(dels["u"].tolist(), dels["v"].tolist()))) < len(dels)  # with replacement
+    first = ch["op"][:200]
+    assert 0 < first.sum() < 200  # coin-flip interleaving, not blocks
+    again = D.gen_changes_ref(n, u, v, w, 5000, 30, seed=11)
+    assert again.tolist() == ch.tolist()
+    assert D.gen_changes_ref(n, u, v, w, 5000, 30, seed=12).tolist() != ch.tolist()
