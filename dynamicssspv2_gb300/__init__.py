@@ -71,7 +71,7 @@ class Stats(C.Structure):
         (name, C.c_double)
         for name in ("t_step1_ms", "t_inval_ms", "t_relax_ms", "t_update_ms", "t_total_ms", "bytes_alg",
                      "bytes_alg_update")
-    ] + [("advances", C.c_int64)]
+    ] + [("advances", C.c_int64), ("tombstoned", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -110,6 +110,8 @@ _sig("dsssp_graph_get_opts", C.c_int, _P, C.POINTER(Opts))
 _sig("dsssp_graph_snapshot", C.c_int, _P)
 _sig("dsssp_graph_restore", C.c_int, _P, _P)
 _sig("dsssp_graph_compact", C.c_int, _P)
+_sig("dsssp_graph_health", C.c_int, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+     C.POINTER(C.c_int64))
 _sig("dsssp_host_alloc", _P, C.c_size_t)
 _sig("dsssp_host_free", None, _P)
 _sig("dsssp_launch_count", C.c_int64)
@@ -149,7 +151,7 @@ EXPORTED = [
     "dsssp_read_changes_file", "dsssp_read_sssp_file", "dsssp_write_sssp_file", "dsssp_gen_er", "dsssp_gen_rmat",
     "dsssp_gen_grid", "dsssp_gen_changes", "dsssp_max_degree_vertex", "dsssp_sssp_noalloc",
     "dsssp_gen_changes_ref", "dsssp_write_changes_file", "dsssp_write_graph_binary", "dsssp_read_graph_binary",
-    "dsssp_write_sssp_binary", "dsssp_read_sssp_binary",
+    "dsssp_write_sssp_binary", "dsssp_read_sssp_binary", "dsssp_graph_health",
 ]
 
 
@@ -234,6 +236,12 @@ class Graph:
         s = C.c_int32()
         _check(_lib.dsssp_graph_info(self._h, C.byref(n), C.byref(e), C.byref(c), C.byref(b), C.byref(s)), "info")
         return {"n": n.value, "entries": e.value, "capacity": c.value, "device_bytes": b.value, "source": s.value}
+
+    def health(self) -> dict:
+        """Live and tombstoned adjacency entries, used and total spare-region slots."""
+        a, b, c, d = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        _check(_lib.dsssp_graph_health(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)), "health")
+        return {"live": a.value, "dead": b.value, "spare_used": c.value, "spare_total": d.value}
 
     def tree_load(self, parent, dist) -> None:
         parent = np.ascontiguousarray(parent, np.int32)

@@ -66,6 +66,8 @@ enum StatIdx {
     ST_ITEMS,
     ST_DIST_OVF,
     ST_ADVANCES,
+    ST_TOMBS,
+    ST_LIVE_INS,
     ST_COUNT
 };
 

@@ -407,7 +407,10 @@ struct dsssp_graph {
     dsssp_opts o{};
     cudaStream_t stream = nullptr;
     long long cap_total = 0;
-    long long entries = 0;
+    long long entries = 0;     // live adjacency entries
+    long long dead = 0;        // tombstoned entries since the last layout
+    long long spare_lo = 0;    // first slot of the spare region
+    long long spare_top = 0;   // its bump pointer as of the last row growth
     DevGraph dg{};
     // batch buffers
     int4* d_chg = nullptr;
@@ -450,6 +453,7 @@ struct dsssp_graph {
     unsigned* s_twin = nullptr;
     long long s_cap = 0;
     long long s_entries = 0;
+    long long s_dead = 0;
     int s_src = -1;
     bool has_snap = false;
     bool has_tree = false;
@@ -604,6 +608,7 @@ int layout_rows(dsssp_graph* g, unsigned long long* keys_in, long long total, co
     // slack move into (bump allocator, reset by the next layout)
     const long long main_slots = cap_total;
     cap_total = main_slots + main_slots * g->o.spare_pct / 100 + 1024;
+    const long long spare_lo = main_slots;
     if (!rc) {
         const unsigned long long sp[2] = {(unsigned long long)main_slots, (unsigned long long)cap_total};
         cudaError_t e = cudaMemcpyAsync(g->d_spare, sp, sizeof(sp), cudaMemcpyHostToDevice, s);
@@ -634,6 +639,9 @@ int layout_rows(dsssp_graph* g, unsigned long long* keys_in, long long total, co
         twin = nullptr;
         g->cap_total = cap_total;
         g->entries = total;
+        g->dead = 0;
+        g->spare_lo = spare_lo;
+        g->spare_top = spare_lo;
         rc = ensure_work(g);
     }
     dfree(cap);
@@ -787,6 +795,7 @@ void fill_stats(const dsssp_graph* g, const Ctl& c, dsssp_stats* st, bool events
     st->n_killed = (int64_t)c.killed;
     st->work_items = (int64_t)c.stat[ST_ITEMS];
     st->advances = (int64_t)c.stat[ST_ADVANCES];
+    st->tombstoned = (int64_t)c.stat[ST_TOMBS];
     // algorithmic bytes (byte model: each item is touched once by this algorithm)
     //   per adjacency entry scanned 16 (entry + neighbour state), per work item 40 (item write
     //   + read, row descriptor, owner state), per pushed vertex 20 (push tag, degree), per
@@ -861,8 +870,11 @@ int grow_rows(dsssp_graph* g, int novf, cudaStream_t s) {
     k_grow_reset<<<blocks_for(rows_max), kThreads, 0, s>>>(q);
     count_launch(3);
     CK(cudaMemcpyAsync(&fail, g->d_fail, sizeof(int), cudaMemcpyDeviceToHost, s), "row growth");
+    unsigned long long top = 0;
+    CK(cudaMemcpyAsync(&top, g->d_spare, sizeof(top), cudaMemcpyDeviceToHost, s), "row growth");
     CK(cudaStreamSynchronize(s), "row growth");
     if (fail) return dsssp::fail(DSSSP_E_CUDA, "row growth: twin index out of range (internal error)");
+    g->spare_top = (long long)top;
     return DSSSP_OK;
 }
 
@@ -918,6 +930,11 @@ int finish_batch(dsssp_graph* g, dsssp_stats* st) {
         CK(cudaStreamSynchronize(s), "batch");
     }
     fill_stats(g, *g->h_ctl, st, g->pend_events, g->pend_k, repacks);
+    if (!repacks) {  // a repack counts the live entries itself
+        const long long tombs = (long long)g->h_ctl->stat[ST_TOMBS];
+        g->entries += 2 * (long long)g->h_ctl->stat[ST_LIVE_INS] - tombs;
+        g->dead += tombs;
+    }
     if (g->h_ctl->status != 0) reset_tags(g, s);
     if (g->h_ctl->stat[ST_DIST_OVF] > 0 && g->h_ctl->status == 0) return status_code(DSSSP_E_OVERFLOW);
     if (g->h_ctl->status == DSSSP_E_TIMEOUT) {
@@ -1376,6 +1393,7 @@ int dsssp_graph_snapshot(dsssp_graph* g) {
     CK(cudaMemcpyAsync(g->s_spare, g->d_spare, sizeof(g->s_spare), cudaMemcpyDeviceToHost, s), "snapshot");
     CK(cudaStreamSynchronize(s), "snapshot");
     g->s_entries = g->entries;
+    g->s_dead = g->dead;
     g->s_src = g->src;
     g->s_has_tree = g->has_tree;
     g->has_snap = true;
@@ -1408,8 +1426,20 @@ int dsssp_graph_restore(dsssp_graph* g, void* stream) {
         CK(cudaMemcpyAsync(g->dg.twin, g->s_twin, (size_t)g->s_cap * 4, cudaMemcpyDeviceToDevice, s), "restore");
     CK(cudaMemcpyAsync(g->d_spare, g->s_spare, sizeof(g->s_spare), cudaMemcpyHostToDevice, s), "restore");
     g->entries = g->s_entries;
+    g->dead = g->s_dead;
+    g->spare_top = (long long)g->s_spare[0];
     g->src = g->s_src;
     g->has_tree = g->s_has_tree;
+    return DSSSP_OK;
+}
+
+int dsssp_graph_health(const dsssp_graph* g, int64_t* live_entries, int64_t* dead_entries, int64_t* spare_used,
+                       int64_t* spare_total) {
+    if (!g) return fail(DSSSP_E_INVAL, "graph_health: NULL graph");
+    if (live_entries) *live_entries = g->entries;
+    if (dead_entries) *dead_entries = g->dead;
+    if (spare_used) *spare_used = g->spare_top - g->spare_lo;
+    if (spare_total) *spare_total = g->cap_total - g->spare_lo;
     return DSSSP_OK;
 }
 

@@ -633,26 +633,26 @@ __device__ __forceinline__ void tombstone_twin(const UpdParams& p, long long j) 
     else set_status(p.g.ctl, -4 /* twin index out of range: internal error */);
 }
 
+// Tombstones one matching entry; the compare-and-swap makes the count exact when a batch
+// deletes one line twice.  Returns the entries tombstoned (2 with the twin).
+__device__ __forceinline__ unsigned tombstone_at(const UpdParams& p, long long j, int w, bool with_twin) {
+    if (atomicCAS(&p.g.adj[j].y, w, -1) != w) return 0;
+    if (with_twin) tombstone_twin(p, j);
+    return with_twin ? 2u : 1u;
+}
+
 // Tombstones every live entry (col, w) of row r; with the twin index also their reverse
-// entries.  Returns the number of entries examined.
+// entries.  Returns the number of entries examined; `dead` counts the entries tombstoned.
 __device__ unsigned long long tombstone_row(const UpdParams& p, const RowDesc& rd, int sorted_len, int col, int w,
-                                            bool with_twin) {
-    int2* adj = p.g.adj;
+                                            bool with_twin, unsigned long long& dead) {
+    const int2* adj = p.g.adj;
     const long long sl = rd.start + sorted_len, end = rd.start + rd.deg;
     long long j = lower_col(adj, rd.start, sl, col);
     unsigned long long probed = 1;
-    for (; j < sl && adj[j].x == col; j++, probed++) {
-        if (adj[j].y == w) {
-            adj[j].y = -1;
-            if (with_twin) tombstone_twin(p, j);
-        }
-    }
-    for (j = sl; j < end; j++, probed++) {
-        if (adj[j].x == col && adj[j].y == w) {
-            adj[j].y = -1;
-            if (with_twin) tombstone_twin(p, j);
-        }
-    }
+    for (; j < sl && adj[j].x == col; j++, probed++)
+        if (adj[j].y == w) dead += tombstone_at(p, j, w, with_twin);
+    for (j = sl; j < end; j++, probed++)
+        if (adj[j].x == col && adj[j].y == w) dead += tombstone_at(p, j, w, with_twin);
     return probed;
 }
 
@@ -686,7 +686,7 @@ __global__ void k_delete(UpdParams p) {
     Ctl* ctl = p.g.ctl;
     if (__ldcg(&ctl->status) != 0) return;  // set by k_prepare: same for every thread
     const long long nthreads = (long long)gridDim.x * blockDim.x;
-    unsigned long long probed = 0, roots = 0;
+    unsigned long long probed = 0, roots = 0, dead = 0;
     __shared__ unsigned s_nroots;
     if (threadIdx.x == 0) s_nroots = 0;
     __syncthreads();
@@ -716,10 +716,10 @@ __global__ void k_delete(UpdParams p) {
                 // search the shorter row; each match's reverse entry is found through twin[]
                 const bool use_a = ra.deg <= rb.deg;
                 probed += tombstone_row(p, use_a ? ra : rb, p.g.sorted_len[use_a ? a : b], (int)(use_a ? b : a), c.z,
-                                        true);
+                                        true, dead);
             } else {
-                probed += tombstone_row(p, ra, p.g.sorted_len[a], (int)b, c.z, false);
-                probed += tombstone_row(p, rb, p.g.sorted_len[b], (int)a, c.z, false);
+                probed += tombstone_row(p, ra, p.g.sorted_len[a], (int)b, c.z, false, dead);
+                probed += tombstone_row(p, rb, p.g.sorted_len[b], (int)a, c.z, false, dead);
             }
             if (c.z >= 0 && !hash_insert(p, dpair_key(a, b), c.z)) set_status(ctl, -4 /* deletion set full */);
         }
@@ -730,6 +730,7 @@ __global__ void k_delete(UpdParams p) {
     stage_flush(roots_stage, p.g.invq, &ctl->inv_count, (unsigned)p.g.n, true, 0, ctl);
     block_add(&ctl->stat[ST_ROOTS], roots);
     block_add(&ctl->stat[ST_DEL_PROBED], probed);
+    block_add(&ctl->stat[ST_TOMBS], dead);
 }
 
 // Insertions that no deletion of the batch removes go into row slack, both directions.  An
@@ -762,7 +763,7 @@ __global__ void k_append(UpdParams p) {
     const Stage far_stage{stage_mem + kMaxWarps * kBuf, kMaxWarps * kBuf, &s_nf};
     const unsigned seed_cap = (unsigned)min(2 * p.k, (long long)g.n);  // distinct claimed ends
     LocalStats ls;
-    unsigned long long killed = 0, ovf = 0;
+    unsigned long long killed = 0, ovf = 0, live_ins = 0;
     // the loop is uniform over the CTA (the staging flushes are CTA-collective)
     for (long long cbase = (long long)blockIdx.x * blockDim.x; cbase < p.k; cbase += nthreads) {
         const long long i = cbase + threadIdx.x;
@@ -776,6 +777,7 @@ __global__ void k_append(UpdParams p) {
                 killed++;
             } else {
                 alive = 1;
+                live_ins++;
                 long long at[2];
 #pragma unroll
                 for (int side = 0; side < 2; side++) {
@@ -827,6 +829,7 @@ __global__ void k_append(UpdParams p) {
     stage_flush(far_stage, g.far0, &ctl->fc[0], (unsigned)g.n, true, 0, ctl);
     flush_stats(ctl, ls);
     block_add(&ctl->stat[ST_OVF], ovf);
+    block_add(&ctl->stat[ST_LIVE_INS], live_ins);
     unsigned long long kk = warp_sum_u64(killed);
     if (lane_id() == 0 && kk) atomicAdd(&ctl->killed, (unsigned)kk);
 }

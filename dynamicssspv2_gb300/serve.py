@@ -11,6 +11,11 @@ and each result equals applying that batch alone (distances bit-exact; parents a
 tree, possibly another one on ties).  Requests that arrive while an epoch runs wait for the
 next one; requests for tenants that were not admitted are refused.
 
+Storage upkeep runs between epochs, only while no request waits: when the store's tombstoned
+entries exceed `compact_dead_frac` of its live entries, or the spare region that overflowing
+rows move into is more than `compact_spare_frac` used, the store is compacted (tombstones
+dropped, rows re-sorted, full slack restored) so later batches keep finding slack.
+
 No counterpart in the reference, which applies one batch per process run.
 """
 from __future__ import annotations
@@ -68,7 +73,7 @@ class Request:
 
 class Server:
     def __init__(self, tenants, memory_budget: int | None = None, max_epoch_requests: int | None = None,
-                 **opts):
+                 compact_dead_frac: float | None = 0.25, compact_spare_frac: float = 0.75, **opts):
         self.tenants = list(tenants)
         slack_pct = opts.get("slack_pct", 25)
         slack_min = opts.get("slack_min", 4)
@@ -88,6 +93,10 @@ class Server:
             self.pool = GraphPool([(t.n, t.u, t.v, t.w) for t in ts], **opts)
             self.pool.tree_compute([t.src for t in ts])
         self.epochs = 0
+        self.compact_dead_frac = compact_dead_frac
+        self.compact_spare_frac = compact_spare_frac
+        self.compactions = 0
+        self.compact_ms = []
 
     def close(self) -> None:
         if self.pool is not None:
@@ -98,6 +107,24 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+    def needs_compaction(self) -> bool:
+        if self.pool is None or self.compact_dead_frac is None:
+            return False
+        h = self.pool.graph.health()
+        if h["dead"] > self.compact_dead_frac * max(1, h["live"]):
+            return True
+        return h["spare_total"] > 0 and h["spare_used"] > self.compact_spare_frac * h["spare_total"]
+
+    def upkeep(self) -> bool:
+        """Compacts the store if it needs it; call only while no request waits."""
+        if not self.needs_compaction():
+            return False
+        t = time.perf_counter()
+        self.pool.graph.compact()
+        self.compact_ms.append((time.perf_counter() - t) * 1e3)
+        self.compactions += 1
+        return True
 
     def tree(self, tenant: int):
         return self.pool.tree_read(self.slot[tenant])
@@ -126,6 +153,7 @@ class Server:
                 queues[r.tenant].append(r)
                 pending += 1
             if pending == 0:
+                self.upkeep()  # idle: storage upkeep is off the latency path
                 if nxt < len(reqs):
                     wait = reqs[nxt].arrival - clock()
                     if wait > 0:

@@ -103,6 +103,7 @@ typedef struct {
     double bytes_alg;          /* algorithmic bytes of the batch (byte model of the engine) */
     double bytes_alg_update;   /* the part moved by the persistent update kernel */
     int64_t advances;          /* near-far threshold advances (0 when delta = 0) */
+    int64_t tombstoned;        /* adjacency entries the batch's deletions tombstoned */
 } dsssp_stats;
 
 /* ---- engine ------------------------------------------------------------------------ */
@@ -173,6 +174,12 @@ int dsssp_graph_restore(dsssp_graph* g, void* stream);
 
 /* Removes tombstones and re-sorts every row, restoring full slack (off the update path). */
 int dsssp_graph_compact(dsssp_graph* g);
+
+/* Storage health, to decide when to compact: live adjacency entries, tombstoned entries
+ * since the last layout, and used / total slots of the spare region that rows move into
+ * when they run out of slack.  Any pointer may be NULL. */
+int dsssp_graph_health(const dsssp_graph* g, int64_t* live_entries, int64_t* dead_entries,
+                       int64_t* spare_used, int64_t* spare_total);
 
 /* Pinned host memory for fast copies (cudaMallocHost) and its release. */
 void* dsssp_host_alloc(size_t bytes);

@@ -216,7 +216,11 @@ def test_sequence_of_batches(delta):
             lw = np.concatenate([cw, ins["w"]])
             keep = kept[: len(lu)].astype(bool)
             cu, cv, cw = lu[keep].astype(np.int32), lv[keep].astype(np.int32), lw[keep].astype(np.int32)
+        h = g.health()
+        assert h["live"] == 2 * len(cu) and h["dead"] > 0
         g.compact()
+        h = g.health()
+        assert h["live"] == 2 * len(cu) and h["dead"] == 0 and h["spare_used"] == 0
         ch = D.gen_changes(n, cu, cv, cw, 100, 100, seed=999)
         g.apply_batch(ch)
         p, d = g.tree_read()
