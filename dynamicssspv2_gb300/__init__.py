@@ -56,6 +56,8 @@ class Opts(C.Structure):
         ("max_rounds", C.c_int64),
         ("spare_pct", C.c_int32),
         ("delta", C.c_int32),
+        ("launch_graph", C.c_int32),
+        ("reserved1", C.c_int32),
     ]
 
 
@@ -71,7 +73,7 @@ class Stats(C.Structure):
         (name, C.c_double)
         for name in ("t_step1_ms", "t_inval_ms", "t_relax_ms", "t_update_ms", "t_total_ms", "bytes_alg",
                      "bytes_alg_update")
-    ] + [("advances", C.c_int64), ("tombstoned", C.c_int64)]
+    ] + [("advances", C.c_int64), ("tombstoned", C.c_int64), ("graph_launch", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -26,6 +26,7 @@ namespace dsssp {
 cudaError_t launch_front(const UpdParams& p, int grid, cudaStream_t s);
 cudaError_t update_occupancy(int block, int* blocks_per_sm);
 cudaError_t launch_update(const UpdParams& p, int grid, int block, cudaStream_t s);
+void batch_kernels(const void* fns[4]);
 
 static std::atomic<long long> g_launches{0};
 void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
@@ -436,12 +437,19 @@ struct dsssp_graph {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     unsigned epoch = 0;
     int coop_grid = 0;
+    // the batch launch sequence as an instantiated CUDA graph (opts.launch_graph)
+    cudaGraph_t bgraph = nullptr;
+    cudaGraphExec_t bexec = nullptr;
+    cudaGraphNode_t bn_hash = nullptr, bn_kern[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool bgraph_timing = false;
+    bool bgraph_failed = false;
     // pending batch
     bool pending = false;
     long long pend_k = 0;
     const int4* pend_chg = nullptr;
     cudaStream_t pend_stream = nullptr;
     bool pend_events = false;
+    bool pend_graph = false;
     // tree staging
     int* d_par = nullptr;
     long long* d_dist = nullptr;
@@ -796,6 +804,7 @@ void fill_stats(const dsssp_graph* g, const Ctl& c, dsssp_stats* st, bool events
     st->work_items = (int64_t)c.stat[ST_ITEMS];
     st->advances = (int64_t)c.stat[ST_ADVANCES];
     st->tombstoned = (int64_t)c.stat[ST_TOMBS];
+    st->graph_launch = g->pend_graph ? 1 : 0;
     // algorithmic bytes (byte model: each item is touched once by this algorithm)
     //   per adjacency entry scanned 16 (entry + neighbour state), per work item 40 (item write
     //   + read, row descriptor, owner state), per pushed vertex 20 (push tag, degree), per
@@ -878,21 +887,143 @@ int grow_rows(dsssp_graph* g, int novf, cudaStream_t s) {
     return DSSSP_OK;
 }
 
+// Kernel-node parameters of the batch kernels for the parameter block p.
+struct BatchNodes {
+    UpdParams p;
+    void* args[1];
+    cudaKernelNodeParams kp[4];
+    cudaMemsetParams hash;
+};
+
+void batch_nodes(const dsssp_graph* g, const UpdParams& p, unsigned long long h, BatchNodes& b) {
+    const void* fns[4];
+    batch_kernels(fns);
+    b.p = p;
+    b.args[0] = &b.p;
+    const long long need = (p.k + 255) / 256;
+    const unsigned front = (unsigned)(need < g->num_sms * 8 ? need : g->num_sms * 8);  // as launch_front
+    for (int i = 0; i < 4; i++) {
+        cudaKernelNodeParams& k = b.kp[i];
+        memset(&k, 0, sizeof(k));
+        k.func = const_cast<void*>(fns[i]);
+        k.gridDim = dim3(i < 3 ? front : (unsigned)g->coop_grid);
+        k.blockDim = dim3(i < 3 ? 256u : (unsigned)g->o.block);
+        k.sharedMemBytes = 0;
+        k.kernelParams = b.args;
+        k.extra = nullptr;
+    }
+    memset(&b.hash, 0, sizeof(b.hash));
+    b.hash.dst = g->d_hset;
+    b.hash.value = 0xFF;
+    b.hash.elementSize = 1;
+    b.hash.width = sizeof(DelSlot) * (size_t)h;
+    b.hash.height = 1;
+    b.hash.pitch = 0;
+}
+
+void drop_batch_graph(dsssp_graph* g) {
+    if (g->bexec) cudaGraphExecDestroy(g->bexec);
+    if (g->bgraph) cudaGraphDestroy(g->bgraph);
+    g->bexec = nullptr;
+    g->bgraph = nullptr;
+}
+
+// Builds and instantiates the batch graph: [event 0] control-block reset, deletion-set reset,
+// k_prepare, k_delete, k_append, [event 1] k_update (cooperative), [event 2] status read.
+cudaError_t build_batch_graph(dsssp_graph* g, const BatchNodes& b, bool timing) {
+    drop_batch_graph(g);
+    cudaGraph_t gr = nullptr;
+    cudaError_t e = cudaGraphCreate(&gr, 0);
+    if (e != cudaSuccess) return e;
+    g->bgraph = gr;
+    cudaGraphNode_t prev = nullptr, n = nullptr;
+    auto dep = [&]() { return prev ? 1 : 0; };
+    if (timing && (e = cudaGraphAddEventRecordNode(&n, gr, &prev, dep(), g->ev[0])) == cudaSuccess) prev = n;
+    if (e == cudaSuccess) {
+        cudaMemsetParams c;
+        memset(&c, 0, sizeof(c));
+        const size_t off = offsetof(Ctl, status);  // line 1 onwards, as clear_ctl
+        c.dst = (char*)g->dg.ctl + off;
+        c.value = 0;
+        c.elementSize = 1;
+        c.width = sizeof(Ctl) - off;
+        c.height = 1;
+        if ((e = cudaGraphAddMemsetNode(&n, gr, &prev, dep(), &c)) == cudaSuccess) prev = n;
+    }
+    if (e == cudaSuccess && (e = cudaGraphAddMemsetNode(&n, gr, &prev, dep(), &b.hash)) == cudaSuccess) {
+        prev = n;
+        g->bn_hash = n;
+    }
+    for (int i = 0; i < 4 && e == cudaSuccess; i++) {
+        if (i == 3 && timing && (e = cudaGraphAddEventRecordNode(&n, gr, &prev, dep(), g->ev[1])) == cudaSuccess)
+            prev = n;
+        if (e != cudaSuccess) break;
+        if ((e = cudaGraphAddKernelNode(&n, gr, &prev, dep(), &b.kp[i])) != cudaSuccess) break;
+        if (i == 3) {  // the update kernel's grid barrier needs all CTAs resident
+            cudaLaunchAttributeValue v;
+            memset(&v, 0, sizeof(v));
+            v.cooperative = 1;
+            if ((e = cudaGraphKernelNodeSetAttribute(n, cudaLaunchAttributeCooperative, &v)) != cudaSuccess) break;
+        }
+        prev = n;
+        g->bn_kern[i] = n;
+    }
+    if (e == cudaSuccess && timing && (e = cudaGraphAddEventRecordNode(&n, gr, &prev, dep(), g->ev[2])) == cudaSuccess)
+        prev = n;
+    if (e == cudaSuccess &&
+        (e = cudaGraphAddMemcpyNode1D(&n, gr, &prev, dep(), g->h_ctl, g->dg.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost)) ==
+            cudaSuccess)
+        prev = n;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&g->bexec, gr, 0);
+    if (e != cudaSuccess) {
+        drop_batch_graph(g);
+        cudaGetLastError();
+    }
+    g->bgraph_timing = timing;
+    return e;
+}
+
+// Replays the batch graph with this batch's parameters; false = use plain launches.
+bool launch_batch_graph(dsssp_graph* g, const UpdParams& p, unsigned long long h, cudaStream_t s) {
+    if (!g->o.launch_graph || g->bgraph_failed || p.k <= 0) return false;
+    BatchNodes b;
+    batch_nodes(g, p, h, b);
+    const bool timing = g->o.timing != 0;
+    cudaError_t e = cudaSuccess;
+    if (!g->bexec || g->bgraph_timing != timing) {
+        e = build_batch_graph(g, b, timing);
+    } else {
+        e = cudaGraphExecMemsetNodeSetParams(g->bexec, g->bn_hash, &b.hash);
+        for (int i = 0; i < 4 && e == cudaSuccess; i++) e = cudaGraphExecKernelNodeSetParams(g->bexec, g->bn_kern[i], &b.kp[i]);
+    }
+    if (e == cudaSuccess) e = cudaGraphLaunch(g->bexec, s);
+    if (e != cudaSuccess) {  // never again for this graph: plain launches
+        cudaGetLastError();
+        drop_batch_graph(g);
+        g->bgraph_failed = true;
+        return false;
+    }
+    count_launch(4);
+    return true;
+}
+
 // Enqueues one batch (records already on the device).
 int enqueue_batch(dsssp_graph* g, const int4* d_chg, long long k, cudaStream_t s) {
     // k_append already claims frontier tags: restart the tag sequence before it could wrap
     // (the mirror holds the round base the last kernel left)
     if (g->h_ctl->round_base > 0xF0000000u) reset_tags(g, g->stream);
+    const size_t hb = (size_t)(2ull * (unsigned long long)k);
+    unsigned long long h = 64;
+    while (h < hb) h <<= 1;  // this batch uses the first h slots of the deletion set
+    UpdParams p = make_params(g, d_chg, k, 0);
+    p.hmask = h - 1;
+    g->pend_graph = launch_batch_graph(g, p, h, s);
+    if (g->pend_graph) return DSSSP_OK;
     const bool ev = g->o.timing != 0;
     if (ev) CK(cudaEventRecord(g->ev[0], s), "event");
     int rc = clear_ctl(g, s);
     if (rc) return rc;
-    const size_t hb = (size_t)(2ull * (unsigned long long)k);
-    unsigned long long h = 64;
-    while (h < hb) h <<= 1;  // this batch uses the first h slots of the deletion set
     CK(cudaMemsetAsync(g->d_hset, 0xFF, sizeof(DelSlot) * h, s), "deletion set reset");
-    UpdParams p = make_params(g, d_chg, k, 0);
-    p.hmask = h - 1;
     CK(launch_front(p, g->num_sms * 8, s), "insert/delete kernels");
     if (ev) CK(cudaEventRecord(g->ev[1], s), "event");
     CK(launch_update(p, g->coop_grid, g->o.block, s), "update kernel");
@@ -971,6 +1102,8 @@ void dsssp_default_opts(dsssp_opts* o) {
     o->max_rounds = 0;
     o->spare_pct = 12;
     o->delta = 0;
+    o->launch_graph = 1;
+    o->reserved1 = 0;
 }
 
 const char* dsssp_strerror(int code) {
@@ -1020,6 +1153,8 @@ void dsssp_graph_destroy(dsssp_graph* g) {
     dfree(g->d_need); dfree(g->d_gidx); dfree(g->d_grow_list); dfree(g->d_grow_count); dfree(g->d_old_start);
     dfree(g->d_old_cap); dfree(g->d_fail);
     dfree(g->s_state); dfree(g->s_rows); dfree(g->s_sorted); dfree(g->s_adj);
+    if (g->bexec) cudaGraphExecDestroy(g->bexec);
+    if (g->bgraph) cudaGraphDestroy(g->bgraph);
     if (g->h_ctl) cudaFreeHost(g->h_ctl);
     for (auto& e : g->ev)
         if (e) cudaEventDestroy(e);
@@ -1258,6 +1393,7 @@ int dsssp_tree_compute_multi(dsssp_graph* g, const int32_t* srcs, int32_t k, dss
     CK(cudaStreamSynchronize(s), "tree compute");
     g->src = uniq[0];
     g->has_tree = g->h_ctl->status == 0;
+    g->pend_graph = false;
     fill_stats(g, *g->h_ctl, st, ev, 0, 0);
     if (g->h_ctl->status != 0) reset_tags(g, s);
     if (g->h_ctl->stat[ST_DIST_OVF] > 0 && g->h_ctl->status == 0) return status_code(DSSSP_E_OVERFLOW);

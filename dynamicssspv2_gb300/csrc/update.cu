@@ -1116,6 +1116,14 @@ cudaError_t launch_front(const UpdParams& p, int grid, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// The batch kernels as graph-node functions: k_prepare, k_delete, k_append, k_update.
+void batch_kernels(const void* fns[4]) {
+    fns[0] = (const void*)k_prepare;
+    fns[1] = (const void*)k_delete;
+    fns[2] = (const void*)k_append;
+    fns[3] = (const void*)k_update;
+}
+
 cudaError_t update_occupancy(int block, int* blocks_per_sm) {
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_update, block, 0);
 }

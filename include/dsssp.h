@@ -74,6 +74,12 @@ typedef struct {
                              T moves to (least waiting distance) + delta.  Same results; far
                              fewer rounds and relaxations on high-diameter graphs.  Costs 12
                              bytes per vertex, allocated when first enabled. */
+    int32_t launch_graph; /* 1 = a batch's launch sequence (control-block reset, deletion-set
+                             reset, the four kernels, the status read) is replayed from an
+                             instantiated CUDA graph whose node parameters are updated per
+                             batch; 0 = plain stream launches.  Falls back to plain launches
+                             if the graph cannot be built. */
+    int32_t reserved1;
 } dsssp_opts;
 
 /* Counters of one batch (or one tree computation), read back from the device. */
@@ -104,6 +110,7 @@ typedef struct {
     double bytes_alg_update;   /* the part moved by the persistent update kernel */
     int64_t advances;          /* near-far threshold advances (0 when delta = 0) */
     int64_t tombstoned;        /* adjacency entries the batch's deletions tombstoned */
+    int64_t graph_launch;      /* 1 = the batch was replayed from the instantiated CUDA graph */
 } dsssp_stats;
 
 /* ---- engine ------------------------------------------------------------------------ */

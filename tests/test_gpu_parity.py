@@ -65,6 +65,7 @@ OPTION_SETS = [
     {"delta": 1},                                          # near-far rounds, narrowest buckets
     {"delta": 25},
     {"delta": 25, "bfs_levels": 0, "small_deg": 4, "large_deg": 4, "chunk": 32},
+    {"launch_graph": 0},                                   # plain stream launches
 ]
 
 
@@ -393,3 +394,36 @@ def test_insertion_into_cut_off_root(opts):
     p, d, _ = run_engine(10, u, v, w, ch, parent, dist, **opts)
     check_against_oracle(10, u, v, w, ch, 0, p, d, f"cross {opts}")
     assert d[9] == 40 and d[3] == 41
+
+
+def test_graph_replay_matches_plain_launches():
+    """The batch sequence replayed from the instantiated CUDA graph (node parameters updated
+    per batch: batch size, deletion-set size, epoch) gives what plain launches give, across
+    batch sizes, a timing switch (graph rebuilt) and a row growth."""
+    n, m = 20000, 80000
+    u, v, w = D.gen_er(n, m, 1, 100, 31)
+    parent, dist = initial_tree(n, u, v, w)
+    with D.Graph(n, u, v, w, slack_pct=0, slack_min=1) as ga, D.Graph(n, u, v, w, slack_pct=0, slack_min=1,
+                                                                       launch_graph=0) as gb:
+        ga.tree_load(parent, dist)
+        gb.tree_load(parent, dist)
+        cu, cv, cw = u, v, w
+        for b, (k, timing) in enumerate([(10, 1), (3000, 1), (40, 0), (20000, 0), (500, 1)]):
+            if b == 2:
+                for g in (ga, gb):
+                    o = g.get_opts()
+                    o.timing = timing
+                    g.set_opts(o)
+            ch = D.gen_changes(n, cu, cv, cw, k // 2, k - k // 2, seed=300 + b)
+            sa = ga.apply_batch(ch)
+            sb = gb.apply_batch(ch)
+            assert sa.graph_launch == 1 and sb.graph_launch == 0
+            pa, da = ga.tree_read()
+            pb, db = gb.tree_read()
+            assert np.array_equal(da, db), f"batch {b}"
+            check_against_oracle(n, cu, cv, cw, ch, 0, pa, da, f"graph replay batch {b}")
+            gr, kept = O.updated_graph(n, cu, cv, cw, ch, return_kept=True)
+            ins = ch[ch["op"] == 1]
+            lu, lv, lw = (np.concatenate([a, ins[f]]) for a, f in ((cu, "u"), (cv, "v"), (cw, "w")))
+            keep = kept[: len(lu)].astype(bool)
+            cu, cv, cw = lu[keep].astype(np.int32), lv[keep].astype(np.int32), lw[keep].astype(np.int32)
