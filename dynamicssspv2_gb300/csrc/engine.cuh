@@ -68,6 +68,8 @@ enum StatIdx {
     ST_ADVANCES,
     ST_TOMBS,
     ST_LIVE_INS,
+    ST_SEED_UPD,    // k_append: distance-lowering seed relaxations
+    ST_SEED_FRONT,  // k_append: ends claimed for the first frontier (or the far list)
     ST_COUNT
 };
 

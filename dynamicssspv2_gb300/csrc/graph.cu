@@ -784,11 +784,14 @@ void fill_stats(const dsssp_graph* g, const Ctl& c, dsssp_stats* st, bool events
     st->inv_levels = (int64_t)c.stat[ST_LEVELS];
     st->pj_passes = (int64_t)c.stat[ST_PJ];
     st->rounds = (int64_t)c.stat[ST_ROUNDS];
-    st->frontier_total = (int64_t)c.stat[ST_FRONTIER];
-    st->edges_relaxed = (int64_t)c.stat[ST_EDGES_RELAX];
+    // totals of the batch; the seeds' share (k_append) is kept apart for the byte model
+    const double live_ins = (double)c.stat[ST_LIVE_INS], seed_upd = (double)c.stat[ST_SEED_UPD],
+                 seed_front = (double)c.stat[ST_SEED_FRONT];
+    st->frontier_total = (int64_t)(c.stat[ST_FRONTIER] + c.stat[ST_SEED_FRONT]);
+    st->edges_relaxed = (int64_t)(c.stat[ST_EDGES_RELAX] + 2 * c.stat[ST_LIVE_INS]);
     st->edges_inval = (int64_t)c.stat[ST_EDGES_INV];
     st->del_probed = (int64_t)c.stat[ST_DEL_PROBED];
-    st->updates = (int64_t)c.stat[ST_UPDATES];
+    st->updates = (int64_t)(c.stat[ST_UPDATES] + c.stat[ST_SEED_UPD]);
     st->overflow_entries = (int64_t)c.stat[ST_OVF];
     st->repacks = repacks;
     if (c.ts[1] > c.ts[0]) st->t_inval_ms = (double)(c.ts[1] - c.ts[0]) * 1e-6;
@@ -806,20 +809,22 @@ void fill_stats(const dsssp_graph* g, const Ctl& c, dsssp_stats* st, bool events
     st->tombstoned = (int64_t)c.stat[ST_TOMBS];
     st->graph_launch = g->pend_graph ? 1 : 0;
     // algorithmic bytes (byte model: each item is touched once by this algorithm)
-    //   per adjacency entry scanned 16 (entry + neighbour state), per work item 40 (item write
-    //   + read, row descriptor, owner state), per pushed vertex 20 (push tag, degree), per
-    //   distance-lowering atomic 8, per cut-off vertex 12 (state, tag), per insertion seed 24,
-    //   per pointer-jumping pass 12 n
+    //   update kernel: per adjacency entry scanned 16 (entry + neighbour state), per work item
+    //   40 (item write + read, row descriptor, owner state), per pushed vertex 20 (push tag,
+    //   degree), per distance-lowering atomic 8, per cut-off vertex 12 (state, tag), per seed
+    //   expanded 8 (list entry, degree), per pointer-jumping pass 12 n
     const double n = (double)g->n;
-    double upd = 16.0 * (double)(st->edges_relaxed + st->edges_inval) + 40.0 * (double)st->work_items +
-                 20.0 * (double)st->frontier_total + 8.0 * (double)st->updates + 12.0 * (double)st->n_invalidated +
-                 24.0 * (double)st->n_ins;
+    double upd = 16.0 * (double)(c.stat[ST_EDGES_RELAX] + c.stat[ST_EDGES_INV]) + 40.0 * (double)st->work_items +
+                 20.0 * (double)c.stat[ST_FRONTIER] + 8.0 * (double)c.stat[ST_UPDATES] +
+                 12.0 * (double)st->n_invalidated + 8.0 * (double)c.seed_count;
     if (st->pj_passes > 0) upd += n * (12.0 + 12.0 * (double)st->pj_passes);
     //   front kernels: 16 per record (read by each of the three), 48 per insertion (two
     //   descriptor atomics + two entries + hash probe), 56 per deletion (two descriptors, two
-    //   prefix lengths, two states, hash slot) + 8 per probed entry + 16 per root
+    //   prefix lengths, two states, hash slot) + 8 per probed entry + 16 per root; per
+    //   surviving insertion 16 (both end states), per seed relaxation 8, per claimed end 8
     const double front = 48.0 * (double)k + 48.0 * (double)st->n_ins + 56.0 * (double)st->n_del +
-                         8.0 * (double)st->del_probed + 16.0 * (double)st->n_roots;
+                         8.0 * (double)st->del_probed + 16.0 * (double)st->n_roots + 16.0 * live_ins +
+                         8.0 * seed_upd + 8.0 * seed_front;
     st->bytes_alg_update = upd;
     st->bytes_alg = upd + front;
 }

@@ -554,37 +554,62 @@ __device__ void block_add(unsigned long long* dst, unsigned long long x) {
     if (threadIdx.x == 0 && s_sum) atomicAdd(dst, s_sum);
 }
 
-// CTA-level staging of appends to a plain u32 list: entries gather in shared memory and go
-// out with one atomic on the list counter per CTA flush.  stage_flush is CTA-collective; it
-// writes when `all` is set or when fewer than `room` free entries are left.
-struct Stage {
-    unsigned* buf;  // shared memory, cap entries
-    unsigned cap;
-    unsigned* n;    // shared counter
+// Per-warp staging of appends to a plain u32 list.  A warp writes its region of shared memory
+// and appends it to the list with one atomic when the region is nearly full; at the end the
+// CTA appends what its warps still hold with one atomic (flush_cta).  The list counters are
+// single words that every CTA hits, so their atomics are kept few, and no CTA-wide barrier
+// is needed while the warps work.
+struct WarpList {
+    unsigned* buf;  // this warp's region of shared memory
+    int cap;        // entries in the region
+    int count;      // warp-uniform
 
-    __device__ __forceinline__ void add(bool pred, unsigned v) const {
-        if (pred) buf[atomicAdd(n, 1u)] = v;
+    __device__ __forceinline__ void add(bool pred, unsigned v) {
+        const unsigned mask = __ballot_sync(kFull, pred);
+        if (pred) buf[count + __popc(mask & ((1u << lane_id()) - 1u))] = v;
+        count += __popc(mask);
+        __syncwarp();
+    }
+
+    // warp-collective: appends the region once fewer than `room` entries are free
+    __device__ __forceinline__ void flush(unsigned* list, unsigned* counter, unsigned list_cap, int room, Ctl* ctl) {
+        if (count + room <= cap) return;
+        unsigned b = 0;
+        if (lane_id() == 0) b = atomicAdd(counter, (unsigned)count);
+        b = __shfl_sync(kFull, b, 0);
+        if ((unsigned long long)b + (unsigned)count > list_cap) {
+            if (lane_id() == 0) set_status(ctl, -4 /* list capacity: internal error */);
+        } else {
+            for (int j = (int)lane_id(); j < count; j += 32) list[b + j] = buf[j];
+        }
+        count = 0;
+        __syncwarp();
+    }
+
+    // CTA-collective (every thread of the CTA)
+    __device__ void flush_cta(unsigned* list, unsigned* counter, unsigned list_cap, Ctl* ctl) {
+        __shared__ unsigned s_off[kMaxWarps], s_base, s_ok;
+        const unsigned w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        if (lane_id() == 0) s_off[w] = (unsigned)count;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned t = 0;
+            for (unsigned k = 0; k < nw; k++) {
+                const unsigned c = s_off[k];
+                s_off[k] = t;
+                t += c;
+            }
+            s_base = t ? atomicAdd(counter, t) : 0u;
+            s_ok = (unsigned long long)s_base + t <= list_cap;
+            if (!s_ok) set_status(ctl, -4 /* list capacity: internal error */);
+        }
+        __syncthreads();
+        if (s_ok)
+            for (int j = (int)lane_id(); j < count; j += 32) list[s_base + s_off[w] + j] = buf[j];
+        count = 0;
+        __syncthreads();
     }
 };
-
-__device__ void stage_flush(const Stage& st, unsigned* list, unsigned* counter, unsigned list_cap, bool all,
-                            unsigned room, Ctl* ctl) {
-    __shared__ unsigned s_base;
-    __syncthreads();
-    const unsigned cnt = *st.n;
-    if (cnt == 0 || (!all && cnt + room <= st.cap)) return;  // same for every thread
-    if (threadIdx.x == 0) s_base = atomicAdd(counter, cnt);
-    __syncthreads();
-    const unsigned b = s_base;
-    if ((unsigned long long)b + cnt > list_cap) {
-        if (threadIdx.x == 0) set_status(ctl, -4 /* list capacity: internal error */);
-    } else {
-        for (unsigned j = threadIdx.x; j < cnt; j += blockDim.x) list[b + j] = st.buf[j];
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) *st.n = 0;
-    __syncthreads();
-}
 
 // ---- row search and the deletion set -------------------------------------------------------
 
@@ -687,13 +712,11 @@ __global__ void k_delete(UpdParams p) {
     if (__ldcg(&ctl->status) != 0) return;  // set by k_prepare: same for every thread
     const long long nthreads = (long long)gridDim.x * blockDim.x;
     unsigned long long probed = 0, roots = 0, dead = 0;
-    __shared__ unsigned s_nroots;
-    if (threadIdx.x == 0) s_nroots = 0;
-    __syncthreads();
-    const Stage roots_stage{reinterpret_cast<unsigned*>(&s_pbuf[0][0]), 2u * kMaxWarps * kBuf, &s_nroots};
-    // the loop is uniform over the CTA (the root staging flushes are CTA-collective)
-    for (long long cbase = (long long)blockIdx.x * blockDim.x; cbase < p.k; cbase += nthreads) {
-        const long long i = cbase + threadIdx.x;
+    const unsigned lane = lane_id();
+    constexpr int kRegion = 2 * kBuf;  // u32 entries of a warp's push-buffer storage
+    WarpList roots_list{reinterpret_cast<unsigned*>(s_pbuf[threadIdx.x >> 5]), kRegion, 0};
+    for (long long base = (long long)blockIdx.x * blockDim.x + threadIdx.x - lane; base < p.k; base += nthreads) {
+        const long long i = base + lane;
         const int4 c = i < p.k ? p.chg[i] : make_int4(0, 0, 0, -1);
         bool cut = false;
         unsigned cutv = 0;
@@ -723,11 +746,11 @@ __global__ void k_delete(UpdParams p) {
             }
             if (c.z >= 0 && !hash_insert(p, dpair_key(a, b), c.z)) set_status(ctl, -4 /* deletion set full */);
         }
-        roots_stage.add(cut, cutv);
+        roots_list.add(cut, cutv);
         roots += cut ? 1 : 0;
-        stage_flush(roots_stage, p.g.invq, &ctl->inv_count, (unsigned)p.g.n, false, blockDim.x, ctl);
+        roots_list.flush(p.g.invq, &ctl->inv_count, (unsigned)p.g.n, 32, ctl);
     }
-    stage_flush(roots_stage, p.g.invq, &ctl->inv_count, (unsigned)p.g.n, true, 0, ctl);
+    roots_list.flush_cta(p.g.invq, &ctl->inv_count, (unsigned)p.g.n, ctl);
     block_add(&ctl->stat[ST_ROOTS], roots);
     block_add(&ctl->stat[ST_DEL_PROBED], probed);
     block_add(&ctl->stat[ST_TOMBS], dead);
@@ -754,19 +777,14 @@ __global__ void k_append(UpdParams p) {
     // near-far: a batch starts with threshold 0, so every seed waits in the far list
     const bool nf = p.delta != 0 && g.far0 != nullptr && g.far1 != nullptr && g.far_tag != nullptr;
     const unsigned long long T = nf ? 0ull : ~0ull;
-    // seeds are staged per CTA (half of the push-buffer storage each for near and far)
-    __shared__ unsigned s_nn, s_nf;
-    if (threadIdx.x == 0) s_nn = s_nf = 0;
-    __syncthreads();
-    unsigned* stage_mem = reinterpret_cast<unsigned*>(&s_pbuf[0][0]);
-    const Stage near_stage{stage_mem, kMaxWarps * kBuf, &s_nn};
-    const Stage far_stage{stage_mem + kMaxWarps * kBuf, kMaxWarps * kBuf, &s_nf};
+    // seeds are staged per warp (half of the warp's push-buffer storage each for near and far)
+    unsigned* region = reinterpret_cast<unsigned*>(s_pbuf[threadIdx.x >> 5]);
+    WarpList near_list{region, kBuf, 0}, far_list{region + kBuf, kBuf, 0};
     const unsigned seed_cap = (unsigned)min(2 * p.k, (long long)g.n);  // distinct claimed ends
     LocalStats ls;
     unsigned long long killed = 0, ovf = 0, live_ins = 0;
-    // the loop is uniform over the CTA (the staging flushes are CTA-collective)
-    for (long long cbase = (long long)blockIdx.x * blockDim.x; cbase < p.k; cbase += nthreads) {
-        const long long i = cbase + threadIdx.x;
+    for (long long base = (long long)blockIdx.x * blockDim.x + threadIdx.x - lane; base < p.k; base += nthreads) {
+        const long long i = base + lane;
         const int4 c = i < p.k ? p.chg[i] : make_int4(0, 0, 0, -1);
         int alive = 0;
         unsigned long long sa = kInfState, sb = kInfState;
@@ -817,17 +835,19 @@ __global__ void k_append(UpdParams p) {
         const bool fa = la && atomicExch(&g.far_tag[c.x], rbase) != rbase;
         const bool db = pbv && !lb && atomicExch(&g.push_tag[c.y], tag0) != tag0;
         const bool da = pa && !la && atomicExch(&g.push_tag[c.x], tag0) != tag0;
-        ls.frontier += (db ? 1 : 0) + (da ? 1 : 0);
-        near_stage.add(db, (unsigned)c.y);  // claimed: one entry per vertex
-        near_stage.add(da, (unsigned)c.x);
-        far_stage.add(fb, (unsigned)c.y);  // far-tagged: one entry per vertex
-        far_stage.add(fa, (unsigned)c.x);
-        stage_flush(near_stage, p.seedq, &ctl->seed_count, seed_cap, false, 2 * blockDim.x, ctl);
-        stage_flush(far_stage, g.far0, &ctl->fc[0], (unsigned)g.n, false, 2 * blockDim.x, ctl);
+        ls.frontier += (db ? 1 : 0) + (da ? 1 : 0) + (fb ? 1 : 0) + (fa ? 1 : 0);
+        near_list.add(db, (unsigned)c.y);  // claimed: one entry per vertex
+        near_list.add(da, (unsigned)c.x);
+        far_list.add(fb, (unsigned)c.y);  // far-tagged: one entry per vertex
+        far_list.add(fa, (unsigned)c.x);
+        near_list.flush(p.seedq, &ctl->seed_count, seed_cap, 64, ctl);
+        far_list.flush(g.far0, &ctl->fc[0], (unsigned)g.n, 64, ctl);
     }
-    stage_flush(near_stage, p.seedq, &ctl->seed_count, seed_cap, true, 0, ctl);
-    stage_flush(far_stage, g.far0, &ctl->fc[0], (unsigned)g.n, true, 0, ctl);
-    flush_stats(ctl, ls);
+    near_list.flush_cta(p.seedq, &ctl->seed_count, seed_cap, ctl);
+    far_list.flush_cta(g.far0, &ctl->fc[0], (unsigned)g.n, ctl);
+    block_add(&ctl->stat[ST_SEED_UPD], ls.updates);  // kept apart from k_update's counters
+    block_add(&ctl->stat[ST_SEED_FRONT], ls.frontier);
+    block_add(&ctl->stat[ST_DIST_OVF], ls.dist_ovf);
     block_add(&ctl->stat[ST_OVF], ovf);
     block_add(&ctl->stat[ST_LIVE_INS], live_ins);
     unsigned long long kk = warp_sum_u64(killed);
