@@ -103,7 +103,9 @@ struct __align__(128) Ctl {
     unsigned pad4[19];
     // line 4b: near-far threshold reduction (double buffer)
     unsigned long long fmin[2];
-    unsigned long long pad4b[14];
+    // small steps run by CTA 0 alone hand their end state to the grid here
+    unsigned long long solo[4];
+    unsigned long long pad4b[10];
     // line 5: barrier diagnostics (first timed-out barrier, arrivals then, CTAs that timed
     // out, max barrier count at exit, 0xFFFFFFFF - min barrier count at exit)
     unsigned diag[8];

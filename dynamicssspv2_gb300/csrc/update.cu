@@ -48,6 +48,9 @@ constexpr int kMaxWarps = 8;               // update kernel blocks have at most 
 constexpr int kBuf = 256;                  // per-warp push buffer (vertex, degree) entries
 constexpr int kAddsPerCheck = 128;         // entries a warp may add between two flush checks
                                            // (visit4: 4 adds of up to 32 lanes)
+constexpr unsigned kSoloWaves = 2;         // a step of at most this many CTA-waves of items
+                                           // runs on CTA 0 alone (block barriers)
+constexpr int kSoloSteps = 256;            // consecutive solo steps before the grid re-syncs
 
 __shared__ unsigned s_nbar;  // grid barriers this CTA has passed
 __shared__ uint2 s_pbuf[kMaxWarps][kBuf];  // (vertex, degree) pushed, not yet expanded
@@ -82,7 +85,7 @@ __device__ bool grid_sync(Ctl* ctl) {
                     atomicAdd(&ctl->diag[2], 1u);
                     break;
                 }
-                __nanosleep(spins < 32 ? 32 : 200);
+                __nanosleep(spins < 32 ? 32 : (spins < 2048 ? 200 : 1000));  // long waits: solo steps
             }
         }
         __threadfence();
@@ -456,15 +459,24 @@ struct PullOp {
     }
 };
 
+// A step of nt thread items and nc CTA items is small when CTA 0 alone finishes it in a few
+// waves: then it skips the grid barrier, whose cost (~2.5 us plus the wait for the slowest
+// CTA) exceeds the work.
+__device__ __forceinline__ bool small_step(unsigned nt, unsigned nc) {
+    return (nt + blockDim.x - 1) / blockDim.x + nc <= kSoloWaves;
+}
+
 // Processes one step's work: CTA items (one CTA per chunk of a long row), then thread
-// items (te edges each) in one grid-stride wave.
+// items (te edges each) in one grid-stride wave, over CTAs cta, cta + 1, ... of ncta (the
+// whole grid, or CTA 0 alone for a small step).
 template <class Op>
-__device__ void run_items(Op& op, const UpdParams& p, const uint2* tl, unsigned nt, const uint2* cl, unsigned nc) {
+__device__ void run_items(Op& op, const UpdParams& p, const uint2* tl, unsigned nt, const uint2* cl, unsigned nc,
+                          unsigned cta, unsigned ncta) {
     const RowDesc* rows = p.g.rows;
     const unsigned lane = lane_id();
-    const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned nthreads = gridDim.x * blockDim.x;
-    for (unsigned t = blockIdx.x; t < nc; t += gridDim.x) {
+    const unsigned gtid = cta * blockDim.x + threadIdx.x;
+    const unsigned nthreads = ncta * blockDim.x;
+    for (unsigned t = cta; t < nc; t += ncta) {
         const uint2 it = __ldcg(&cl[t]);
         const RowDesc rd = rows[it.x];
         const unsigned long long du = __shfl_sync(kFull, op.prep(it.x), 0);
@@ -944,6 +956,44 @@ __device__ void update_body(UpdParams& p) {
                 need_pj = true;
                 break;
             }
+            if (small_step(hiT - loT, hiC - loC)) {
+                // small levels: CTA 0 walks on alone while they stay small; the others wait
+                if (blockIdx.x == 0) {
+                    for (int steps = 0; steps < kSoloSteps; steps++) {
+                        if ((loT >= hiT && loC >= hiC) || level >= p.bfs_levels || !small_step(hiT - loT, hiC - loC))
+                            break;
+                        if (threadIdx.x == 0) {
+                            ctl->ltT[(level + 2) % 3] = 0;
+                            ctl->ltC[(level + 2) % 3] = 0;
+                        }
+                        MarkOp op{&p,
+                                  Out{g.it + hiT, &ctl->ltT[(level + 1) % 3], g.tcap - hiT, g.ic + hiC,
+                                      &ctl->ltC[(level + 1) % 3], g.ccap - hiC},
+                                  PushBuf{pbuf, 0}, &ls};
+                        run_items(op, p, g.it + loT, hiT - loT, g.ic + loC, hiC - loC, 0, 1);
+                        __syncthreads();
+                        loT = hiT;
+                        loC = hiC;
+                        hiT += __ldcg(&ctl->ltT[(level + 1) % 3]);
+                        hiC += __ldcg(&ctl->ltC[(level + 1) % 3]);
+                        level++;
+                        __syncthreads();  // every thread has read the counters before the next reset
+                    }
+                    if (threadIdx.x == 0) {
+                        ctl->solo[0] = ((unsigned long long)hiT << 32) | loT;
+                        ctl->solo[1] = ((unsigned long long)hiC << 32) | loC;
+                        ctl->solo[2] = (unsigned long long)level;
+                    }
+                }
+                if (!grid_sync(ctl)) return;
+                const unsigned long long a = __ldcg(&ctl->solo[0]), b = __ldcg(&ctl->solo[1]);
+                loT = (unsigned)a;
+                hiT = (unsigned)(a >> 32);
+                loC = (unsigned)b;
+                hiC = (unsigned)(b >> 32);
+                level = (int)__ldcg(&ctl->solo[2]);
+                continue;
+            }
             if (leader) {
                 ctl->ltT[(level + 2) % 3] = 0;
                 ctl->ltC[(level + 2) % 3] = 0;
@@ -952,7 +1002,7 @@ __device__ void update_body(UpdParams& p) {
                       Out{g.it + hiT, &ctl->ltT[(level + 1) % 3], g.tcap - hiT, g.ic + hiC, &ctl->ltC[(level + 1) % 3],
                           g.ccap - hiC},
                       PushBuf{pbuf, 0}, &ls};
-            run_items(op, p, g.it + loT, hiT - loT, g.ic + loC, hiC - loC);
+            run_items(op, p, g.it + loT, hiT - loT, g.ic + loC, hiC - loC, blockIdx.x, gridDim.x);
             if (!grid_sync(ctl)) return;
             loT = hiT;
             loC = hiC;
@@ -1037,7 +1087,7 @@ __device__ void update_body(UpdParams& p) {
         }
         {
             PullOp op{&p, tag0, relax0, PushBuf{pbuf, 0}, &ls, far_of(cf, fgen, T), kInfState, false};
-            run_items(op, p, g.it, hiT, g.ic, hiC);
+            run_items(op, p, g.it, hiT, g.ic, hiC, blockIdx.x, gridDim.x);
         }
         if (!grid_sync(ctl)) return;
     }
@@ -1097,6 +1147,36 @@ __device__ void update_body(UpdParams& p) {
             if (leader) set_status(ctl, -5 /* NO_CONVERGENCE */);
             break;
         }
+        if (small_step(nT, nC)) {
+            // small rounds: CTA 0 relaxes on alone while they stay small; the others wait.  An
+            // empty frontier goes back to the grid (near-far advance or the end).
+            if (blockIdx.x == 0) {
+                long long rr = r;
+                unsigned t = nT, c = nC;
+                for (int steps = 0; steps < kSoloSteps; steps++) {
+                    if ((t == 0 && c == 0) || !small_step(t, c) || rr >= p.max_rounds) break;
+                    if (threadIdx.x == 0) {
+                        ctl->rcT[(rr + 2) % 3] = 0;
+                        ctl->rcC[(rr + 2) % 3] = 0;
+                    }
+                    const bool odd = (rr & 1) != 0;
+                    RelaxOp op{&p, rbase + (unsigned)rr + 2u,
+                               Out{odd ? g.rt0 : g.rt1, &ctl->rcT[(rr + 1) % 3], g.tcap, odd ? g.rc0 : g.rc1,
+                                   &ctl->rcC[(rr + 1) % 3], g.ccap},
+                               PushBuf{pbuf, 0}, &ls, far_of(cf, fgen, T)};
+                    run_items(op, p, odd ? g.rt1 : g.rt0, t, odd ? g.rc1 : g.rc0, c, 0, 1);
+                    __syncthreads();
+                    rr++;
+                    t = __ldcg(&ctl->rcT[rr % 3]);
+                    c = __ldcg(&ctl->rcC[rr % 3]);
+                    __syncthreads();  // every thread has read the counters before the next reset
+                }
+                if (threadIdx.x == 0) ctl->solo[3] = (unsigned long long)rr;
+            }
+            if (!grid_sync(ctl)) break;
+            r = (long long)__ldcg(&ctl->solo[3]) - 1;  // the loop steps to the first round left
+            continue;
+        }
         if (leader) {
             ctl->rcT[(r + 2) % 3] = 0;
             ctl->rcC[(r + 2) % 3] = 0;
@@ -1106,7 +1186,7 @@ __device__ void update_body(UpdParams& p) {
                    Out{odd ? g.rt0 : g.rt1, &ctl->rcT[(r + 1) % 3], g.tcap, odd ? g.rc0 : g.rc1,
                        &ctl->rcC[(r + 1) % 3], g.ccap},
                    PushBuf{pbuf, 0}, &ls, far_of(cf, fgen, T)};
-        run_items(op, p, odd ? g.rt1 : g.rt0, nT, odd ? g.rc1 : g.rc0, nC);
+        run_items(op, p, odd ? g.rt1 : g.rt0, nT, odd ? g.rc1 : g.rc0, nC, blockIdx.x, gridDim.x);
         if (!grid_sync(ctl)) break;
     }
     flush_stats(ctl, ls);
