@@ -306,6 +306,7 @@ def run_engine(args, dist: Dist) -> int:
     h_ch = torch.from_numpy(ch.view(np.uint8).copy()).pin_memory()
     h_par = torch.empty(n, dtype=torch.int32).pin_memory()
     h_dist = torch.empty(n, dtype=torch.int64).pin_memory()
+    h_vtx = torch.empty(n, dtype=torch.int32).pin_memory()
     import ctypes as C
 
     def reset():
@@ -323,6 +324,15 @@ def run_engine(args, dist: Dist) -> int:
         D._check(D._lib.dsssp_apply_batch(g.handle, h_ch.data_ptr(), batch, sptr, C.byref(st)), "apply_batch")
         D._check(D._lib.dsssp_tree_read(g.handle, h_par.data_ptr(), h_dist.data_ptr()), "tree_read")
         return time.perf_counter() - t0, st
+
+    def e2e_delta_step():  # the same batch, reading back only the entries it may have changed
+        t0 = time.perf_counter()
+        st = D.Stats()
+        cnt = C.c_int64()
+        D._check(D._lib.dsssp_apply_batch(g.handle, h_ch.data_ptr(), batch, sptr, C.byref(st)), "apply_batch")
+        D._check(D._lib.dsssp_tree_read_changed(g.handle, h_vtx.data_ptr(), h_par.data_ptr(), h_dist.data_ptr(), n,
+                                                C.byref(cnt)), "tree_read_changed")
+        return time.perf_counter() - t0, cnt.value
 
     clk = ClockSampler(dev).__enter__()
     if clk.proc:
@@ -349,13 +359,19 @@ def run_engine(args, dist: Dist) -> int:
 
     # end-to-end through the C ABI with host buffers (median over the steps: host-side
     # copies see more run-to-run noise than the device)
-    e2e_times = []
+    e2e_times, delta_times, delta_counts = [], [], []
     for _ in range(max(5, min(args.steps, 20))):
         reset()
         dt, _ = e2e_step()
         e2e_times.append(dt)
+    for _ in range(max(5, min(args.steps, 20))):
+        reset()
+        dt, cnt = e2e_delta_step()
+        delta_times.append(dt)
+        delta_counts.append(cnt)
     clk.__exit__(None, None, None)
     e2e_value, e2e_t = whole_job_rate(dist, batch, 1, statistics.median(e2e_times))
+    delta_value, delta_t = whole_job_rate(dist, batch, 1, statistics.median(delta_times))
 
     # roofline of the dominant kernel (the persistent update kernel)
     upd_ms = statistics.mean(s.t_update_ms for s in stats)
@@ -396,7 +412,14 @@ def run_engine(args, dist: Dist) -> int:
         "config": cfg,
         "e2e": {"value": e2e_value, "unit": "change-edges/s", "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": n * (4 + 8) + 320, "ms_per_step": 1e3 * e2e_t,
-                "ms_all_steps": [round(1e3 * t, 4) for t in e2e_times], "timed": "host clock per step, median"},
+                "ms_all_steps": [round(1e3 * t, 4) for t in e2e_times], "timed": "host clock per step, median",
+                "result": "the whole updated tree (dsssp_tree_read: parent int32 + dist int64 per vertex)"},
+        "e2e_changed": {"value": delta_value, "unit": "change-edges/s", "h2d_bytes_per_step": nbytes,
+                        "d2h_bytes_per_step": int(statistics.median(delta_counts)) * (4 + 4 + 8) + 8 + 320,
+                        "ms_per_step": 1e3 * delta_t, "changed_vertices": int(statistics.median(delta_counts)),
+                        "timed": "host clock per step, median",
+                        "result": "the entries the batch may have changed (dsssp_tree_read_changed: vertex, "
+                                  "parent, dist), which rebuild the updated tree from the previous one"},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": profiled_traffic(args.workload),

@@ -104,6 +104,7 @@ _sig("dsssp_tree_compute", C.c_int, _P, C.c_int32, C.POINTER(Stats))
 _sig("dsssp_tree_compute_multi", C.c_int, _P, _i32p, C.c_int32, C.POINTER(Stats))
 _sig("dsssp_forest_load", C.c_int, _P, _i32p, _i64p)
 _sig("dsssp_tree_read", C.c_int, _P, _P, _P)
+_sig("dsssp_tree_read_changed", C.c_int, _P, _P, _P, _P, C.c_int64, C.POINTER(C.c_int64))
 _sig("dsssp_apply_batch", C.c_int, _P, _P, C.c_int64, _P, C.POINTER(Stats))
 _sig("dsssp_apply_batch_async", C.c_int, _P, _P, C.c_int64, _P)
 _sig("dsssp_batch_finish", C.c_int, _P, C.POINTER(Stats))
@@ -153,7 +154,7 @@ EXPORTED = [
     "dsssp_read_changes_file", "dsssp_read_sssp_file", "dsssp_write_sssp_file", "dsssp_gen_er", "dsssp_gen_rmat",
     "dsssp_gen_grid", "dsssp_gen_changes", "dsssp_max_degree_vertex", "dsssp_sssp_noalloc",
     "dsssp_gen_changes_ref", "dsssp_write_changes_file", "dsssp_write_graph_binary", "dsssp_read_graph_binary",
-    "dsssp_write_sssp_binary", "dsssp_read_sssp_binary", "dsssp_graph_health",
+    "dsssp_write_sssp_binary", "dsssp_read_sssp_binary", "dsssp_graph_health", "dsssp_tree_read_changed",
 ]
 
 
@@ -277,6 +278,20 @@ class Graph:
             dist = np.empty(self.n, np.int64)
         _check(_lib.dsssp_tree_read(self._h, parent.ctypes.data, dist.ctypes.data), "tree_read")
         return parent, dist
+
+    def tree_read_changed(self, vertex: np.ndarray | None = None, parent: np.ndarray | None = None,
+                          dist: np.ndarray | None = None):
+        """(vertex, parent, dist) of every vertex the last batch may have changed (unordered);
+        buffers of n entries may be passed in (pinned ones for fast copies)."""
+        vertex = np.empty(self.n, np.int32) if vertex is None else vertex
+        parent = np.empty(self.n, np.int32) if parent is None else parent
+        dist = np.empty(self.n, np.int64) if dist is None else dist
+        cnt = C.c_int64()
+        _check(_lib.dsssp_tree_read_changed(self._h, vertex.ctypes.data, parent.ctypes.data, dist.ctypes.data,
+                                            min(len(vertex), len(parent), len(dist)), C.byref(cnt)),
+               "tree_read_changed")
+        k = cnt.value
+        return vertex[:k], parent[:k], dist[:k]
 
     def apply_batch(self, changes: np.ndarray, stream: int | None = None) -> Stats:
         changes = np.ascontiguousarray(changes, CHANGE_DTYPE)

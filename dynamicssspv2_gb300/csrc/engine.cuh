@@ -136,6 +136,7 @@ struct DevGraph {
     unsigned* far0;     // near-far: vertices whose distance is at or above the threshold
     unsigned* far1;
     unsigned* far_tag;  // far-list membership tag (de-duplication)
+    unsigned* chg_tag;  // batch epoch of an equal-distance parent swap (changed-vertex set)
     long long tcap;
     long long ccap;
     long long cap_total;  // adjacency slots (bounds of twin-derived indices)

@@ -348,6 +348,39 @@ __global__ void k_tree_unpack(const unsigned long long* state, int n, int* paren
     }
 }
 
+// Vertices the last batch may have changed: cut off in this epoch, or holding a push tag or
+// far-list generation of the batch's tag range [lo, hi).  CTA-aggregated append.
+__global__ void k_tree_changed(const unsigned long long* state, const unsigned* inv_tag, const unsigned* chg_tag,
+                               const unsigned* push_tag, const unsigned* far_tag, int n, unsigned epoch, unsigned lo,
+                               unsigned hi, int* vertex, int* parent, long long* dist, unsigned* count) {
+    __shared__ unsigned s_n, s_base;
+    __shared__ int s_v[kThreads];
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    bool ch = false;
+    if (v < n) {
+        const unsigned pt = push_tag[v];
+        ch = inv_tag[v] == epoch || chg_tag[v] == epoch || (pt >= lo && pt < hi);
+        if (!ch && far_tag) {
+            const unsigned ft = far_tag[v];
+            ch = ft >= lo && ft < hi;
+        }
+    }
+    if (ch) s_v[atomicAdd(&s_n, 1u)] = v;
+    __syncthreads();
+    if (threadIdx.x == 0 && s_n) s_base = atomicAdd(count, s_n);
+    __syncthreads();
+    if (threadIdx.x < s_n) {
+        const int x = s_v[threadIdx.x];
+        const unsigned long long s = state[x];
+        const unsigned i = s_base + threadIdx.x;
+        vertex[i] = x;
+        parent[i] = s == kInfState ? -1 : (int)(unsigned)s;
+        dist[i] = s == kInfState ? (long long)DSSSP_UNREACHABLE : (long long)(s >> 32);
+    }
+}
+
 __global__ void k_state_reset(unsigned long long* state, int n) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v < n) state[v] = kInfState;
@@ -450,6 +483,13 @@ struct dsssp_graph {
     cudaStream_t pend_stream = nullptr;
     bool pend_events = false;
     bool pend_graph = false;
+    // tag range of the last successful batch (tree_read_changed); delta_ok false after a
+    // tree load or computation, a failed batch or a tag reset
+    unsigned delta_lo = 0, delta_hi = 0, delta_epoch = 0;
+    bool delta_ok = false;
+    unsigned pend_rb0 = 0;
+    int* d_vtx = nullptr;
+    unsigned* d_count = nullptr;
     // tree staging
     int* d_par = nullptr;
     long long* d_dist = nullptr;
@@ -743,6 +783,7 @@ int clear_ctl(dsssp_graph* g, cudaStream_t s) {
 int next_epoch(dsssp_graph* g, cudaStream_t s) {
     if (g->epoch >= 0xFFFFFFF0u) {
         CK(cudaMemsetAsync(g->dg.inv_tag, 0, sizeof(unsigned) * (size_t)g->n, s), "tag reset");
+        CK(cudaMemsetAsync(g->dg.chg_tag, 0, sizeof(unsigned) * (size_t)g->n, s), "tag reset");
         g->epoch = 0;
     }
     g->epoch++;
@@ -1022,6 +1063,7 @@ int enqueue_batch(dsssp_graph* g, const int4* d_chg, long long k, cudaStream_t s
     while (h < hb) h <<= 1;  // this batch uses the first h slots of the deletion set
     UpdParams p = make_params(g, d_chg, k, 0);
     p.hmask = h - 1;
+    g->pend_rb0 = g->h_ctl->round_base;  // the device reads the same value (mirror)
     g->pend_graph = launch_batch_graph(g, p, h, s);
     if (g->pend_graph) return DSSSP_OK;
     const bool ev = g->o.timing != 0;
@@ -1071,6 +1113,10 @@ int finish_batch(dsssp_graph* g, dsssp_stats* st) {
         g->entries += 2 * (long long)g->h_ctl->stat[ST_LIVE_INS] - tombs;
         g->dead += tombs;
     }
+    g->delta_ok = g->h_ctl->status == 0 && g->h_ctl->stat[ST_DIST_OVF] == 0;
+    g->delta_lo = g->pend_rb0;
+    g->delta_hi = g->h_ctl->round_base;
+    g->delta_epoch = g->epoch;
     if (g->h_ctl->status != 0) reset_tags(g, s);
     if (g->h_ctl->stat[ST_DIST_OVF] > 0 && g->h_ctl->status == 0) return status_code(DSSSP_E_OVERFLOW);
     if (g->h_ctl->status == DSSSP_E_TIMEOUT) {
@@ -1152,9 +1198,9 @@ void dsssp_graph_destroy(dsssp_graph* g) {
     DevGraph& d = g->dg;
     dfree(d.state); dfree(d.rows); dfree(d.sorted_len); dfree(d.adj); dfree(d.inv_tag);
     dfree(d.push_tag); dfree(d.jm); dfree(d.invq); dfree(d.rt0); dfree(d.rt1); dfree(d.rc0); dfree(d.rc1);
-    dfree(d.it); dfree(d.ic); dfree(d.ctl); dfree(d.far0); dfree(d.far1); dfree(d.far_tag);
+    dfree(d.it); dfree(d.ic); dfree(d.ctl); dfree(d.far0); dfree(d.far1); dfree(d.far_tag); dfree(d.chg_tag);
     dfree(g->d_chg); dfree(g->d_ins_state); dfree(g->d_ovf); dfree(g->d_hset); dfree(d.twin); dfree(g->s_twin);
-    dfree(g->d_par); dfree(g->d_dist); dfree(g->d_srcs); dfree(g->d_slot); dfree(g->d_seedq); dfree(g->d_spare);
+    dfree(g->d_par); dfree(g->d_dist); dfree(g->d_vtx); dfree(g->d_count); dfree(g->d_srcs); dfree(g->d_slot); dfree(g->d_seedq); dfree(g->d_spare);
     dfree(g->d_need); dfree(g->d_gidx); dfree(g->d_grow_list); dfree(g->d_grow_count); dfree(g->d_old_start);
     dfree(g->d_old_cap); dfree(g->d_fail);
     dfree(g->s_state); dfree(g->s_rows); dfree(g->s_sorted); dfree(g->s_adj);
@@ -1226,6 +1272,7 @@ int dsssp_graph_create(int32_t n, int64_t m, const int32_t* u, const int32_t* v,
     if (!rc) rc = dalloc(&d.push_tag, N, "push_tag");
     if (!rc) rc = dalloc(&d.jm, N, "jm");
     if (!rc) rc = dalloc(&d.invq, N, "invq");
+    if (!rc) rc = dalloc(&d.chg_tag, N, "change tags");
     if (!rc) rc = dalloc(&d.ctl, 1, "control block");
     if (!rc) rc = dalloc(&g->d_spare, 2, "spare region words");
     if (!rc) rc = dalloc(&g->d_grow_count, 1, "row growth");
@@ -1234,6 +1281,7 @@ int dsssp_graph_create(int32_t n, int64_t m, const int32_t* u, const int32_t* v,
     cudaStream_t s = g->stream;
     cudaMemsetAsync(d.state, 0xFF, sizeof(unsigned long long) * N, s);
     cudaMemsetAsync(d.inv_tag, 0, sizeof(unsigned) * N, s);
+    cudaMemsetAsync(d.chg_tag, 0, sizeof(unsigned) * N, s);
     cudaMemsetAsync(d.push_tag, 0, sizeof(unsigned) * N, s);
     cudaMemsetAsync(d.ctl, 0, sizeof(Ctl), s);
     Ctl init{};
@@ -1349,6 +1397,7 @@ static int tree_load_impl(dsssp_graph* g, const int32_t* parent, const int64_t* 
     }
     g->src = (int)g->h_ctl->stat[1];
     g->has_tree = true;
+    g->delta_ok = false;
     return DSSSP_OK;
 }
 
@@ -1398,6 +1447,7 @@ int dsssp_tree_compute_multi(dsssp_graph* g, const int32_t* srcs, int32_t k, dss
     CK(cudaStreamSynchronize(s), "tree compute");
     g->src = uniq[0];
     g->has_tree = g->h_ctl->status == 0;
+    g->delta_ok = false;
     g->pend_graph = false;
     fill_stats(g, *g->h_ctl, st, ev, 0, 0);
     if (g->h_ctl->status != 0) reset_tags(g, s);
@@ -1427,6 +1477,44 @@ int dsssp_tree_read(dsssp_graph* g, int32_t* parent, int64_t* dist) {
     if (parent) CK(cudaMemcpyAsync(parent, g->d_par, sizeof(int) * (size_t)g->n, cudaMemcpyDeviceToHost, s), "tree read");
     if (dist) CK(cudaMemcpyAsync(dist, g->d_dist, sizeof(long long) * (size_t)g->n, cudaMemcpyDeviceToHost, s), "tree read");
     CK(cudaStreamSynchronize(s), "tree read");
+    return DSSSP_OK;
+}
+
+int dsssp_tree_read_changed(dsssp_graph* g, int32_t* vertex, int32_t* parent, int64_t* dist, int64_t cap,
+                            int64_t* count) {
+    if (!g || !vertex || !parent || !dist || cap < 0 || !count) return fail(DSSSP_E_INVAL, "tree_read_changed: bad arguments");
+    int rc = set_device(g);
+    if (rc) return rc;
+    if (g->pending) return fail(DSSSP_E_INVAL, "tree_read_changed: a batch is still pending");
+    if (!g->delta_ok) return fail(DSSSP_E_INVAL, "tree_read_changed: no successful batch since the tree was set");
+    cudaStream_t s = g->stream;
+    if (!g->d_par) {
+        rc = dalloc(&g->d_par, (size_t)g->n, "tree staging");
+        if (!rc) rc = dalloc(&g->d_dist, (size_t)g->n, "tree staging");
+        if (rc) return rc;
+    }
+    if (!g->d_vtx) {
+        rc = dalloc(&g->d_vtx, (size_t)g->n, "tree staging");
+        if (!rc) rc = dalloc(&g->d_count, 1, "tree staging");
+        if (rc) return rc;
+    }
+    unsigned cnt = 0;
+    CK(cudaMemsetAsync(g->d_count, 0, sizeof(unsigned), s), "tree read");
+    k_tree_changed<<<blocks_for(g->n), kThreads, 0, s>>>(g->dg.state, g->dg.inv_tag, g->dg.chg_tag, g->dg.push_tag,
+                                                         g->dg.far_tag,
+                                                         g->n, g->delta_epoch, g->delta_lo, g->delta_hi, g->d_vtx,
+                                                         g->d_par, g->d_dist, g->d_count);
+    count_launch(1);
+    CK(cudaMemcpyAsync(&cnt, g->d_count, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "tree read");
+    CK(cudaStreamSynchronize(s), "tree read");
+    *count = cnt;
+    if ((int64_t)cnt > cap) return fail(DSSSP_E_INVAL, "tree_read_changed: %u changed vertices exceed cap %lld", cnt, (long long)cap);
+    if (cnt) {
+        CK(cudaMemcpyAsync(vertex, g->d_vtx, sizeof(int) * cnt, cudaMemcpyDeviceToHost, s), "tree read");
+        CK(cudaMemcpyAsync(parent, g->d_par, sizeof(int) * cnt, cudaMemcpyDeviceToHost, s), "tree read");
+        CK(cudaMemcpyAsync(dist, g->d_dist, sizeof(long long) * cnt, cudaMemcpyDeviceToHost, s), "tree read");
+        CK(cudaStreamSynchronize(s), "tree read");
+    }
     return DSSSP_OK;
 }
 
@@ -1571,6 +1659,7 @@ int dsssp_graph_restore(dsssp_graph* g, void* stream) {
     g->spare_top = (long long)g->s_spare[0];
     g->src = g->s_src;
     g->has_tree = g->s_has_tree;
+    g->delta_ok = false;  // the tags name batches after the snapshot
     return DSSSP_OK;
 }
 

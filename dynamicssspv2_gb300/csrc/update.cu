@@ -98,9 +98,12 @@ __device__ bool grid_sync(Ctl* ctl) {
 
 // Offers distance nd through parent u to vertex c whose current word is cur.  Returns true
 // when c's distance went down (c must then be pushed).  Zero-weight edges only replace a
-// strictly larger distance, so equal-distance parent swaps can never close a cycle.
-__device__ __forceinline__ bool relax_to(unsigned long long* state, unsigned c, unsigned long long nd,
+// strictly larger distance, so equal-distance parent swaps can never close a cycle.  A swap
+// to a smaller parent id at the same distance (the packed minimum's tie rule) is recorded in
+// chg_tag, so the batch's set of changed vertices stays complete.
+__device__ __forceinline__ bool relax_to(const DevGraph& g, unsigned epoch, unsigned c, unsigned long long nd,
                                          unsigned u, int w, unsigned long long cur, LocalStats& ls) {
+    unsigned long long* state = g.state;
     if (nd >= kDistInf) {
         if (cur == kInfState) ls.dist_ovf++;
         return false;
@@ -113,6 +116,7 @@ __device__ __forceinline__ bool relax_to(unsigned long long* state, unsigned c, 
             ls.updates++;
             return true;
         }
+        if (old > cand && g.chg_tag) g.chg_tag[c] = epoch;
         return false;
     }
     while ((cur >> 32) > nd) {
@@ -326,7 +330,7 @@ struct RelaxOp {
         for (int q = 0; q < 4; q++) {
             bool push = false;
             const unsigned long long nd = du + (unsigned)e[q].y;
-            if (e[q].y >= 0) push = relax_to(state, (unsigned)e[q].x, nd, u, e[q].y, cur[q], *ls);
+            if (e[q].y >= 0) push = relax_to(p->g, p->epoch, (unsigned)e[q].x, nd, u, e[q].y, cur[q], *ls);
             const bool later = push && nd >= far.T;
             far_push(*p, far, later, (unsigned)e[q].x);
             int deg;
@@ -426,7 +430,7 @@ struct PullOp {
             if (e[q].y > 0) {
                 const unsigned long long cand = (nd << 32) | (unsigned)e[q].x;
                 best = cand < best ? cand : best;
-            } else if (relax_to(state, x, nd, (unsigned)e[q].x, 0, __ldcg(&state[x]), *ls)) {
+            } else if (relax_to(p->g, p->epoch, x, nd, (unsigned)e[q].x, 0, __ldcg(&state[x]), *ls)) {
                 need = true;
             }
         }
@@ -837,9 +841,9 @@ __global__ void k_append(UpdParams p) {
         bool pa = false, pbv = false;
         const unsigned long long ndb = (sa >> 32) + (unsigned)c.z, nda = (sb >> 32) + (unsigned)c.z;
         if (alive) {
-            if ((sa >> 32) != kDistInf) pbv = relax_to(g.state, (unsigned)c.y, ndb, (unsigned)c.x, c.z, sb, ls);
+            if ((sa >> 32) != kDistInf) pbv = relax_to(g, p.epoch, (unsigned)c.y, ndb, (unsigned)c.x, c.z, sb, ls);
             if ((sb >> 32) != kDistInf)
-                pa = relax_to(g.state, (unsigned)c.x, nda, (unsigned)c.y, c.z, __ldcg(&g.state[c.x]), ls);
+                pa = relax_to(g, p.epoch, (unsigned)c.x, nda, (unsigned)c.y, c.z, __ldcg(&g.state[c.x]), ls);
             ls.edges_relax += 2;
         }
         const bool lb = pbv && ndb >= T, la = pa && nda >= T;

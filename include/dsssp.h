@@ -153,6 +153,16 @@ int dsssp_forest_load(dsssp_graph* g, const int32_t* parent, const int64_t* dist
  * Replaces printSSSP and the host print of SSSPmainForUndirected.cu:298-312. */
 int dsssp_tree_read(dsssp_graph* g, int32_t* parent, int64_t* dist);
 
+/* Reads back only the part of the tree the last batch may have changed: every vertex that
+ * the batch cut off or whose distance it lowered (a superset of the vertices whose parent or
+ * distance differs from before the batch), in no particular order.  vertex/parent/dist get
+ * *count entries (at most cap; cap = n always suffices).  A caller that keeps the previous
+ * tree on the host applies these entries to have the updated tree, at a fraction of the
+ * copy volume of dsssp_tree_read.  DSSSP_E_INVAL when there is no successful batch since the
+ * tree was loaded or computed, or when the set exceeds cap (then *count is its size). */
+int dsssp_tree_read_changed(dsssp_graph* g, int32_t* vertex, int32_t* parent, int64_t* dist,
+                            int64_t cap, int64_t* count);
+
 /* Applies one change batch from host memory and waits for it: copies the records to the
  * device, appends insertions into row slack, deletes every entry matching a deletion,
  * invalidates cut-off subtrees and relaxes to the new shortest-path tree.

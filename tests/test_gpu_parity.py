@@ -427,3 +427,39 @@ def test_graph_replay_matches_plain_launches():
             lu, lv, lw = (np.concatenate([a, ins[f]]) for a, f in ((cu, "u"), (cv, "v"), (cw, "w")))
             keep = kept[: len(lu)].astype(bool)
             cu, cv, cw = lu[keep].astype(np.int32), lv[keep].astype(np.int32), lw[keep].astype(np.int32)
+
+
+@pytest.mark.parametrize("opts", [{}, {"delta": 20}, {"slack_pct": 0, "slack_min": 0, "spare_pct": 0}])
+def test_changed_entries_rebuild_the_tree(opts):
+    """tree_read_changed after each batch, applied to the previous host tree, gives the tree
+    tree_read gives (including batches with row growth, a repack and near-far rounds)."""
+    n, m = 6000, 24000
+    u, v, w = D.gen_er(n, m, 1, 100, 41)
+    parent, dist = initial_tree(n, u, v, w)
+    with D.Graph(n, u, v, w, **opts) as g:
+        g.tree_load(parent, dist)
+        with pytest.raises(D.DsssspError):  # no batch yet
+            g.tree_read_changed()
+        host_p, host_d = parent.copy(), dist.copy()
+        for b in range(4):
+            ch = D.gen_changes(n, u, v, w, 300, 300, seed=500 + b)
+            g.apply_batch(ch)
+            vx, pp, dd = g.tree_read_changed()
+            assert len(vx) == len(np.unique(vx)) and len(vx) < n
+            host_p[vx], host_d[vx] = pp, dd
+            fp, fd = g.tree_read()
+            assert np.array_equal(host_p, fp) and np.array_equal(host_d, fd), f"batch {b}"
+            u, v, w = (np.asarray(a) for a in apply_lines_to(n, u, v, w, ch))
+        bad = D.make_changes([0], [n + 5], [1], [1])
+        with pytest.raises(D.DsssspError):
+            g.apply_batch(bad)
+        with pytest.raises(D.DsssspError):  # the last batch failed
+            g.tree_read_changed()
+
+
+def apply_lines_to(n, u, v, w, ch):
+    _, kept = O.updated_graph(n, u, v, w, ch, return_kept=True)
+    ins = ch[ch["op"] == 1]
+    lu, lv, lw = (np.concatenate([a, ins[f]]) for a, f in ((u, "u"), (v, "v"), (w, "w")))
+    keep = kept[: len(lu)].astype(bool)
+    return lu[keep].astype(np.int32), lv[keep].astype(np.int32), lw[keep].astype(np.int32)
