@@ -105,6 +105,7 @@ _sig("dsssp_tree_compute_multi", C.c_int, _P, _i32p, C.c_int32, C.POINTER(Stats)
 _sig("dsssp_forest_load", C.c_int, _P, _i32p, _i64p)
 _sig("dsssp_tree_read", C.c_int, _P, _P, _P)
 _sig("dsssp_tree_read_changed", C.c_int, _P, _P, _P, _P, C.c_int64, C.POINTER(C.c_int64))
+_sig("dsssp_tree_validate", C.c_int, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32))
 _sig("dsssp_apply_batch", C.c_int, _P, _P, C.c_int64, _P, C.POINTER(Stats))
 _sig("dsssp_apply_batch_async", C.c_int, _P, _P, C.c_int64, _P)
 _sig("dsssp_batch_finish", C.c_int, _P, C.POINTER(Stats))
@@ -155,6 +156,7 @@ EXPORTED = [
     "dsssp_gen_grid", "dsssp_gen_changes", "dsssp_max_degree_vertex", "dsssp_sssp_noalloc",
     "dsssp_gen_changes_ref", "dsssp_write_changes_file", "dsssp_write_graph_binary", "dsssp_read_graph_binary",
     "dsssp_write_sssp_binary", "dsssp_read_sssp_binary", "dsssp_graph_health", "dsssp_tree_read_changed",
+    "dsssp_tree_validate",
 ]
 
 
@@ -278,6 +280,12 @@ class Graph:
             dist = np.empty(self.n, np.int64)
         _check(_lib.dsssp_tree_read(self._h, parent.ctypes.data, dist.ctypes.data), "tree_read")
         return parent, dist
+
+    def validate(self) -> dict:
+        """Device-side certificate of the resident tree: {violations, roots, first_bad}."""
+        bad, roots, first = C.c_int64(), C.c_int64(), C.c_int32()
+        _check(_lib.dsssp_tree_validate(self._h, C.byref(bad), C.byref(roots), C.byref(first)), "tree_validate")
+        return {"violations": bad.value, "roots": roots.value, "first_bad": first.value}
 
     def tree_read_changed(self, vertex: np.ndarray | None = None, parent: np.ndarray | None = None,
                           dist: np.ndarray | None = None):

@@ -381,6 +381,66 @@ __global__ void k_tree_changed(const unsigned long long* state, const unsigned* 
     }
 }
 
+// ---- certificate of the resident tree (dsssp_tree_validate) -------------------------------
+// A warp per vertex v checks v's live adjacency entries: no entry (u, w) offers a shorter
+// distance (dist[u] + w < dist[v], an unreachable v included), a reachable non-root v has a
+// live entry to its parent p with dist[p] + w == dist[v], and a root (its own parent) has
+// distance 0.  out[0] counts violations, out[1] roots, out[2] the least violating vertex.
+__global__ void k_validate_rows(const unsigned long long* state, const RowDesc* rows, const int2* adj, int n,
+                                unsigned* jm, unsigned long long* out) {
+    const unsigned lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long v = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
+        const unsigned long long sv = state[v];
+        const bool reach = sv != kInfState;
+        const unsigned long long dv = reach ? (sv >> 32) : (unsigned long long)kDistInf;
+        const unsigned pv = (unsigned)sv;
+        const RowDesc rd = rows[v];
+        bool bad = false, tight = false;
+        for (int i = (int)lane; i < rd.deg; i += 32) {
+            const int2 e = adj[rd.start + i];
+            if (e.y < 0) continue;
+            const unsigned long long su = state[e.x];
+            if (su == kInfState) continue;
+            const unsigned long long du = su >> 32;
+            if (du + (unsigned)e.y < dv) bad = true;  // a shorter distance is on offer
+            if (reach && (unsigned)e.x == pv && du + (unsigned)e.y == dv) tight = true;
+        }
+        bad = __any_sync(0xFFFFFFFFu, bad);
+        tight = __any_sync(0xFFFFFFFFu, tight);
+        if (lane == 0) {
+            const bool root = reach && pv == (unsigned)v;
+            if (reach && !root && (pv >= (unsigned)n || !tight)) bad = true;  // no tight live parent edge
+            if (root && dv != 0) bad = true;
+            if (root) atomicAdd(&out[1], 1ull);
+            if (bad) {
+                atomicAdd(&out[0], 1ull);
+                atomicMin(&out[2], (unsigned long long)v);
+            }
+            // pointer-jumping word: terminal (kTagOk) at roots and unreachable vertices
+            jm[v] = (!reach || root || pv >= (unsigned)n) ? kTagOk : pv;
+        }
+    }
+}
+
+// One pointer-jumping pass: jm[v] <- jm[jm[v]] until it is terminal.
+__global__ void k_validate_jump(unsigned* jm, int n) {
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const unsigned j = jm[v];
+        if (j < kTagInv) jm[v] = jm[j];
+    }
+}
+
+// Vertices whose parent chain is still not terminal after 32 doublings lie on a cycle.
+__global__ void k_validate_cycles(const unsigned* jm, int n, unsigned long long* out) {
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        if (jm[v] < kTagInv) {
+            atomicAdd(&out[0], 1ull);
+            atomicMin(&out[2], (unsigned long long)v);
+        }
+    }
+}
+
 __global__ void k_state_reset(unsigned long long* state, int n) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v < n) state[v] = kInfState;
@@ -1515,6 +1575,36 @@ int dsssp_tree_read_changed(dsssp_graph* g, int32_t* vertex, int32_t* parent, in
         CK(cudaMemcpyAsync(dist, g->d_dist, sizeof(long long) * cnt, cudaMemcpyDeviceToHost, s), "tree read");
         CK(cudaStreamSynchronize(s), "tree read");
     }
+    return DSSSP_OK;
+}
+
+int dsssp_tree_validate(dsssp_graph* g, int64_t* violations, int64_t* roots, int32_t* first_bad) {
+    if (!g || !violations) return fail(DSSSP_E_INVAL, "tree_validate: bad arguments");
+    int rc = set_device(g);
+    if (rc) return rc;
+    if (g->pending) return fail(DSSSP_E_INVAL, "tree_validate: a batch is still pending");
+    cudaStream_t s = g->stream;
+    unsigned long long* d_out = nullptr;
+    rc = dalloc(&d_out, 3, "validation counters");
+    if (rc) return rc;
+    const unsigned long long init[3] = {0, 0, ~0ull};
+    unsigned long long out[3] = {0, 0, 0};
+    cudaError_t e = cudaMemcpyAsync(d_out, init, sizeof(init), cudaMemcpyHostToDevice, s);
+    const unsigned grid = (unsigned)(g->num_sms * 8);
+    if (e == cudaSuccess) {
+        k_validate_rows<<<grid, kThreads, 0, s>>>(g->dg.state, g->dg.rows, g->dg.adj, g->n, g->dg.jm, d_out);
+        for (int pass = 0; pass < 32; pass++) k_validate_jump<<<grid, kThreads, 0, s>>>(g->dg.jm, g->n);
+        k_validate_cycles<<<grid, kThreads, 0, s>>>(g->dg.jm, g->n, d_out);
+        count_launch(34);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, sizeof(out), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    dfree(d_out);
+    if (e != cudaSuccess) return cuda_fail(e, "tree_validate");
+    *violations = (int64_t)out[0];
+    if (roots) *roots = (int64_t)out[1];
+    if (first_bad) *first_bad = out[0] ? (int32_t)out[2] : -1;
     return DSSSP_OK;
 }
 

@@ -153,6 +153,15 @@ int dsssp_forest_load(dsssp_graph* g, const int32_t* parent, const int64_t* dist
  * Replaces printSSSP and the host print of SSSPmainForUndirected.cu:298-312. */
 int dsssp_tree_read(dsssp_graph* g, int32_t* parent, int64_t* dist);
 
+/* Certificate of the resident tree on the device: counts violations of (a) no live edge
+ * (u, v, w) with dist[u] + w < dist[v] (an unreachable v included), (b) every reachable
+ * vertex other than a root has a live edge to its parent p with dist[p] + w == dist[v],
+ * (c) a root (its own parent) has distance 0, (d) parent chains end at a root (no cycle).
+ * Zero violations means the distances are the exact shortest distances from the set of
+ * roots and the parents form a shortest-path forest.  *roots gets the number of roots and
+ * *first_bad the least violating vertex (-1 if none); either may be NULL. */
+int dsssp_tree_validate(dsssp_graph* g, int64_t* violations, int64_t* roots, int32_t* first_bad);
+
 /* Reads back only the part of the tree the last batch may have changed: every vertex that
  * the batch cut off or whose distance it lowered (a superset of the vertices whose parent or
  * distance differs from before the batch), in no particular order.  vertex/parent/dist get

@@ -463,3 +463,39 @@ def apply_lines_to(n, u, v, w, ch):
     lu, lv, lw = (np.concatenate([a, ins[f]]) for a, f in ((u, "u"), (v, "v"), (w, "w")))
     keep = kept[: len(lu)].astype(bool)
     return lu[keep].astype(np.int32), lv[keep].astype(np.int32), lw[keep].astype(np.int32)
+
+
+def test_device_certificate_of_the_tree():
+    """dsssp_tree_validate: zero violations for computed and updated trees (zero weights,
+    near-far, repacks), and it catches a wrong distance and a parent cycle."""
+    n, m = 4000, 16000
+    u, v, w = D.gen_er(n, m, 0, 30, 51)  # weight 0 included
+    with D.Graph(n, u, v, w, slack_pct=0, slack_min=0, spare_pct=0) as g:
+        g.tree_compute(0)
+        c = g.validate()
+        assert c["violations"] == 0 and c["roots"] == 1 and c["first_bad"] == -1
+        for b, opts in enumerate(({}, {"delta": 7}, {"bfs_levels": 0})):
+            o = g.get_opts()
+            for key, val in opts.items():
+                setattr(o, key, val)
+            g.set_opts(o)
+            ch = D.gen_changes(n, u, v, w, 400, 400, wlo=0, whi=30, seed=600 + b)
+            st = g.apply_batch(ch)
+            assert g.validate()["violations"] == 0, f"batch {b}"
+            u, v, w = apply_lines_to(n, u, v, w, ch)
+        assert st.repacks + st.overflow_entries > 0
+        parent, dist = g.tree_read()
+        bad = dist.copy()
+        k = int(np.flatnonzero((parent >= 0) & (np.arange(n) != 0))[0])
+        bad[k] += 1
+        g.tree_load(parent, bad)
+        c = g.validate()
+        assert c["violations"] >= 1
+    # a parent cycle over zero-weight edges, cut off from the source: distances look tight
+    u = np.array([0, 2, 3, 4], np.int32)
+    v = np.array([1, 3, 4, 2], np.int32)
+    w = np.array([1, 0, 0, 0], np.int32)
+    with D.Graph(5, u, v, w) as g:
+        g.tree_load(np.array([0, 0, 4, 2, 3], np.int32), np.array([0, 1, 5, 5, 5], np.int64))
+        c = g.validate()
+        assert c["violations"] == 3 and c["first_bad"] == 2
