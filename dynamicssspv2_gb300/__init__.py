@@ -106,6 +106,9 @@ _sig("dsssp_forest_load", C.c_int, _P, _i32p, _i64p)
 _sig("dsssp_tree_read", C.c_int, _P, _P, _P)
 _sig("dsssp_tree_read_changed", C.c_int, _P, _P, _P, _P, C.c_int64, C.POINTER(C.c_int64))
 _sig("dsssp_tree_validate", C.c_int, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32))
+_sig("dsssp_debug_set", C.c_int, _P, C.c_int32, C.c_int64)
+DEBUG_SPIN_LIMIT = 1
+DEBUG_STALL_US = 2
 _sig("dsssp_apply_batch", C.c_int, _P, _P, C.c_int64, _P, C.POINTER(Stats))
 _sig("dsssp_apply_batch_async", C.c_int, _P, _P, C.c_int64, _P)
 _sig("dsssp_batch_finish", C.c_int, _P, C.POINTER(Stats))
@@ -156,7 +159,7 @@ EXPORTED = [
     "dsssp_gen_grid", "dsssp_gen_changes", "dsssp_max_degree_vertex", "dsssp_sssp_noalloc",
     "dsssp_gen_changes_ref", "dsssp_write_changes_file", "dsssp_write_graph_binary", "dsssp_read_graph_binary",
     "dsssp_write_sssp_binary", "dsssp_read_sssp_binary", "dsssp_graph_health", "dsssp_tree_read_changed",
-    "dsssp_tree_validate",
+    "dsssp_tree_validate", "dsssp_debug_set",
 ]
 
 
@@ -280,6 +283,10 @@ class Graph:
             dist = np.empty(self.n, np.int64)
         _check(_lib.dsssp_tree_read(self._h, parent.ctypes.data, dist.ctypes.data), "tree_read")
         return parent, dist
+
+    def debug_set(self, what: int, value: int) -> None:
+        """Failure-detection test hooks (DEBUG_SPIN_LIMIT, DEBUG_STALL_US)."""
+        _check(_lib.dsssp_debug_set(self._h, int(what), int(value)), "debug_set")
 
     def validate(self) -> dict:
         """Device-side certificate of the resident tree: {violations, roots, first_bad}."""

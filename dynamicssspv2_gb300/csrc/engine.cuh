@@ -78,7 +78,9 @@ struct __align__(128) Ctl {
     // line 0 (persistent)
     unsigned bar_gen;
     unsigned round_base;
-    unsigned pad0[30];
+    unsigned spin_limit;  // grid-barrier poll limit (0 = default); persistent, set by the host
+    unsigned stall_us;    // test hook: the last CTA of k_update waits this long before its first barrier
+    unsigned pad0[28];
     // line 1
     int status;
     int ovf_count;

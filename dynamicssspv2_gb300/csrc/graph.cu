@@ -1578,6 +1578,21 @@ int dsssp_tree_read_changed(dsssp_graph* g, int32_t* vertex, int32_t* parent, in
     return DSSSP_OK;
 }
 
+int dsssp_debug_set(dsssp_graph* g, int32_t what, int64_t value) {
+    if (!g) return fail(DSSSP_E_INVAL, "debug_set: NULL graph");
+    int rc = set_device(g);
+    if (rc) return rc;
+    if (g->pending) return fail(DSSSP_E_INVAL, "debug_set: a batch is still pending");
+    unsigned* field = nullptr;
+    if (what == DSSSP_DEBUG_SPIN_LIMIT && value >= 0 && value <= (1ll << 24)) field = &g->dg.ctl->spin_limit;
+    else if (what == DSSSP_DEBUG_STALL_US && value >= 0 && value <= 1000000) field = &g->dg.ctl->stall_us;
+    if (!field) return fail(DSSSP_E_INVAL, "debug_set: unknown hook %d or value %lld out of range", what, (long long)value);
+    const unsigned v = (unsigned)value;
+    CK(cudaMemcpyAsync(field, &v, sizeof(v), cudaMemcpyHostToDevice, g->stream), "debug_set");
+    CK(cudaStreamSynchronize(g->stream), "debug_set");
+    return DSSSP_OK;
+}
+
 int dsssp_tree_validate(dsssp_graph* g, int64_t* violations, int64_t* roots, int32_t* first_bad) {
     if (!g || !violations) return fail(DSSSP_E_INVAL, "tree_validate: bad arguments");
     int rc = set_device(g);

@@ -43,7 +43,7 @@ namespace dsssp {
 namespace {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
-constexpr unsigned kSpinLimit = 1u << 24;  // x ~200 ns sleeps: a barrier gives up after ~3 s
+constexpr unsigned kSpinLimit = 1u << 20;  // polls of ~1 us: a barrier gives up after ~1 s
 constexpr int kMaxWarps = 8;               // update kernel blocks have at most 256 threads
 constexpr int kBuf = 256;                  // per-warp push buffer (vertex, degree) entries
 constexpr int kAddsPerCheck = 128;         // entries a warp may add between two flush checks
@@ -52,7 +52,8 @@ constexpr unsigned kSoloWaves = 2;         // a step of at most this many CTA-wa
                                            // runs on CTA 0 alone (block barriers)
 constexpr int kSoloSteps = 256;            // consecutive solo steps before the grid re-syncs
 
-__shared__ unsigned s_nbar;  // grid barriers this CTA has passed
+__shared__ unsigned s_nbar;        // grid barriers this CTA has passed
+__shared__ unsigned s_spin_limit;  // polls before a grid barrier gives up
 __shared__ uint2 s_pbuf[kMaxWarps][kBuf];  // (vertex, degree) pushed, not yet expanded
 
 struct LocalStats {
@@ -77,7 +78,7 @@ __device__ bool grid_sync(Ctl* ctl) {
         } else {
             unsigned spins = 0;
             while (ld_acquire(&ctl->bar_gen) == gen) {
-                if (++spins > kSpinLimit) {
+                if (++spins > s_spin_limit) {
                     if (atomicCAS(&ctl->status, 0, -6 /* DSSSP_E_TIMEOUT */) == 0) {
                         ctl->diag[0] = s_nbar;
                         ctl->diag[1] = atomicAdd(&ctl->bar_count, 0u);
@@ -873,7 +874,11 @@ __global__ void k_append(UpdParams p) {
 __device__ void update_body(UpdParams& p);
 
 __global__ void __launch_bounds__(256, 4) k_update(UpdParams p) {
-    if (threadIdx.x == 0) s_nbar = 0;
+    if (threadIdx.x == 0) {
+        s_nbar = 0;
+        const unsigned lim = __ldcg(&p.g.ctl->spin_limit);
+        s_spin_limit = lim ? lim : kSpinLimit;
+    }
     __syncthreads();
     update_body(p);
     __syncthreads();
@@ -890,6 +895,13 @@ __device__ void update_body(UpdParams& p) {
     if (threadIdx.x == 0) s_skip = __ldcg(&ctl->status) != 0;  // set before launch: same for every CTA
     __syncthreads();
     if (s_skip) return;
+    const unsigned stall_us = __ldcg(&ctl->stall_us);
+    if (stall_us && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+        // test hook (failure detection): arrive late at the first barrier so that the others
+        // run out of polls; a bounded wait (at most 2^21 sleeps of 1 us)
+        const unsigned long long t0 = globaltimer();
+        for (unsigned i = 0; i < (1u << 21) && globaltimer() - t0 < 1000ull * stall_us; i++) __nanosleep(1000);
+    }
     const unsigned lane = lane_id();
     const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned nthreads = gridDim.x * blockDim.x;

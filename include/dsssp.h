@@ -153,6 +153,16 @@ int dsssp_forest_load(dsssp_graph* g, const int32_t* parent, const int64_t* dist
  * Replaces printSSSP and the host print of SSSPmainForUndirected.cu:298-312. */
 int dsssp_tree_read(dsssp_graph* g, int32_t* parent, int64_t* dist);
 
+/* Test hooks for failure detection (not for production use).
+ * DSSSP_DEBUG_SPIN_LIMIT: polls of about 1 us before a grid barrier of the update kernel
+ *   gives up with DSSSP_E_TIMEOUT (0 = the default 2^20, about 1 s).
+ * DSSSP_DEBUG_STALL_US: the last CTA of the update kernel waits this many microseconds
+ *   (0..1,000,000; 0 = off) before its first grid barrier, so that a small spin limit runs
+ *   out: the batch fails with DSSSP_E_TIMEOUT and the device stays usable. */
+#define DSSSP_DEBUG_SPIN_LIMIT 1
+#define DSSSP_DEBUG_STALL_US 2
+int dsssp_debug_set(dsssp_graph* g, int32_t what, int64_t value);
+
 /* Certificate of the resident tree on the device: counts violations of (a) no live edge
  * (u, v, w) with dist[u] + w < dist[v] (an unreachable v included), (b) every reachable
  * vertex other than a root has a live edge to its parent p with dist[p] + w == dist[v],
