@@ -9,7 +9,9 @@ one launch sequence (their work overlaps on the device).  A tenant never has two
 in one epoch, so each tenant sees its batches applied one after another in arrival order,
 and each result equals applying that batch alone (distances bit-exact; parents a valid
 tree, possibly another one on ties).  Requests that arrive while an epoch runs wait for the
-next one; requests for tenants that were not admitted are refused.
+next one; requests for tenants that were not admitted are refused, and a request whose
+batch names a vertex outside its tenant's graph or inserts a negative weight fails on
+arrival (`error` says why) without touching the epoch it would have joined.
 
 Storage upkeep runs between epochs, only while no request waits: when the store's tombstoned
 entries exceed `compact_dead_frac` of its live entries, or the spare region that overflowing
@@ -64,6 +66,7 @@ class Request:
     start: float = float("nan")
     done: float = float("nan")
     refused: bool = False
+    error: str | None = None
     result: tuple | None = field(default=None, repr=False)
 
     @property
@@ -126,6 +129,18 @@ class Server:
         self.compactions += 1
         return True
 
+    def check(self, r: Request) -> str | None:
+        """Why the request's batch cannot be applied to its tenant, or None."""
+        ch = np.asarray(r.changes, CHANGE_DTYPE)
+        live = (ch["op"] == 0) | (ch["op"] == 1)
+        n = self.tenants[r.tenant].n
+        cu, cv = ch["u"][live], ch["v"][live]
+        if ((cu < 0) | (cu >= n) | (cv < 0) | (cv >= n)).any():
+            return f"a change names a vertex outside 0..{n - 1}"
+        if ((ch["op"] == 1) & (ch["w"] < 0)).any():
+            return "an insertion has a negative weight"
+        return None
+
     def tree(self, tenant: int):
         return self.pool.tree_read(self.slot[tenant])
 
@@ -148,6 +163,10 @@ class Server:
                 nxt += 1
                 if r.tenant not in self.slot:
                     r.refused = True
+                    r.done = r.start = r.arrival
+                    continue
+                r.error = self.check(r)
+                if r.error is not None:
                     r.done = r.start = r.arrival
                     continue
                 queues[r.tenant].append(r)
@@ -180,14 +199,15 @@ class Server:
 
 
 def summarize(reqs) -> dict:
-    served = [r for r in reqs if not r.refused]
+    served = [r for r in reqs if not r.refused and r.error is None]
     lat = np.array([r.latency for r in served]) if served else np.zeros(0)
     changes = sum(len(r.changes) for r in served)
     span = (max(r.done for r in served) - min(r.arrival for r in served)) if served else 0.0
     return {
         "requests": len(reqs),
         "served": len(served),
-        "refused": len(reqs) - len(served),
+        "refused": sum(1 for r in reqs if r.refused),
+        "failed": sum(1 for r in reqs if r.error is not None),
         "changes": int(changes),
         "span_s": span,
         "change_edges_per_s": changes / span if span > 0 else 0.0,

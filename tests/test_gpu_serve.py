@@ -93,3 +93,30 @@ def test_saturated_serving_batches_all_tenants():
         out = srv.serve(reqs, realtime=False)
     assert srv.epochs == 3  # every epoch takes one request of each tenant
     assert summarize(out)["mean_requests_per_epoch"] == 5
+
+
+def test_malformed_requests_fail_alone():
+    """Requests naming a vertex outside their tenant's graph or inserting a negative weight fail
+    on arrival; the requests around them are served exactly as if they were not there."""
+    tenants = make_tenants(3, 7)
+    rng = np.random.default_rng(8)
+    good = [Request(t, 0.001 * i, random_batch(rng, tenants[t], 80)) for i, t in enumerate([0, 1, 2, 0, 1, 2])]
+    bad_vertex = random_batch(rng, tenants[1], 20)
+    bad_vertex["v"][3] = tenants[1].n + 7
+    bad_weight = random_batch(rng, tenants[2], 20)
+    bad_weight["w"][bad_weight["op"] == 1] = -5
+    reqs = good + [Request(1, 0.0025, bad_vertex), Request(2, 0.0035, bad_weight)]
+    with Server(tenants) as srv:
+        out = srv.serve(reqs, record=True)
+    failed = [r for r in out if r.error is not None]
+    assert len(failed) == 2 and all(r.result is None for r in failed)
+    assert "vertex" in failed[0].error and "negative" in failed[1].error
+    s = summarize(out)
+    assert s["failed"] == 2 and s["served"] == len(good)
+    for t, ten in enumerate(tenants):
+        mine = sorted([r for r in out if r.tenant == t and r.error is None], key=lambda r: r.arrival)
+        with D.Graph(ten.n, ten.u, ten.v, ten.w) as g:
+            g.tree_compute(ten.src)
+            for r in mine:
+                g.apply_batch(r.changes)
+                assert np.array_equal(g.tree_read()[1], r.result[1])
