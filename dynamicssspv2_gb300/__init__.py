@@ -109,6 +109,60 @@ _sig("dsssp_tree_validate", C.c_int, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int
 _sig("dsssp_debug_set", C.c_int, _P, C.c_int32, C.c_int64)
 DEBUG_SPIN_LIMIT = 1
 DEBUG_STALL_US = 2
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [
+        ("memory_budget", C.c_int64),
+        ("max_epoch_requests", C.c_int32),
+        ("record", C.c_int32),
+        ("compact_dead_frac", C.c_double),
+        ("compact_spare_frac", C.c_double),
+    ]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [
+        ("id", C.c_int64),
+        ("tenant", C.c_int32),
+        ("status", C.c_int32),
+        ("epoch", C.c_int64),
+        ("changes", C.c_int64),
+        ("arrival_us", C.c_double),
+        ("start_us", C.c_double),
+        ("done_us", C.c_double),
+        ("error", C.c_char * 96),
+    ]
+
+
+REFUSED = 1
+_PP = C.POINTER(C.c_void_p)
+_sig("dsssp_tree_read_range", C.c_int, _P, C.c_int32, C.c_int32, _P, _P)
+_sig("dsssp_pool_create", C.c_int, C.c_int32, _P, _P, _PP, _PP, _PP, C.POINTER(Opts), C.POINTER(_P))
+_sig("dsssp_pool_destroy", None, _P)
+_sig("dsssp_pool_graph", _P, _P)
+_sig("dsssp_pool_offsets", C.c_int, _P, _P)
+_sig("dsssp_pool_tree_compute", C.c_int, _P, _P, C.POINTER(Stats))
+_sig("dsssp_pool_forest_load", C.c_int, _P, _PP, _PP)
+_sig("dsssp_pool_union", C.c_int, _P, C.c_int32, _P, _PP, _P, _P, C.c_int64, C.POINTER(C.c_int64))
+_sig("dsssp_pool_apply", C.c_int, _P, C.c_int32, _P, _PP, _P, C.POINTER(Stats))
+_sig("dsssp_pool_tree_read", C.c_int, _P, C.c_int32, _P, _P)
+_sig("dsssp_estimate_footprint", C.c_int64, C.c_int32, C.c_int64, C.c_int32, C.c_int32)
+_sig("dsssp_default_server_opts", None, C.POINTER(ServerOpts))
+_sig("dsssp_server_create", C.c_int, C.c_int32, _P, _P, _PP, _PP, _PP, _P, C.POINTER(ServerOpts), C.POINTER(Opts),
+     C.POINTER(_P))
+_sig("dsssp_server_destroy", None, _P)
+_sig("dsssp_server_slot", C.c_int, _P, C.c_int32)
+_sig("dsssp_submit", C.c_int, _P, C.c_int32, _P, C.c_int64, C.POINTER(C.c_int64))
+_sig("dsssp_submit_many", C.c_int, _P, C.c_int32, _P, _PP, _P, _P)
+_sig("dsssp_poll", C.c_int, _P, C.POINTER(RequestInfo), C.c_int32, C.c_int32, C.POINTER(C.c_int32))
+_sig("dsssp_server_drain", C.c_int, _P, C.c_int32)
+_sig("dsssp_server_result", C.c_int, _P, C.c_int64, _P, _P)
+_sig("dsssp_server_tree_read", C.c_int, _P, C.c_int32, _P, _P)
+_sig("dsssp_server_info", C.c_int, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double),
+     C.POINTER(C.c_int64))
+_sig("dsssp_server_pool", _P, _P)
+_sig("dsssp_server_set_record", C.c_int, _P, C.c_int32)
 _sig("dsssp_apply_batch", C.c_int, _P, _P, C.c_int64, _P, C.POINTER(Stats))
 _sig("dsssp_apply_batch_async", C.c_int, _P, _P, C.c_int64, _P)
 _sig("dsssp_batch_finish", C.c_int, _P, C.POINTER(Stats))
@@ -159,7 +213,13 @@ EXPORTED = [
     "dsssp_gen_grid", "dsssp_gen_changes", "dsssp_max_degree_vertex", "dsssp_sssp_noalloc",
     "dsssp_gen_changes_ref", "dsssp_write_changes_file", "dsssp_write_graph_binary", "dsssp_read_graph_binary",
     "dsssp_write_sssp_binary", "dsssp_read_sssp_binary", "dsssp_graph_health", "dsssp_tree_read_changed",
-    "dsssp_tree_validate", "dsssp_debug_set",
+    "dsssp_tree_validate", "dsssp_debug_set", "dsssp_tree_read_range",
+    "dsssp_pool_create", "dsssp_pool_destroy", "dsssp_pool_graph", "dsssp_pool_offsets", "dsssp_pool_tree_compute",
+    "dsssp_pool_forest_load", "dsssp_pool_union", "dsssp_pool_apply", "dsssp_pool_tree_read",
+    "dsssp_estimate_footprint", "dsssp_default_server_opts", "dsssp_server_create", "dsssp_server_destroy",
+    "dsssp_server_slot", "dsssp_submit", "dsssp_submit_many", "dsssp_poll", "dsssp_server_drain",
+    "dsssp_server_result", "dsssp_server_tree_read", "dsssp_server_info", "dsssp_server_pool",
+    "dsssp_server_set_record",
 ]
 
 
@@ -227,7 +287,8 @@ class Graph:
             _lib.dsssp_graph_destroy(self._h)
             self._h = _P()
 
-    __del__ = close
+    def __del__(self):
+        self.close()  # dispatches to a subclass's close (a pool's graph is owned by the pool)
 
     def __enter__(self):
         return self

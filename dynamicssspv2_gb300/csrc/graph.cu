@@ -1540,6 +1540,27 @@ int dsssp_tree_read(dsssp_graph* g, int32_t* parent, int64_t* dist) {
     return DSSSP_OK;
 }
 
+int dsssp_tree_read_range(dsssp_graph* g, int32_t first, int32_t count, int32_t* parent, int64_t* dist) {
+    if (!g || first < 0 || count < 0 || (long long)first + count > g->n || (count > 0 && (!parent || !dist)))
+        return fail(DSSSP_E_INVAL, "tree_read_range: bad arguments");
+    int rc = set_device(g);
+    if (rc) return rc;
+    if (g->pending) return fail(DSSSP_E_INVAL, "tree_read_range: a batch is still pending");
+    if (count == 0) return DSSSP_OK;
+    cudaStream_t s = g->stream;
+    if (!g->d_par) {
+        rc = dalloc(&g->d_par, (size_t)g->n, "tree staging");
+        if (!rc) rc = dalloc(&g->d_dist, (size_t)g->n, "tree staging");
+        if (rc) return rc;
+    }
+    k_tree_unpack<<<blocks_for(count), kThreads, 0, s>>>(g->dg.state + first, count, g->d_par, g->d_dist);
+    count_launch(1);
+    CK(cudaMemcpyAsync(parent, g->d_par, sizeof(int) * (size_t)count, cudaMemcpyDeviceToHost, s), "tree read");
+    CK(cudaMemcpyAsync(dist, g->d_dist, sizeof(long long) * (size_t)count, cudaMemcpyDeviceToHost, s), "tree read");
+    CK(cudaStreamSynchronize(s), "tree read");
+    return DSSSP_OK;
+}
+
 int dsssp_tree_read_changed(dsssp_graph* g, int32_t* vertex, int32_t* parent, int64_t* dist, int64_t cap,
                             int64_t* count) {
     if (!g || !vertex || !parent || !dist || cap < 0 || !count) return fail(DSSSP_E_INVAL, "tree_read_changed: bad arguments");

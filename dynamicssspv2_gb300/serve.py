@@ -1,17 +1,19 @@
 """Serving layer: resident tenant graphs, change batches applied as they arrive.
 
-A Server keeps the graphs and trees of its tenants resident in HBM in one pooled graph store
-(`GraphPool`), admitting tenants in order while their estimated device footprint fits the
-memory budget.  Requests -- (arrival time, tenant, change batch) -- are served with
-continuous batching: whenever the device is free, every tenant with a waiting request
-contributes its oldest request to the next epoch, and the epoch's requests run together in
-one launch sequence (their work overlaps on the device).  A tenant never has two requests
-in one epoch, so each tenant sees its batches applied one after another in arrival order,
-and each result equals applying that batch alone (distances bit-exact; parents a valid
-tree, possibly another one on ties).  Requests that arrive while an epoch runs wait for the
-next one; requests for tenants that were not admitted are refused, and a request whose
-batch names a vertex outside its tenant's graph or inserts a negative weight fails on
-arrival (`error` says why) without touching the epoch it would have joined.
+A thin binding of the native server (`dsssp_server_*`, `dsssp_submit`, `dsssp_poll` in
+include/dsssp.h, csrc/serve.cpp).  It keeps the graphs and trees of its tenants resident in
+HBM in one pooled graph store, admitting tenants in order while their estimated device
+footprint fits the memory budget.  Requests -- (arrival time, tenant, change batch) -- are
+served with continuous batching by a native worker thread: whenever the device is free,
+every tenant with a waiting request contributes its oldest request to the next epoch, and
+the epoch's requests run together in one launch sequence (their work overlaps on the
+device).  A tenant never has two requests in one epoch, so each tenant sees its batches
+applied one after another in arrival order, and each result equals applying that batch
+alone (distances bit-exact; parents a valid tree, possibly another one on ties).  Requests
+that arrive while an epoch runs wait for the next one; requests for tenants that were not
+admitted are refused, and a request whose batch names a vertex outside its tenant's graph or
+inserts a negative weight fails on arrival (`error` says why) without touching the epoch it
+would have joined.
 
 Storage upkeep runs between epochs, only while no request waits: when the store's tombstoned
 entries exceed `compact_dead_frac` of its live entries, or the spare region that overflowing
@@ -22,27 +24,19 @@ No counterpart in the reference, which applies one batch per process run.
 """
 from __future__ import annotations
 
-import collections
+import ctypes as C
 import time
 from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import CHANGE_DTYPE
-from .pool import GraphPool
-
-# Device bytes per vertex and per adjacency slot of the engine's graph store: state 8, row
-# descriptor 16, sorted-prefix length 4, three tags 12, cut-off root list 4; per slot the
-# entry 8 and the twin 4; work lists: three lists of thread items (8 B per slot / te + per
-# vertex) and three of CTA items; plus a snapshot-free margin.
-_BYTES_PER_VERTEX = 8 + 16 + 4 + 12 + 4 + 3 * 8
-_BYTES_PER_SLOT = 8 + 4 + 3 * 8 / 4
+from . import CHANGE_DTYPE, REFUSED, RequestInfo, ServerOpts, _check, _lib, default_opts
+from .pool import _ptrs
 
 
 def estimate_footprint(n: int, m: int, slack_pct: int = 25, slack_min: int = 4) -> int:
     """Device bytes the engine needs for a graph of n vertices and m undirected edges."""
-    slots = 2 * m * (1 + slack_pct / 100.0) + n * slack_min
-    return int(n * _BYTES_PER_VERTEX + slots * _BYTES_PER_SLOT + (1 << 20))
+    return int(_lib.dsssp_estimate_footprint(int(n), int(m), int(slack_pct), int(slack_min)))
 
 
 @dataclass
@@ -78,32 +72,33 @@ class Server:
     def __init__(self, tenants, memory_budget: int | None = None, max_epoch_requests: int | None = None,
                  compact_dead_frac: float | None = 0.25, compact_spare_frac: float = 0.75, **opts):
         self.tenants = list(tenants)
-        slack_pct = opts.get("slack_pct", 25)
-        slack_min = opts.get("slack_min", 4)
-        self.footprints = [estimate_footprint(t.n, len(t.u), slack_pct, slack_min) for t in self.tenants]
-        self.admitted = []
-        used = 0
-        for i, fp in enumerate(self.footprints):
-            if memory_budget is None or used + fp <= memory_budget:
-                self.admitted.append(i)
-                used += fp
-        self.reserved = used
-        self.slot = {t: j for j, t in enumerate(self.admitted)}  # tenant index -> pool index
-        self.max_epoch_requests = max_epoch_requests
-        self.pool = None
-        if self.admitted:
-            ts = [self.tenants[i] for i in self.admitted]
-            self.pool = GraphPool([(t.n, t.u, t.v, t.w) for t in ts], **opts)
-            self.pool.tree_compute([t.src for t in ts])
-        self.epochs = 0
-        self.compact_dead_frac = compact_dead_frac
-        self.compact_spare_frac = compact_spare_frac
-        self.compactions = 0
-        self.compact_ms = []
+        o = default_opts(**opts)
+        self.footprints = [estimate_footprint(t.n, len(t.u), o.slack_pct, o.slack_min) for t in self.tenants]
+        so = ServerOpts()
+        _lib.dsssp_default_server_opts(C.byref(so))
+        so.memory_budget = int(memory_budget or 0)
+        so.max_epoch_requests = int(max_epoch_requests or 0)
+        so.compact_dead_frac = -1.0 if compact_dead_frac is None else float(compact_dead_frac)
+        so.compact_spare_frac = float(compact_spare_frac)
+        n = np.asarray([t.n for t in self.tenants], np.int32)
+        us = [np.ascontiguousarray(t.u, np.int32) for t in self.tenants]
+        vs = [np.ascontiguousarray(t.v, np.int32) for t in self.tenants]
+        ws = [np.ascontiguousarray(t.w, np.int32) for t in self.tenants]
+        m = np.asarray([len(a) for a in us], np.int64)
+        src = np.asarray([t.src for t in self.tenants], np.int32)
+        h = C.c_void_p()
+        _check(_lib.dsssp_server_create(len(n), n.ctypes.data, m.ctypes.data, _ptrs(us), _ptrs(vs), _ptrs(ws),
+                                        src.ctypes.data, C.byref(so), C.byref(o), C.byref(h)), "server_create")
+        self._h = h
+        self.admitted = [t for t in range(len(self.tenants)) if _lib.dsssp_server_slot(h, t) >= 0]
+        self.slot = {t: _lib.dsssp_server_slot(h, t) for t in self.admitted}
+        self.reserved = sum(self.footprints[t] for t in self.admitted)
 
     def close(self) -> None:
-        if self.pool is not None:
-            self.pool.close()
+        if getattr(self, "_h", None) and self._h.value:
+            self._final = self._info()  # counters stay readable after close
+            _lib.dsssp_server_destroy(self._h)
+            self._h = C.c_void_p()
 
     def __enter__(self):
         return self
@@ -111,90 +106,85 @@ class Server:
     def __exit__(self, *exc):
         self.close()
 
-    def needs_compaction(self) -> bool:
-        if self.pool is None or self.compact_dead_frac is None:
-            return False
-        h = self.pool.graph.health()
-        if h["dead"] > self.compact_dead_frac * max(1, h["live"]):
-            return True
-        return h["spare_total"] > 0 and h["spare_used"] > self.compact_spare_frac * h["spare_total"]
+    def __del__(self):
+        self.close()
 
-    def upkeep(self) -> bool:
-        """Compacts the store if it needs it; call only while no request waits."""
-        if not self.needs_compaction():
-            return False
-        t = time.perf_counter()
-        self.pool.graph.compact()
-        self.compact_ms.append((time.perf_counter() - t) * 1e3)
-        self.compactions += 1
-        return True
+    def _info(self):
+        if not (getattr(self, "_h", None) and self._h.value):
+            return self._final
+        e, c, pend = C.c_int64(), C.c_int64(), C.c_int64()
+        ms = C.c_double()
+        _check(_lib.dsssp_server_info(self._h, C.byref(e), C.byref(c), C.byref(ms), C.byref(pend)), "server_info")
+        return e.value, c.value, ms.value, pend.value
 
-    def check(self, r: Request) -> str | None:
-        """Why the request's batch cannot be applied to its tenant, or None."""
-        ch = np.asarray(r.changes, CHANGE_DTYPE)
-        live = (ch["op"] == 0) | (ch["op"] == 1)
-        n = self.tenants[r.tenant].n
-        cu, cv = ch["u"][live], ch["v"][live]
-        if ((cu < 0) | (cu >= n) | (cv < 0) | (cv >= n)).any():
-            return f"a change names a vertex outside 0..{n - 1}"
-        if ((ch["op"] == 1) & (ch["w"] < 0)).any():
-            return "an insertion has a negative weight"
-        return None
+    @property
+    def epochs(self) -> int:
+        return self._info()[0]
+
+    @property
+    def compactions(self) -> int:
+        return self._info()[1]
 
     def tree(self, tenant: int):
-        return self.pool.tree_read(self.slot[tenant])
+        t = self.tenants[tenant]
+        p = np.empty(t.n, np.int32)
+        d = np.empty(t.n, np.int64)
+        _check(_lib.dsssp_server_tree_read(self._h, int(tenant), p.ctypes.data, d.ctypes.data), "server_tree_read")
+        return p, d
 
-    def serve(self, requests, record: bool = False, realtime: bool = True):
-        """Serves the requests (sorted by arrival); returns them with epoch, done time and
-        latency filled in.  realtime=False ignores arrival gaps (saturated server)."""
+    def serve(self, requests, record: bool = False, realtime: bool = True, timeout_s: float = 600.0):
+        """Submits the requests (sorted by arrival) and returns them with epoch, start and done
+        times (seconds, on the arrival clock) and latency filled in.  realtime submits each
+        request at its arrival time; realtime=False submits all at once (a saturated server)."""
         reqs = sorted(requests, key=lambda r: r.arrival)
         for i, r in enumerate(reqs):
             if r.rid < 0:
                 r.rid = i
-        queues = collections.defaultdict(collections.deque)
-        nxt = 0
-        t0 = time.perf_counter()
-        clock = lambda: time.perf_counter() - t0  # noqa: E731
-        pending = 0
-        while nxt < len(reqs) or pending:
-            now = clock() if realtime else float("inf")
-            while nxt < len(reqs) and reqs[nxt].arrival <= now:
-                r = reqs[nxt]
-                nxt += 1
-                if r.tenant not in self.slot:
-                    r.refused = True
-                    r.done = r.start = r.arrival
-                    continue
-                r.error = self.check(r)
-                if r.error is not None:
-                    r.done = r.start = r.arrival
-                    continue
-                queues[r.tenant].append(r)
-                pending += 1
-            if pending == 0:
-                self.upkeep()  # idle: storage upkeep is off the latency path
-                if nxt < len(reqs):
-                    wait = reqs[nxt].arrival - clock()
-                    if wait > 0:
-                        time.sleep(min(wait, 0.002) if wait > 0.0005 else 0)
-                continue
-            epoch = []
-            for t in sorted(queues, key=lambda t: queues[t][0].arrival if queues[t] else float("inf")):
-                if queues[t]:
-                    epoch.append(queues[t].popleft())
-                    if self.max_epoch_requests and len(epoch) >= self.max_epoch_requests:
+        _check(_lib.dsssp_server_set_record(self._h, 1 if record else 0), "server_set_record")
+        arrays = [np.ascontiguousarray(r.changes, CHANGE_DTYPE) for r in reqs]
+        by_id = {}
+        if realtime:
+            t0 = time.perf_counter()
+            for r, a in zip(reqs, arrays):
+                while True:
+                    wait = r.arrival - (time.perf_counter() - t0)
+                    if wait <= 0:
                         break
-            pending -= len(epoch)
-            start = clock()
-            self.pool.apply([(self.slot[r.tenant], r.changes) for r in epoch])
-            done = clock()
-            for r in epoch:
-                r.epoch = self.epochs
-                r.start = start
-                r.done = done
-                if record:
-                    r.result = self.pool.tree_read(self.slot[r.tenant])
-            self.epochs += 1
+                    if wait > 0.0005:
+                        time.sleep(min(wait - 0.0002, 0.002))
+                rid = C.c_int64()
+                _check(_lib.dsssp_submit(self._h, int(r.tenant), a.ctypes.data if len(a) else None, len(a),
+                                         C.byref(rid)), "submit")
+                by_id[rid.value] = r
+        elif reqs:
+            ten = np.asarray([r.tenant for r in reqs], np.int32)
+            sizes = np.asarray([len(a) for a in arrays], np.int64)
+            ids = np.empty(len(reqs), np.int64)
+            _check(_lib.dsssp_submit_many(self._h, len(reqs), ten.ctypes.data, _ptrs(arrays), sizes.ctypes.data,
+                                          ids.ctypes.data), "submit_many")
+            by_id = {int(i): r for i, r in zip(ids, reqs)}
+        _check(_lib.dsssp_server_drain(self._h, int(timeout_s * 1000)), "server_drain")
+        buf = (RequestInfo * 256)()
+        cnt = C.c_int32()
+        left = len(by_id)
+        while left:
+            _check(_lib.dsssp_poll(self._h, buf, 256, 100, C.byref(cnt)), "poll")
+            for info in buf[: cnt.value]:
+                r = by_id[info.id]
+                left -= 1
+                # the native clock starts with the server: keep each request on its own
+                # arrival clock and carry over the native intervals
+                r.epoch = int(info.epoch)
+                r.start = r.arrival + (info.start_us - info.arrival_us) * 1e-6
+                r.done = r.arrival + (info.done_us - info.arrival_us) * 1e-6
+                r.refused = info.status == REFUSED
+                r.error = None if info.status in (0, REFUSED) else info.error.decode(errors="replace")
+                if record and info.status == 0:
+                    t = self.tenants[r.tenant]
+                    p = np.empty(t.n, np.int32)
+                    d = np.empty(t.n, np.int64)
+                    _check(_lib.dsssp_server_result(self._h, info.id, p.ctypes.data, d.ctypes.data), "server_result")
+                    r.result = (p, d)
         return reqs
 
 

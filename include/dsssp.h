@@ -172,6 +172,10 @@ int dsssp_debug_set(dsssp_graph* g, int32_t what, int64_t value);
  * *first_bad the least violating vertex (-1 if none); either may be NULL. */
 int dsssp_tree_validate(dsssp_graph* g, int64_t* violations, int64_t* roots, int32_t* first_bad);
 
+/* Reads parent and dist of vertices [first, first + count) into caller arrays of count
+ * entries (the part of a pooled store that belongs to one graph). */
+int dsssp_tree_read_range(dsssp_graph* g, int32_t first, int32_t count, int32_t* parent, int64_t* dist);
+
 /* Reads back only the part of the tree the last batch may have changed: every vertex that
  * the batch cut off or whose distance it lowered (a superset of the vertices whose parent or
  * distance differs from before the batch), in no particular order.  vertex/parent/dist get
@@ -340,6 +344,98 @@ int dsssp_gen_changes(int32_t n, int64_t m, const int32_t* eu, const int32_t* ev
 int dsssp_gen_changes_ref(int32_t n, int64_t m, const int32_t* eu, const int32_t* ev,
                           const int32_t* ew, int64_t num_changes, int32_t ins_pct, int32_t wlo,
                           int32_t whi, uint64_t seed, dsssp_change** changes);
+
+/* ---- batching: a pooled graph store ------------------------------------------------
+ * Many graphs side by side in one engine graph (graph i owns ids [off[i], off[i] + n[i])):
+ * one launch sequence applies a set of batches, at most one per graph, and each graph's
+ * result equals applying its batch alone.  Graph-local vertex ids throughout; the pool
+ * validates every batch against its graph (DSSSP_E_BAD_VERTEX / DSSSP_E_BAD_WEIGHT, nothing
+ * applied).  No counterpart in the reference, which updates one graph per process run. */
+typedef struct dsssp_pool dsssp_pool;
+int dsssp_pool_create(int32_t count, const int32_t* n, const int64_t* m, const int32_t* const* u,
+                      const int32_t* const* v, const int32_t* const* w, const dsssp_opts* o,
+                      dsssp_pool** out);
+void dsssp_pool_destroy(dsssp_pool* p);
+/* The underlying engine graph (options, snapshots, statistics); owned by the pool. */
+dsssp_graph* dsssp_pool_graph(dsssp_pool* p);
+/* count + 1 offsets of the graphs in the pool's id space. */
+int dsssp_pool_offsets(const dsssp_pool* p, int64_t* offsets);
+/* sources[i] = source of graph i (local id). */
+int dsssp_pool_tree_compute(dsssp_pool* p, const int32_t* sources, dsssp_stats* st);
+/* parent[i], dist[i] = tree of graph i (local ids, parent -1 = unreachable). */
+int dsssp_pool_forest_load(dsssp_pool* p, const int32_t* const* parent, const int64_t* const* dist);
+/* The union batch of nb batches (graphs[b] gets batches[b] of sizes[b] records) written to
+ * out (cap records); *k = its size.  out may be NULL to validate and size it only. */
+int dsssp_pool_union(dsssp_pool* p, int32_t nb, const int32_t* graphs, const dsssp_change* const* batches,
+                     const int64_t* sizes, dsssp_change* out, int64_t cap, int64_t* k);
+/* Applies the union batch of nb batches in one launch sequence and waits for it. */
+int dsssp_pool_apply(dsssp_pool* p, int32_t nb, const int32_t* graphs, const dsssp_change* const* batches,
+                     const int64_t* sizes, dsssp_stats* st);
+/* The tree of one graph (n[graph] entries, local ids). */
+int dsssp_pool_tree_read(dsssp_pool* p, int32_t graph, int32_t* parent, int64_t* dist);
+/* Device bytes the engine needs for a graph of n vertices and m undirected edges (admission). */
+int64_t dsssp_estimate_footprint(int32_t n, int64_t m, int32_t slack_pct, int32_t slack_min);
+
+/* ---- serving: a request loop with continuous batching ----------------------------
+ * Tenants are admitted in order while their estimated footprint fits memory_budget and live
+ * in one pool.  dsssp_submit queues a request and returns; a worker thread runs epochs back to
+ * back, each taking the oldest waiting request of every tenant (oldest first, at most
+ * max_epoch_requests) and applying them as one union batch.  A tenant's requests apply in
+ * arrival order and each result equals applying that batch alone.  While no request waits,
+ * the worker compacts the store once its tombstones exceed compact_dead_frac of the live
+ * entries (< 0: never) or its spare region is more than compact_spare_frac used.  Completed
+ * requests are collected with dsssp_poll.  Submitting, polling and reading are thread-safe. */
+typedef struct dsssp_server dsssp_server;
+typedef struct {
+    int64_t memory_budget;       /* device bytes for tenants; 0 = no limit */
+    int32_t max_epoch_requests;  /* 0 = one request of every waiting tenant */
+    int32_t record;              /* 1 = keep the tenant's tree after each request (dsssp_server_result) */
+    double compact_dead_frac;    /* default 0.25 */
+    double compact_spare_frac;   /* default 0.75 */
+} dsssp_server_opts;
+
+#define DSSSP_REFUSED 1 /* request status: its tenant was not admitted */
+
+typedef struct {
+    int64_t id;
+    int32_t tenant;
+    int32_t status;      /* 0 served; DSSSP_REFUSED; a negative DSSSP_E_* code (error says why) */
+    int64_t epoch;       /* epoch that served it, -1 if none */
+    int64_t changes;     /* records in its batch */
+    double arrival_us;   /* submission, microseconds since the server was created */
+    double start_us;     /* its epoch's start */
+    double done_us;      /* its epoch's end (the result is in the tree) */
+    char error[96];
+} dsssp_request_info;
+
+void dsssp_default_server_opts(dsssp_server_opts* so);
+/* Tenant t: graph (n[t], m[t], u[t], v[t], w[t]) with source sources[t]; trees are computed
+ * on the device before the worker starts. */
+int dsssp_server_create(int32_t count, const int32_t* n, const int64_t* m, const int32_t* const* u,
+                        const int32_t* const* v, const int32_t* const* w, const int32_t* sources,
+                        const dsssp_server_opts* so, const dsssp_opts* o, dsssp_server** out);
+/* Finishes the queued requests, stops the worker and frees everything. */
+void dsssp_server_destroy(dsssp_server* s);
+/* Pool graph of a tenant, -1 if it was not admitted. */
+int dsssp_server_slot(const dsssp_server* s, int32_t tenant);
+/* Queues a copy of the batch; *id identifies the request in dsssp_poll. */
+int dsssp_submit(dsssp_server* s, int32_t tenant, const dsssp_change* changes, int64_t k, int64_t* id);
+/* Queues several requests at one instant (they can share an epoch). */
+int dsssp_submit_many(dsssp_server* s, int32_t count, const int32_t* tenants,
+                      const dsssp_change* const* batches, const int64_t* sizes, int64_t* ids);
+/* Up to cap completed requests (waiting up to wait_ms for the first one). */
+int dsssp_poll(dsssp_server* s, dsssp_request_info* out, int32_t cap, int32_t wait_ms, int32_t* count);
+/* Waits until no request is queued or running; DSSSP_E_TIMEOUT after timeout_ms. */
+int dsssp_server_drain(dsssp_server* s, int32_t timeout_ms);
+/* Record mode: the tenant's tree right after request id (once per request). */
+int dsssp_server_result(dsssp_server* s, int64_t id, int32_t* parent, int64_t* dist);
+/* The tenant's current tree. */
+int dsssp_server_tree_read(dsssp_server* s, int32_t tenant, int32_t* parent, int64_t* dist);
+int dsssp_server_info(dsssp_server* s, int64_t* epochs, int64_t* compactions, double* compact_ms,
+                      int64_t* pending);
+dsssp_pool* dsssp_server_pool(dsssp_server* s);
+/* Switches record mode (0 also drops recorded trees not yet read). */
+int dsssp_server_set_record(dsssp_server* s, int32_t on);
 
 /* Vertex of maximum degree (lowest id on ties) of an edge list. */
 int32_t dsssp_max_degree_vertex(int32_t n, int64_t m, const int32_t* u, const int32_t* v);

@@ -59,8 +59,13 @@ def test_pool_partial_batches_and_forest_load():
                 check_against_oracle(n, u, v, w, ch, 0, p, d, f"graph {i}")
             else:
                 assert np.array_equal(d, trees[i][1]) and np.array_equal(p, trees[i][0])
-        with pytest.raises(ValueError):
+        with pytest.raises(D.DsssspError):  # two batches of one graph in one union
             pool.apply([(1, graphs[1][4]), (1, graphs[1][4])])
+        bad = graphs[2][4].copy()
+        bad["u"][0] = graphs[2][0]  # one past the graph's last vertex
+        with pytest.raises(D.DsssspError) as e:
+            pool.apply([(2, bad)])
+        assert e.value.code == D.E_BAD_VERTEX and "graph 2" in str(e.value)
 
 
 def test_multi_source_distances():

@@ -39,9 +39,10 @@ def test_each_result_same_alone_and_in_the_mix():
     for t, ten in enumerate(tenants):
         for j in range(4):
             reqs.append(Request(t, float(rng.uniform(0, 0.03)), random_batch(rng, ten, int(rng.integers(10, 300)))))
-    # a tiny tombstone threshold makes the server compact in the idle gaps between requests
+    # all requests at once: every epoch mixes several tenants; a tiny tombstone threshold makes
+    # the server compact once it is idle
     with Server(tenants, compact_dead_frac=1e-4) as srv:
-        out = srv.serve(reqs, record=True)
+        out = srv.serve(reqs, record=True, realtime=False)
     assert srv.compactions > 0
     epochs = {}
     for r in out:
