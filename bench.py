@@ -376,6 +376,7 @@ def run_engine(args, dist: Dist) -> int:
     # roofline of the dominant kernel (the persistent update kernel)
     upd_ms = statistics.mean(s.t_update_ms for s in stats)
     upd_bytes = statistics.mean(s.bytes_alg_update for s in stats)
+    eng_bytes = statistics.mean(s.bytes_engine_update for s in stats)
     peak, peak_kind = measured_peak_hbm()
     achieved = upd_bytes / (upd_ms * 1e-3) / 1e9
     s0 = stats[-1]
@@ -424,7 +425,11 @@ def run_engine(args, dist: Dist) -> int:
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": profiled_traffic(args.workload),
                      "kernel": "k_update", "peak_kind": peak_kind, "ms_per_launch": upd_ms,
-                     "alg_bytes_per_launch": upd_bytes},
+                     "alg_bytes_per_launch": upd_bytes,
+                     "alg_model": "per-unit byte model: 16 B per cut-off vertex + 4 B per child, 20 B per frontier "
+                                  "vertex (pulls included) + 16 B per scanned edge, 12 B per lowering atomic",
+                     "engine_bytes_per_launch": eng_bytes,
+                     "achieved_engine_count": eng_bytes / (upd_ms * 1e-3) / 1e9},
         "cpu_baseline": cpu,
         "clocks": clocks,
         "detail": {

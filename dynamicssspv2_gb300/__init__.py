@@ -73,7 +73,8 @@ class Stats(C.Structure):
         (name, C.c_double)
         for name in ("t_step1_ms", "t_inval_ms", "t_relax_ms", "t_update_ms", "t_total_ms", "bytes_alg",
                      "bytes_alg_update")
-    ] + [("advances", C.c_int64), ("tombstoned", C.c_int64), ("graph_launch", C.c_int64)]
+    ] + [("advances", C.c_int64), ("tombstoned", C.c_int64), ("graph_launch", C.c_int64),
+         ("bytes_engine_update", C.c_double)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}

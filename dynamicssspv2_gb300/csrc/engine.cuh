@@ -70,6 +70,7 @@ enum StatIdx {
     ST_LIVE_INS,
     ST_SEED_UPD,    // k_append: distance-lowering seed relaxations
     ST_SEED_FRONT,  // k_append: ends claimed for the first frontier (or the far list)
+    ST_EDGES_PULL,  // adjacency entries scanned by the pulls of cut-off vertices
     ST_COUNT
 };
 

@@ -890,7 +890,7 @@ void fill_stats(const dsssp_graph* g, const Ctl& c, dsssp_stats* st, bool events
                  seed_front = (double)c.stat[ST_SEED_FRONT];
     st->frontier_total = (int64_t)(c.stat[ST_FRONTIER] + c.stat[ST_SEED_FRONT]);
     st->edges_relaxed = (int64_t)(c.stat[ST_EDGES_RELAX] + 2 * c.stat[ST_LIVE_INS]);
-    st->edges_inval = (int64_t)c.stat[ST_EDGES_INV];
+    st->edges_inval = (int64_t)(c.stat[ST_EDGES_INV] + c.stat[ST_EDGES_PULL]);
     st->del_probed = (int64_t)c.stat[ST_DEL_PROBED];
     st->updates = (int64_t)(c.stat[ST_UPDATES] + c.stat[ST_SEED_UPD]);
     st->overflow_entries = (int64_t)c.stat[ST_OVF];
@@ -909,16 +909,26 @@ void fill_stats(const dsssp_graph* g, const Ctl& c, dsssp_stats* st, bool events
     st->advances = (int64_t)c.stat[ST_ADVANCES];
     st->tombstoned = (int64_t)c.stat[ST_TOMBS];
     st->graph_launch = g->pend_graph ? 1 : 0;
-    // algorithmic bytes (byte model: each item is touched once by this algorithm)
-    //   update kernel: per adjacency entry scanned 16 (entry + neighbour state), per work item
-    //   40 (item write + read, row descriptor, owner state), per pushed vertex 20 (push tag,
-    //   degree), per distance-lowering atomic 8, per cut-off vertex 12 (state, tag), per seed
-    //   expanded 8 (list entry, degree), per pointer-jumping pass 12 n
+    // algorithmic bytes.  The update kernel's figure uses the per-unit bytes of the task's
+    // byte model: per cut-off vertex 16 (state write, child-range offsets) + 4 per child, per
+    // frontier vertex 20 (queue id, row offset and length, own state) + 16 per scanned edge
+    // ((col, wt) + neighbour state), per distance-lowering atomic 12 (word, next-frontier
+    // push).  A cut-off vertex's pull counts as a frontier vertex with its scanned edges; the
+    // walk's scans of whole rows to find children are work beyond the model (no credit).
+    const double inv = (double)st->n_invalidated, roots = (double)st->n_roots;
+    const double upd = 16.0 * inv + 4.0 * (inv > roots ? inv - roots : 0.0) +
+                       20.0 * ((double)c.stat[ST_FRONTIER] + inv) +
+                       16.0 * ((double)c.stat[ST_EDGES_RELAX] + (double)c.stat[ST_EDGES_PULL]) +
+                       12.0 * (double)c.stat[ST_UPDATES];
+    //   the engine's own count of what the update kernel touches (reported beside it): per
+    //   adjacency entry scanned 16, per work item 40, per pushed vertex 20, per lowering
+    //   atomic 8, per cut-off vertex 12, per seed expanded 8, per pointer-jumping pass 12 n
     const double n = (double)g->n;
-    double upd = 16.0 * (double)(c.stat[ST_EDGES_RELAX] + c.stat[ST_EDGES_INV]) + 40.0 * (double)st->work_items +
-                 20.0 * (double)c.stat[ST_FRONTIER] + 8.0 * (double)c.stat[ST_UPDATES] +
-                 12.0 * (double)st->n_invalidated + 8.0 * (double)c.seed_count;
-    if (st->pj_passes > 0) upd += n * (12.0 + 12.0 * (double)st->pj_passes);
+    double eng = 16.0 * (double)(c.stat[ST_EDGES_RELAX] + c.stat[ST_EDGES_INV] + c.stat[ST_EDGES_PULL]) +
+                 40.0 * (double)st->work_items + 20.0 * (double)c.stat[ST_FRONTIER] + 8.0 * (double)c.stat[ST_UPDATES] +
+                 12.0 * inv + 8.0 * (double)c.seed_count;
+    if (st->pj_passes > 0) eng += n * (12.0 + 12.0 * (double)st->pj_passes);
+    st->bytes_engine_update = eng;
     //   front kernels: 16 per record (read by each of the three), 48 per insertion (two
     //   descriptor atomics + two entries + hash probe), 56 per deletion (two descriptors, two
     //   prefix lengths, two states, hash slot) + 8 per probed entry + 16 per root; per

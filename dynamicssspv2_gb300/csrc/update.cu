@@ -58,7 +58,7 @@ __shared__ uint2 s_pbuf[kMaxWarps][kBuf];  // (vertex, degree) pushed, not yet e
 
 struct LocalStats {
     unsigned long long edges_relax = 0, edges_inv = 0, updates = 0, dist_ovf = 0, frontier = 0, items = 0,
-                       marked = 0;
+                       marked = 0, edges_pull = 0;
 };
 
 // Grid-wide barrier for a cooperative launch.  The wait is bounded: on timeout the status
@@ -421,7 +421,7 @@ struct PullOp {
         for (int q = 0; q < 4; q++) s[q] = e[q].y >= 0 ? __ldcg(&state[e[q].x]) : kInfState;
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            ls->edges_inv += ok[q] ? 1 : 0;
+            ls->edges_pull += ok[q] ? 1 : 0;
             if (e[q].y < 0 || s[q] == kInfState) continue;
             const unsigned long long nd = (s[q] >> 32) + (unsigned)e[q].y;
             if (nd >= kDistInf) {
@@ -534,19 +534,20 @@ __device__ void run_items(Op& op, const UpdParams& p, const uint2* tl, unsigned 
 
 // Block-reduced statistics: one atomic per block and counter.
 __device__ void flush_stats(Ctl* ctl, const LocalStats& ls) {
-    __shared__ unsigned long long s_acc[7];
-    if (threadIdx.x < 7) s_acc[threadIdx.x] = 0;
+    __shared__ unsigned long long s_acc[8];
+    if (threadIdx.x < 8) s_acc[threadIdx.x] = 0;
     __syncthreads();
-    const unsigned long long v[7] = {ls.edges_relax, ls.edges_inv, ls.updates, ls.dist_ovf,
-                                     ls.frontier, ls.items, ls.marked};
+    const unsigned long long v[8] = {ls.edges_relax, ls.edges_inv, ls.updates, ls.dist_ovf,
+                                     ls.frontier, ls.items, ls.marked, ls.edges_pull};
 #pragma unroll
-    for (int s = 0; s < 7; s++) {
+    for (int s = 0; s < 8; s++) {
         const unsigned long long x = warp_sum_u64(v[s]);
         if (lane_id() == 0 && x) atomicAdd(&s_acc[s], x);
     }
     __syncthreads();
-    const int idx[7] = {ST_EDGES_RELAX, ST_EDGES_INV, ST_UPDATES, ST_DIST_OVF, ST_FRONTIER, ST_ITEMS, ST_INV};
-    if (threadIdx.x < 7 && s_acc[threadIdx.x]) atomicAdd(&ctl->stat[idx[threadIdx.x]], s_acc[threadIdx.x]);
+    const int idx[8] = {ST_EDGES_RELAX, ST_EDGES_INV, ST_UPDATES, ST_DIST_OVF, ST_FRONTIER, ST_ITEMS, ST_INV,
+                        ST_EDGES_PULL};
+    if (threadIdx.x < 8 && s_acc[threadIdx.x]) atomicAdd(&ctl->stat[idx[threadIdx.x]], s_acc[threadIdx.x]);
 }
 
 __device__ void block_max(unsigned long long* dst, unsigned long long x) {

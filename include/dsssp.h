@@ -107,10 +107,15 @@ typedef struct {
     double t_update_ms;        /* the persistent update kernel (CUDA events) */
     double t_total_ms;         /* the whole batch on the device (CUDA events) */
     double bytes_alg;          /* algorithmic bytes of the batch (byte model of the engine) */
-    double bytes_alg_update;   /* the part moved by the persistent update kernel */
+    double bytes_alg_update;   /* the update kernel's algorithmic bytes (per-unit byte model:
+                                  cut-off vertices and children, frontier vertices and their
+                                  scanned edges, lowering atomics) */
     int64_t advances;          /* near-far threshold advances (0 when delta = 0) */
     int64_t tombstoned;        /* adjacency entries the batch's deletions tombstoned */
     int64_t graph_launch;      /* 1 = the batch was replayed from the instantiated CUDA graph */
+    double bytes_engine_update; /* the update kernel's bytes by the engine's own count (all row
+                                   scans of the subtree walk included; bytes_alg_update credits
+                                   only the task byte model's units) */
 } dsssp_stats;
 
 /* ---- engine ------------------------------------------------------------------------ */
