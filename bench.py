@@ -668,6 +668,8 @@ def run_serving(args, dist: Dist) -> int:
         st = summarize(reqs)
         st["offered_load"] = load
         st["offered_requests_per_s"] = load * cap_rate
+        # device certificate of every tenant's tree after this load (untimed)
+        st["certificate_violations"] = srv.validate()["violations"]
         loads.append(st)
     mism = 0
     for t in checked:

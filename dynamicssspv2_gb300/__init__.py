@@ -164,6 +164,7 @@ _sig("dsssp_server_info", C.c_int, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int64
      C.POINTER(C.c_int64))
 _sig("dsssp_server_pool", _P, _P)
 _sig("dsssp_server_set_record", C.c_int, _P, C.c_int32)
+_sig("dsssp_server_validate", C.c_int, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int64))
 _sig("dsssp_apply_batch", C.c_int, _P, _P, C.c_int64, _P, C.POINTER(Stats))
 _sig("dsssp_apply_batch_async", C.c_int, _P, _P, C.c_int64, _P)
 _sig("dsssp_batch_finish", C.c_int, _P, C.POINTER(Stats))
@@ -220,7 +221,7 @@ EXPORTED = [
     "dsssp_estimate_footprint", "dsssp_default_server_opts", "dsssp_server_create", "dsssp_server_destroy",
     "dsssp_server_slot", "dsssp_submit", "dsssp_submit_many", "dsssp_poll", "dsssp_server_drain",
     "dsssp_server_result", "dsssp_server_tree_read", "dsssp_server_info", "dsssp_server_pool",
-    "dsssp_server_set_record",
+    "dsssp_server_set_record", "dsssp_server_validate",
 ]
 
 

@@ -554,6 +554,12 @@ int dsssp_server_info(dsssp_server* s, int64_t* epochs, int64_t* compactions, do
 
 dsssp_pool* dsssp_server_pool(dsssp_server* s) { return s ? s->pool : nullptr; }
 
+int dsssp_server_validate(dsssp_server* s, int64_t* violations, int64_t* roots) {
+    if (!s || !violations) return fail(DSSSP_E_INVAL, "server_validate: bad arguments");
+    std::lock_guard<std::mutex> d(s->dev);
+    return dsssp_tree_validate(s->pool->g, violations, roots, nullptr);
+}
+
 int dsssp_server_set_record(dsssp_server* s, int32_t on) {
     if (!s) return fail(DSSSP_E_INVAL, "server_set_record: NULL server");
     s->record = on ? 1 : 0;

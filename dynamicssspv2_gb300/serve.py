@@ -125,6 +125,12 @@ class Server:
     def compactions(self) -> int:
         return self._info()[1]
 
+    def validate(self) -> dict:
+        """Device certificate of every admitted tenant's tree: {violations, roots}."""
+        bad, roots = C.c_int64(), C.c_int64()
+        _check(_lib.dsssp_server_validate(self._h, C.byref(bad), C.byref(roots)), "server_validate")
+        return {"violations": bad.value, "roots": roots.value}
+
     def tree(self, tenant: int):
         t = self.tenants[tenant]
         p = np.empty(t.n, np.int32)

@@ -439,6 +439,9 @@ int dsssp_server_tree_read(dsssp_server* s, int32_t tenant, int32_t* parent, int
 int dsssp_server_info(dsssp_server* s, int64_t* epochs, int64_t* compactions, double* compact_ms,
                       int64_t* pending);
 dsssp_pool* dsssp_server_pool(dsssp_server* s);
+/* Device certificate (dsssp_tree_validate) of every tenant's tree at once; *roots = one per
+ * admitted tenant when all is well. */
+int dsssp_server_validate(dsssp_server* s, int64_t* violations, int64_t* roots);
 /* Switches record mode (0 also drops recorded trees not yet read). */
 int dsssp_server_set_record(dsssp_server* s, int32_t on);
 

@@ -43,6 +43,7 @@ def test_each_result_same_alone_and_in_the_mix():
     # the server compact once it is idle
     with Server(tenants, compact_dead_frac=1e-4) as srv:
         out = srv.serve(reqs, record=True, realtime=False)
+        assert srv.validate() == {"violations": 0, "roots": len(tenants)}
     assert srv.compactions > 0
     epochs = {}
     for r in out:
