@@ -501,6 +501,8 @@ struct dsssp_graph {
     dsssp_opts o{};
     cudaStream_t stream = nullptr;
     long long cap_total = 0;
+    double mean_w = 1.0;       // mean edge weight (automatic near-far width)
+    long long last_rounds = 0; // relaxation rounds of the last batch or tree computation
     long long entries = 0;     // live adjacency entries
     long long dead = 0;        // tombstoned entries since the last layout
     long long spare_lo = 0;    // first slot of the spare region
@@ -590,19 +592,42 @@ long long cta_item_capacity(long long cap_total, const dsssp_opts& o) {
     return cap_total / o.chunk + cap_total / (o.large_deg > 0 ? o.large_deg : 1) + 64;
 }
 
+// Near-far lists: one entry per vertex at most; allocated when near-far rounds first run.
+int ensure_far(dsssp_graph* g) {
+    DevGraph& d = g->dg;
+    if (d.far_tag) return DSSSP_OK;
+    int rc = dalloc(&d.far0, (size_t)g->n, "far list");
+    if (!rc) rc = dalloc(&d.far1, (size_t)g->n, "far list");
+    if (!rc) rc = dalloc(&d.far_tag, (size_t)g->n, "far tags");
+    if (rc) {
+        dfree(d.far0); dfree(d.far1); dfree(d.far_tag);
+        return rc;
+    }
+    CK(cudaMemsetAsync(d.far_tag, 0, sizeof(unsigned) * (size_t)g->n, g->stream), "far tags");
+    return DSSSP_OK;
+}
+
+// Near-far bucket width of the next batch or tree computation.  delta > 0 is used as given;
+// delta < 0 (automatic) turns near-far rounds on with 8 times the mean edge weight once the
+// last batch or tree computation needed more than kAutoRounds rounds (a high-diameter graph);
+// 0 keeps plain rounds.
+constexpr long long kAutoRounds = 256;
+unsigned long long effective_delta(const dsssp_graph* g) {
+    if (g->o.delta > 0) return (unsigned long long)g->o.delta;
+    if (g->o.delta < 0 && g->last_rounds > kAutoRounds) {
+        const double d = 8.0 * g->mean_w;
+        return d < 1.0 ? 1ull : (unsigned long long)(d + 0.5);
+    }
+    return 0;
+}
+
 int ensure_work(dsssp_graph* g) {
     const long long nt = thread_item_capacity(g->cap_total, g->n, g->o);
     const long long nc = cta_item_capacity(g->cap_total, g->o);
     DevGraph& d = g->dg;
-    if (g->o.delta > 0 && !d.far_tag) {  // near-far lists: one entry per vertex at most
-        int rc = dalloc(&d.far0, (size_t)g->n, "far list");
-        if (!rc) rc = dalloc(&d.far1, (size_t)g->n, "far list");
-        if (!rc) rc = dalloc(&d.far_tag, (size_t)g->n, "far tags");
-        if (rc) {
-            dfree(d.far0); dfree(d.far1); dfree(d.far_tag);
-            return rc;
-        }
-        CK(cudaMemsetAsync(d.far_tag, 0, sizeof(unsigned) * (size_t)g->n, g->stream), "far tags");
+    if (g->o.delta > 0) {
+        const int rc = ensure_far(g);
+        if (rc) return rc;
     }
     if (d.tcap >= nt && d.ccap >= nc && d.rt0) return DSSSP_OK;
     dfree(d.rt0); dfree(d.rt1); dfree(d.rc0); dfree(d.rc1); dfree(d.it); dfree(d.ic);
@@ -826,7 +851,7 @@ UpdParams make_params(const dsssp_graph* g, const int4* chg, long long k, int mo
     p.chunk = g->o.chunk;
     p.bfs_levels = g->o.bfs_levels;
     p.mode = mode;
-    p.delta = g->o.delta > 0 ? (unsigned long long)g->o.delta : 0ull;
+    p.delta = g->dg.far_tag ? effective_delta(g) : 0ull;  // the caller ensured the lists
     p.seedq = g->d_seedq;
     p.srcs = g->d_srcs;
     p.nsrc = 0;
@@ -1128,6 +1153,10 @@ int enqueue_batch(dsssp_graph* g, const int4* d_chg, long long k, cudaStream_t s
     // k_append already claims frontier tags: restart the tag sequence before it could wrap
     // (the mirror holds the round base the last kernel left)
     if (g->h_ctl->round_base > 0xF0000000u) reset_tags(g, g->stream);
+    if (effective_delta(g) > 0) {
+        const int rc = ensure_far(g);
+        if (rc) return rc;
+    }
     const size_t hb = (size_t)(2ull * (unsigned long long)k);
     unsigned long long h = 64;
     while (h < hb) h <<= 1;  // this batch uses the first h slots of the deletion set
@@ -1184,6 +1213,7 @@ int finish_batch(dsssp_graph* g, dsssp_stats* st) {
         g->dead += tombs;
     }
     g->delta_ok = g->h_ctl->status == 0 && g->h_ctl->stat[ST_DIST_OVF] == 0;
+    if (g->h_ctl->status == 0) g->last_rounds = (long long)g->h_ctl->stat[ST_ROUNDS];
     g->delta_lo = g->pend_rb0;
     g->delta_hi = g->h_ctl->round_base;
     g->delta_epoch = g->epoch;
@@ -1222,7 +1252,7 @@ void dsssp_default_opts(dsssp_opts* o) {
     o->timing = 1;
     o->max_rounds = 0;
     o->spare_pct = 12;
-    o->delta = 0;
+    o->delta = -1;
     o->launch_graph = 1;
     o->reserved1 = 0;
 }
@@ -1287,7 +1317,7 @@ static int check_opts(const dsssp_opts& o) {
     if (o.slack_pct < 0 || o.slack_min < 0 || o.small_deg < 4 || o.small_deg > 64 || o.small_deg % 4 ||
         o.large_deg < o.small_deg || o.chunk < 32 ||
         o.bfs_levels < 0 || o.block < 32 || o.block > 256 || o.block % 32 || o.ctas_per_sm < 0 || o.max_rounds < 0 ||
-        o.spare_pct < 0 || o.spare_pct > 400 || o.delta < 0)
+        o.spare_pct < 0 || o.spare_pct > 400 || o.delta < -1)
         return fail(DSSSP_E_INVAL, "invalid dsssp_opts");
     return DSSSP_OK;
 }
@@ -1305,6 +1335,12 @@ int dsssp_graph_create(int32_t n, int64_t m, const int32_t* u, const int32_t* v,
     }
     dsssp_graph* g = new dsssp_graph();
     if (opts) g->o = *opts;
+    if (m > 0) {  // mean weight for the automatic near-far width
+        double sw = 0;
+#pragma omp parallel for reduction(+ : sw)
+        for (int64_t i = 0; i < m; i++) sw += (double)(w[i] > 0 ? w[i] : 0);
+        g->mean_w = sw / (double)m;
+    }
     else dsssp_default_opts(&g->o);
     int rc = check_opts(g->o);
     if (rc) { delete g; return rc; }
@@ -1509,6 +1545,10 @@ int dsssp_tree_compute_multi(dsssp_graph* g, const int32_t* srcs, int32_t k, dss
     k_set_sources<<<blocks_for(nsrc), kThreads, 0, s>>>(g->dg.state, g->n, g->d_srcs, nsrc, g->dg.ctl);
     count_launch(2);
     if (ev) CK(cudaEventRecord(g->ev[1], s), "event");
+    if (effective_delta(g) > 0) {
+        rc = ensure_far(g);
+        if (rc) return rc;
+    }
     UpdParams p = make_params(g, nullptr, 0, 1);
     p.nsrc = nsrc;
     CK(launch_update(p, g->coop_grid, g->o.block, s), "update kernel");
@@ -1517,6 +1557,7 @@ int dsssp_tree_compute_multi(dsssp_graph* g, const int32_t* srcs, int32_t k, dss
     CK(cudaStreamSynchronize(s), "tree compute");
     g->src = uniq[0];
     g->has_tree = g->h_ctl->status == 0;
+    g->last_rounds = (long long)g->h_ctl->stat[ST_ROUNDS];
     g->delta_ok = false;
     g->pend_graph = false;
     fill_stats(g, *g->h_ctl, st, ev, 0, 0);

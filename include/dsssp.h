@@ -72,8 +72,11 @@ typedef struct {
                              rounds; > 0 = a round relaxes only vertices whose distance is below
                              a threshold T, the others wait until the near frontier is empty and
                              T moves to (least waiting distance) + delta.  Same results; far
-                             fewer rounds and relaxations on high-diameter graphs.  Costs 12
-                             bytes per vertex, allocated when first enabled. */
+                             fewer rounds and relaxations on high-diameter graphs.  -1 (the
+                             default) = automatic: near-far with 8 x the mean edge weight once
+                             the last batch or tree computation needed more than 256 rounds,
+                             plain rounds otherwise.  Costs 12 bytes per vertex, allocated when
+                             first used. */
     int32_t launch_graph; /* 1 = a batch's launch sequence (control-block reset, deletion-set
                              reset, the four kernels, the status read) is replayed from an
                              instantiated CUDA graph whose node parameters are updated per

@@ -185,7 +185,7 @@ def test_near_far_same_tree_on_grid(delta):
     ch = D.make_changes(near, pu, np.asarray(dist)[near] - np.asarray(dist)[pu], np.zeros(len(near)))
     ins = D.gen_changes(n, u, v, w, 300, 0, seed=6)
     ch = np.concatenate([ch, ins])
-    p0, d0, st0 = run_engine(n, u, v, w, ch, parent, dist)
+    p0, d0, st0 = run_engine(n, u, v, w, ch, parent, dist, delta=0)
     p1, d1, st1 = run_engine(n, u, v, w, ch, parent, dist, delta=delta)
     check_against_oracle(n, u, v, w, ch, 0, p1, d1, f"near-far delta {delta}")
     assert np.array_equal(d0, d1) and np.array_equal(p0, p1)
@@ -499,3 +499,24 @@ def test_device_certificate_of_the_tree():
         g.tree_load(np.array([0, 0, 4, 2, 3], np.int32), np.array([0, 1, 5, 5, 5], np.int64))
         c = g.validate()
         assert c["violations"] == 3 and c["first_bad"] == 2
+
+
+def test_automatic_near_far_on_a_deep_graph():
+    """delta -1 (the default): plain rounds while batches converge in few rounds, near-far
+    rounds after one that needed more than 256 (a 400 x 40 grid from its corner)."""
+    u, v, w = D.gen_grid(400, 40, 0.0, 0, 1, 20, seed=9)
+    n = 400 * 40
+    with D.Graph(n, u, v, w) as g:
+        assert g.get_opts().delta == -1
+        st = g.tree_compute(0)
+        assert st.advances == 0 and st.rounds > 256
+        ch = D.gen_changes(n, u, v, w, 50, 150, D.INS_LOCAL, 40, 2.0, 0, 0, 1, 20, seed=10)
+        st = g.apply_batch(ch)
+        p, d = g.tree_read()
+        assert st.advances > 0
+        check_against_oracle(n, u, v, w, ch, 0, p, d, "automatic near-far")
+    er = D.gen_er(5000, 20000, 1, 100, 11)
+    with D.Graph(5000, *er) as g:
+        assert g.tree_compute(0).rounds < 256
+        st = g.apply_batch(D.gen_changes(5000, *er, 200, 200, seed=12))
+        assert st.advances == 0
