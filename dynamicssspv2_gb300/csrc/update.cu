@@ -299,6 +299,29 @@ __device__ __forceinline__ void far_push(const UpdParams& p, const Far& f, bool 
     if (pred) f.list[base + __popc(mask & ((1u << lane) - 1u))] = c;
 }
 
+// Appends c[q] for every pred[q] of every lane to the far list with one atomic per warp
+// (warp-collective; the far tags are already claimed).
+__device__ __forceinline__ void far_append4(const UpdParams& p, const Far& f, const bool (&pred)[4],
+                                            const unsigned (&c)[4]) {
+    unsigned cnt = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) cnt += pred[q] ? 1u : 0u;
+    if (!__any_sync(kFull, cnt != 0)) return;
+    const unsigned incl = warp_incl_scan(cnt);
+    const unsigned total = __shfl_sync(kFull, incl, 31);
+    unsigned base = 0;
+    if (lane_id() == 31) base = atomicAdd(f.cnt, total);
+    base = __shfl_sync(kFull, base, 31);
+    if ((unsigned long long)base + total > f.cap) {  // cannot happen: one entry per vertex
+        if (lane_id() == 31) set_status(p.g.ctl, -4);
+        return;
+    }
+    unsigned at = base + incl - cnt;
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+        if (pred[q]) f.list[at++] = c[q];
+}
+
 // ---- per-edge operations ---------------------------------------------------------------
 // visit4 handles up to four adjacency entries per lane and is called by all 32 lanes.
 
@@ -327,19 +350,53 @@ struct RelaxOp {
         unsigned long long cur[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) cur[q] = e[q].y >= 0 ? __ldcg(&state[e[q].x]) : 0ull;
+        // The lane's four offers go out before any result is used, then its claims: two
+        // memory latencies for the four edges instead of two per improving edge.
+        unsigned long long old[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            bool push = false;
             const unsigned long long nd = du + (unsigned)e[q].y;
-            if (e[q].y >= 0) push = relax_to(p->g, p->epoch, (unsigned)e[q].x, nd, u, e[q].y, cur[q], *ls);
-            const bool later = push && nd >= far.T;
-            far_push(*p, far, later, (unsigned)e[q].x);
-            int deg;
-            const bool doit = claim_with_deg(*p, push && !later, (unsigned)e[q].x, tag, deg);
+            const bool offer = e[q].y > 0 && nd < kDistInf && ((nd << 32) | u) < cur[q];
+            if (e[q].y > 0 && nd >= kDistInf && cur[q] == kInfState) ls->dist_ovf++;
+            old[q] = offer ? atomicMin(&state[e[q].x], (nd << 32) | u) : 0ull;
+        }
+        bool push[4], later[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const unsigned long long nd = du + (unsigned)e[q].y;
+            const unsigned long long cand = (nd << 32) | u;
+            push[q] = false;
+            if (e[q].y > 0 && nd < kDistInf && cand < cur[q]) {
+                push[q] = (old[q] >> 32) > nd;
+                if (push[q]) ls->updates++;
+                else if (old[q] > cand && p->g.chg_tag) p->g.chg_tag[e[q].x] = p->epoch;
+            } else if (e[q].y == 0) {  // zero weight: strict improvements only (compare-and-swap)
+                push[q] = relax_to(p->g, p->epoch, (unsigned)e[q].x, nd, u, 0, cur[q], *ls);
+            }
+            later[q] = push[q] && nd >= far.T;
+        }
+        unsigned ftag[4], ctag[4];
+        int deg[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const unsigned c = (unsigned)e[q].x;
+            const bool want = push[q] && !later[q];
+            ftag[q] = later[q] ? atomicExch(&far.tag[c], far.gen) : far.gen;
+            deg[q] = want ? p->g.rows[c].deg : 0;
+            ctag[q] = want ? atomicExch(&p->g.push_tag[c], tag) : tag;
+        }
+        bool fl[4];
+        unsigned fc[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            fl[q] = later[q] && ftag[q] != far.gen;
+            fc[q] = (unsigned)e[q].x;
+            const bool doit = push[q] && !later[q] && ctag[q] != tag;
             ls->frontier += doit ? 1 : 0;
-            pb.add(doit, (unsigned)e[q].x, deg);
+            pb.add(doit, (unsigned)e[q].x, deg[q]);
             ls->edges_relax += ok[q] ? 1 : 0;
         }
+        far_append4(*p, far, fl, fc);
         pb.flush(*p, out, *ls);
     }
 };
@@ -367,16 +424,24 @@ struct MarkOp {
         unsigned long long s[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) s[q] = e[q].y >= 0 ? __ldcg(&state[e[q].x]) : kInfState;
+        // a child is cut off even when already tagged: a root that an insertion of this batch
+        // re-parented onto a vertex of a cut-off subtree must lose that distance.  The four
+        // tag exchanges and degree loads go out before any result is used.
+        unsigned old[4];
+        int deg[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const unsigned c = (unsigned)e[q].x;
-            // a child is cut off even when already tagged: a root that an insertion of this
-            // batch re-parented onto a vertex of a cut-off subtree must lose that distance
             const bool child = e[q].y >= 0 && (unsigned)s[q] == x;
             if (child) state[c] = kInfState;
-            const bool mark = child && atomicExch(&p->g.inv_tag[c], p->epoch) != p->epoch;
+            old[q] = child ? atomicExch(&p->g.inv_tag[c], p->epoch) : p->epoch;
+            deg[q] = child ? p->g.rows[c].deg : 0;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const bool mark = old[q] != p->epoch;
             ls->marked += mark ? 1 : 0;
-            pb.add(mark, c, mark ? p->g.rows[c].deg : 0);
+            pb.add(mark, (unsigned)e[q].x, mark ? deg[q] : 0);
             ls->edges_inv += ok[q] ? 1 : 0;
         }
         pb.flush(*p, out, *ls);
@@ -393,9 +458,10 @@ struct PullOp {
     unsigned long long best;
     bool need;
 
-    // pushes x (pred) to the next round or, at or above the threshold, to the far list
-    __device__ __forceinline__ void route(bool pred, unsigned x) {
-        const bool later = pred && (__ldcg(&p->g.state[x]) >> 32) >= far.T;
+    // pushes x (pred) to the next round or, at or above the threshold, to the far list; d is
+    // x's distance when the caller knows it (its own lowering atomicMin), else kDistInf
+    __device__ __forceinline__ void route(bool pred, unsigned x, unsigned long long d) {
+        const bool later = pred && far.T != ~0ull && (d < kDistInf ? d : __ldcg(&p->g.state[x]) >> 32) >= far.T;
         far_push(*p, far, later, x);
         int deg;
         const bool doit = claim_with_deg(*p, pred && !later, x, tag, deg);
@@ -446,7 +512,7 @@ struct PullOp {
                 ls->updates++;
             }
         }
-        route(valid && (need || improved), x);
+        route(valid && (need || improved), x, improved ? best >> 32 : kDistInf);
     }
     // an item shared by the warp (part of a CTA item)
     __device__ __forceinline__ void end_group(unsigned x) {
@@ -460,7 +526,7 @@ struct PullOp {
                 ls->updates++;
             }
         }
-        route(lane_id() == 0 && (nd || improved), x);
+        route(lane_id() == 0 && (nd || improved), x, improved ? b >> 32 : kDistInf);
     }
 };
 
