@@ -13,9 +13,11 @@
 //   push_tag[n]   u32  round tag of the last frontier push (de-duplication)
 //   jm[n]         u32  pointer-jumping word (ancestor or terminal tag)
 //   invq[n]       u32  vertices cut off directly by a deleted tree edge
-//   work items    8 B  (vertex, chunk): a pushed vertex of degree d becomes ceil(d/te) thread
-//                      items of te edges, or, above large_deg, ceil(d/chunk) CTA items;
-//                      rt/rc = relaxation frontier (double buffer), it/ic = cut-off vertices
+//   work items    16 B (first slot, vertex, count): a pushed vertex of degree d becomes
+//                      ceil(d/te) thread items of te edges, or, above large_deg, ceil(d/chunk)
+//                      CTA items; an item names its adjacency slots itself, so processing it
+//                      needs no row-descriptor load.  rt/rc = relaxation frontier (double
+//                      buffer), it/ic = cut-off vertices
 //   ctl           control block: grid barrier, status word, list counters, statistics, one
 //                 128-byte line per group of fields that different CTAs hit at the same time
 #pragma once
@@ -120,6 +122,17 @@ struct __align__(128) Ctl {
     unsigned long long pad6[8];
 };
 
+// A work item: adjacency slots [lo, lo + cnt) of vertex v's row, as {lo low word, lo high
+// word, v, cnt} (one 16-byte load).
+using Item = uint4;
+
+__device__ __forceinline__ Item make_item(unsigned v, long long lo, unsigned cnt) {
+    return make_uint4((unsigned)lo, (unsigned)((unsigned long long)lo >> 32), v, cnt);
+}
+__device__ __forceinline__ long long item_lo(const Item& it) {
+    return (long long)(((unsigned long long)it.y << 32) | it.x);
+}
+
 struct DevGraph {
     unsigned long long* state;
     RowDesc* rows;
@@ -130,12 +143,12 @@ struct DevGraph {
     unsigned* push_tag;
     unsigned* jm;
     unsigned* invq;
-    uint2* rt0;  // relaxation thread items, double buffer
-    uint2* rt1;
-    uint2* rc0;  // relaxation CTA items, double buffer
-    uint2* rc1;
-    uint2* it;   // cut-off vertices' thread items
-    uint2* ic;   // cut-off vertices' CTA items
+    Item* rt0;  // relaxation thread items, double buffer
+    Item* rt1;
+    Item* rc0;  // relaxation CTA items, double buffer
+    Item* rc1;
+    Item* it;   // cut-off vertices' thread items
+    Item* ic;   // cut-off vertices' CTA items
     unsigned* far0;     // near-far: vertices whose distance is at or above the threshold
     unsigned* far1;
     unsigned* far_tag;  // far-list membership tag (de-duplication)
@@ -215,28 +228,6 @@ __device__ __forceinline__ void warp_append(bool pred, unsigned val, unsigned* l
     if (lane == leader) base = atomicAdd(counter, (unsigned)__popc(mask));
     base = __shfl_sync(0xFFFFFFFFu, base, leader);
     if (pred) list[base + __popc(mask & ((1u << lane) - 1u))] = val;
-}
-
-// Appends items (val, 0..cnt-1) for every lane, one atomic per warp.  Returns false (and
-// appends nothing) if the list would exceed cap.
-__device__ __forceinline__ bool warp_append_chunks(unsigned val, unsigned cnt, uint2* list, unsigned* counter,
-                                                   long long cap) {
-    const unsigned lane = lane_id();
-    unsigned incl = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const unsigned t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-        if (lane >= (unsigned)o) incl += t;
-    }
-    const unsigned total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-    if (total == 0) return true;
-    unsigned base = 0;
-    if (lane == 31) base = atomicAdd(counter, total);
-    base = __shfl_sync(0xFFFFFFFFu, base, 31);
-    if ((long long)base + total > cap) return false;
-    const unsigned first = base + incl - cnt;
-    for (unsigned k = 0; k < cnt; k++) list[first + k] = make_uint2(val, k);
-    return true;
 }
 
 // Adjacency entries are read once per push: streaming loads (evict-first in L1 and L2) keep

@@ -43,10 +43,10 @@ constexpr size_t kOffRows = align256(kOffCtl + sizeof(Ctl));
 constexpr size_t kOffState = align256(kOffRows + sizeof(RowDesc) * kMaxV);
 constexpr size_t kOffTag = align256(kOffState + 8 * kMaxV);
 constexpr size_t kOffRt0 = align256(kOffTag + 4 * kMaxV);
-constexpr size_t kOffRt1 = align256(kOffRt0 + 8 * kTcap);
-constexpr size_t kOffRc0 = align256(kOffRt1 + 8 * kTcap);
-constexpr size_t kOffRc1 = align256(kOffRc0 + 8 * kCcap);
-constexpr size_t kOffSrc = align256(kOffRc1 + 8 * kCcap);
+constexpr size_t kOffRt1 = align256(kOffRt0 + sizeof(Item) * kTcap);
+constexpr size_t kOffRc0 = align256(kOffRt1 + sizeof(Item) * kTcap);
+constexpr size_t kOffRc1 = align256(kOffRc0 + sizeof(Item) * kCcap);
+constexpr size_t kOffSrc = align256(kOffRc1 + sizeof(Item) * kCcap);
 constexpr size_t kScratchBytes = align256(kOffSrc + sizeof(int));
 
 // The work space.  Shared by every call on a device; kept between calls.
@@ -178,10 +178,10 @@ extern "C" int dsssp_sssp_noalloc(int32_t n, int64_t nnz, const int64_t* d_row_o
     p.g.state = reinterpret_cast<unsigned long long*>(base + kOffState);
     p.g.push_tag = reinterpret_cast<unsigned*>(base + kOffTag);
     p.g.adj = const_cast<int2*>(adj);
-    p.g.rt0 = reinterpret_cast<uint2*>(base + kOffRt0);
-    p.g.rt1 = reinterpret_cast<uint2*>(base + kOffRt1);
-    p.g.rc0 = reinterpret_cast<uint2*>(base + kOffRc0);
-    p.g.rc1 = reinterpret_cast<uint2*>(base + kOffRc1);
+    p.g.rt0 = reinterpret_cast<Item*>(base + kOffRt0);
+    p.g.rt1 = reinterpret_cast<Item*>(base + kOffRt1);
+    p.g.rc0 = reinterpret_cast<Item*>(base + kOffRc0);
+    p.g.rc1 = reinterpret_cast<Item*>(base + kOffRc1);
     p.g.tcap = kTcap;
     p.g.ccap = kCcap;
     p.g.n = n;

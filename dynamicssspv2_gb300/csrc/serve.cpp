@@ -113,10 +113,10 @@ extern "C" {
 
 int64_t dsssp_estimate_footprint(int32_t n, int64_t m, int32_t slack_pct, int32_t slack_min) {
     // per vertex: state 8, row descriptor 16, sorted-prefix length 4, four tags 16, cut-off
-    // root list 4, three thread-item lists 24; per slot: entry 8, twin 4, three thread-item
-    // lists (8 bytes per small_deg slots); plus a margin for the batch buffers
+    // root list 4, three thread-item lists 48; per slot: entry 8, twin 4, three thread-item
+    // lists (16 bytes per small_deg slots); plus a margin for the batch buffers
     const double slots = 2.0 * (double)m * (1.0 + slack_pct / 100.0) + (double)n * slack_min;
-    return (int64_t)((double)n * (8 + 16 + 4 + 16 + 4 + 24) + slots * (8 + 4 + 3 * 8 / 4.0) + (1 << 20));
+    return (int64_t)((double)n * (8 + 16 + 4 + 16 + 4 + 48) + slots * (8 + 4 + 3 * 16 / 4.0) + (1 << 20));
 }
 
 int dsssp_pool_create(int32_t count, const int32_t* n, const int64_t* m, const int32_t* const* u,

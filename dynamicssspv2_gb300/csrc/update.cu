@@ -45,16 +45,21 @@ namespace {
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr unsigned kSpinLimit = 1u << 20;  // polls of ~1 us: a barrier gives up after ~1 s
 constexpr int kMaxWarps = 8;               // update kernel blocks have at most 256 threads
-constexpr int kBuf = 256;                  // per-warp push buffer (vertex, degree) entries
+constexpr int kBuf = 176;                  // per-warp push buffer entries (16 bytes each: four
+                                           // CTAs of the update kernel stay within 100 KB of
+                                           // shared memory, which leaves the L1 its 156 KB)
+constexpr int kListRegion = 512;           // per-warp u32 staging of the batch front kernels
 constexpr int kAddsPerCheck = 128;         // entries a warp may add between two flush checks
                                            // (visit4: 4 adds of up to 32 lanes)
+static_assert(kBuf > kAddsPerCheck, "a push buffer must take one visit's adds after a check");
 constexpr unsigned kSoloWaves = 2;         // a step of at most this many CTA-waves of items
                                            // runs on CTA 0 alone (block barriers)
 constexpr int kSoloSteps = 256;            // consecutive solo steps before the grid re-syncs
 
 __shared__ unsigned s_nbar;        // grid barriers this CTA has passed
 __shared__ unsigned s_spin_limit;  // polls before a grid barrier gives up
-__shared__ uint2 s_pbuf[kMaxWarps][kBuf];  // (vertex, degree) pushed, not yet expanded
+__shared__ uint4 s_pbuf[kMaxWarps][kBuf];  // (vertex, degree, row start) pushed, not yet expanded
+__shared__ unsigned s_wlist[kMaxWarps][kListRegion];  // k_delete / k_append list staging
 
 struct LocalStats {
     unsigned long long edges_relax = 0, edges_inv = 0, updates = 0, dist_ovf = 0, frontier = 0, items = 0,
@@ -133,27 +138,16 @@ __device__ __forceinline__ bool relax_to(const DevGraph& g, unsigned epoch, unsi
 
 // Destination of pushed vertices: a thread-item list and a CTA-item list with counters.
 struct Out {
-    uint2* tl;
+    Item* tl;
     unsigned* tcnt;
     long long tcap;
-    uint2* cl;
+    Item* cl;
     unsigned* ccnt;
     long long ccap;
 };
 
-// Splits the vertex each lane holds (degree deg, 0 = none) into work items (warp-collective).
-__device__ __forceinline__ void expand(unsigned v, int deg, const UpdParams& p, const Out& o, LocalStats& ls) {
-    const bool heavy = deg > p.large_deg;
-    const unsigned nt = (!heavy && deg > 0) ? (unsigned)((deg + p.te - 1) / p.te) : 0u;
-    const unsigned nc = heavy ? (unsigned)((deg + p.chunk - 1) / p.chunk) : 0u;
-    const bool ok1 = warp_append_chunks(v, nt, o.tl, o.tcnt, o.tcap);
-    const bool ok2 = warp_append_chunks(v, nc, o.cl, o.ccnt, o.ccap);
-    if (!(ok1 && ok2) && lane_id() == 0) set_status(p.g.ctl, -4 /* work list capacity: internal error */);
-    ls.items += nt + nc;
-}
-
 // Work items of the entries a lane holds in a push buffer (entries lane, lane + 32, ...).
-__device__ __forceinline__ void buf_counts(const uint2* buf, int count, const UpdParams& p, unsigned& nt,
+__device__ __forceinline__ void buf_counts(const uint4* buf, int count, const UpdParams& p, unsigned& nt,
                                            unsigned& nc) {
     nt = nc = 0;
     for (int e = (int)lane_id(); e < count; e += 32) {
@@ -164,17 +158,16 @@ __device__ __forceinline__ void buf_counts(const uint2* buf, int count, const Up
 }
 
 // Writes those items from list positions ft (thread items) and fc (CTA items) on.
-__device__ __forceinline__ void buf_write(const uint2* buf, int count, const UpdParams& p, const Out& o, unsigned ft,
+__device__ __forceinline__ void buf_write(const uint4* buf, int count, const UpdParams& p, const Out& o, unsigned ft,
                                           unsigned fc) {
     for (int e = (int)lane_id(); e < count; e += 32) {
-        const uint2 x = buf[e];
+        const uint4 x = buf[e];
         const int deg = (int)x.y;
+        const long long start = (long long)(((unsigned long long)x.w << 32) | x.z);
         if (deg > p.large_deg) {
-            const unsigned n = (unsigned)((deg + p.chunk - 1) / p.chunk);
-            for (unsigned k = 0; k < n; k++) o.cl[fc++] = make_uint2(x.x, k);
+            for (int k = 0; k < deg; k += p.chunk) o.cl[fc++] = make_item(x.x, start + k, (unsigned)min(p.chunk, deg - k));
         } else if (deg > 0) {
-            const unsigned n = (unsigned)((deg + p.te - 1) / p.te);
-            for (unsigned k = 0; k < n; k++) o.tl[ft++] = make_uint2(x.x, k);
+            for (int k = 0; k < deg; k += p.te) o.tl[ft++] = make_item(x.x, start + k, (unsigned)min(p.te, deg - k));
         }
     }
 }
@@ -188,17 +181,20 @@ __device__ __forceinline__ unsigned warp_incl_scan(unsigned x) {
     return x;
 }
 
-// Per-warp shared-memory buffer of pushed (vertex, degree).  Entries are split into work
+// Per-warp shared-memory buffer of pushed (vertex, degree, row start).  Entries are split into work
 // items when the buffer is nearly full (one list-counter atomic per warp for up to kBuf
 // vertices) and at the end of a phase (one atomic per CTA): the list counters are single
 // words that every CTA appends to, so their atomics are kept few.
 struct PushBuf {
-    uint2* buf;
+    uint4* buf;
     int count;  // warp-uniform
 
-    __device__ __forceinline__ void add(bool pred, unsigned v, int deg) {
+    // pushes v with its row (start, deg) for every lane with pred
+    __device__ __forceinline__ void add(bool pred, unsigned v, const RowDesc& rd) {
         const unsigned mask = __ballot_sync(kFull, pred);
-        if (pred) buf[count + __popc(mask & ((1u << lane_id()) - 1u))] = make_uint2(v, (unsigned)deg);
+        if (pred)
+            buf[count + __popc(mask & ((1u << lane_id()) - 1u))] =
+                make_uint4(v, (unsigned)rd.deg, (unsigned)rd.start, (unsigned)((unsigned long long)rd.start >> 32));
         count += __popc(mask);
         __syncwarp();
     }
@@ -261,14 +257,20 @@ struct PushBuf {
     }
 };
 
-// Claims c for the next frontier; the degree load is issued alongside the claim.
-__device__ __forceinline__ bool claim_with_deg(const UpdParams& p, bool want, unsigned c, unsigned tag, int& deg) {
-    deg = 0;
+// Claims c for the next frontier; its row descriptor (for the work items) is loaded alongside
+// the claim.
+__device__ __forceinline__ bool claim_with_row(const UpdParams& p, bool want, unsigned c, unsigned tag, RowDesc& rd) {
+    rd = RowDesc{0, 0, 0};
     if (!want) return false;
-    const int d = p.g.rows[c].deg;
+    const RowDesc r = p.g.rows[c];
     const bool won = atomicExch(&p.g.push_tag[c], tag) != tag;
-    deg = d;
+    rd = r;
     return won;
+}
+
+// The row descriptor of v when pred holds (an empty row otherwise).
+__device__ __forceinline__ RowDesc row_if(const UpdParams& p, bool pred, unsigned v) {
+    return pred ? p.g.rows[v] : RowDesc{0, 0, 0};
 }
 
 // Near-far ordering: pushes whose new distance is at or above the threshold T go to a far
@@ -351,13 +353,16 @@ struct RelaxOp {
 #pragma unroll
         for (int q = 0; q < 4; q++) cur[q] = e[q].y >= 0 ? __ldcg(&state[e[q].x]) : 0ull;
         // The lane's four offers go out before any result is used, then its claims: two
-        // memory latencies for the four edges instead of two per improving edge.
+        // memory latencies for the four edges instead of two per improving edge.  The
+        // adjacency loads above were issued alongside the load of du (an unreachable u offers
+        // nothing).
+        const bool live = du < kDistInf;
         unsigned long long old[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const unsigned long long nd = du + (unsigned)e[q].y;
-            const bool offer = e[q].y > 0 && nd < kDistInf && ((nd << 32) | u) < cur[q];
-            if (e[q].y > 0 && nd >= kDistInf && cur[q] == kInfState) ls->dist_ovf++;
+            const bool offer = live && e[q].y > 0 && nd < kDistInf && ((nd << 32) | u) < cur[q];
+            if (live && e[q].y > 0 && nd >= kDistInf && cur[q] == kInfState) ls->dist_ovf++;
             old[q] = offer ? atomicMin(&state[e[q].x], (nd << 32) | u) : 0ull;
         }
         bool push[4], later[4];
@@ -366,23 +371,23 @@ struct RelaxOp {
             const unsigned long long nd = du + (unsigned)e[q].y;
             const unsigned long long cand = (nd << 32) | u;
             push[q] = false;
-            if (e[q].y > 0 && nd < kDistInf && cand < cur[q]) {
+            if (live && e[q].y > 0 && nd < kDistInf && cand < cur[q]) {
                 push[q] = (old[q] >> 32) > nd;
                 if (push[q]) ls->updates++;
                 else if (old[q] > cand && p->g.chg_tag) p->g.chg_tag[e[q].x] = p->epoch;
-            } else if (e[q].y == 0) {  // zero weight: strict improvements only (compare-and-swap)
+            } else if (live && e[q].y == 0) {  // zero weight: strict improvements only (compare-and-swap)
                 push[q] = relax_to(p->g, p->epoch, (unsigned)e[q].x, nd, u, 0, cur[q], *ls);
             }
             later[q] = push[q] && nd >= far.T;
         }
         unsigned ftag[4], ctag[4];
-        int deg[4];
+        RowDesc rd[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const unsigned c = (unsigned)e[q].x;
             const bool want = push[q] && !later[q];
             ftag[q] = later[q] ? atomicExch(&far.tag[c], far.gen) : far.gen;
-            deg[q] = want ? p->g.rows[c].deg : 0;
+            rd[q] = row_if(*p, want, c);
             ctag[q] = want ? atomicExch(&p->g.push_tag[c], tag) : tag;
         }
         bool fl[4];
@@ -393,8 +398,8 @@ struct RelaxOp {
             fc[q] = (unsigned)e[q].x;
             const bool doit = push[q] && !later[q] && ctag[q] != tag;
             ls->frontier += doit ? 1 : 0;
-            pb.add(doit, (unsigned)e[q].x, deg[q]);
-            ls->edges_relax += ok[q] ? 1 : 0;
+            pb.add(doit, (unsigned)e[q].x, rd[q]);
+            ls->edges_relax += ok[q] && live ? 1 : 0;
         }
         far_append4(*p, far, fl, fc);
         pb.flush(*p, out, *ls);
@@ -428,20 +433,20 @@ struct MarkOp {
         // re-parented onto a vertex of a cut-off subtree must lose that distance.  The four
         // tag exchanges and degree loads go out before any result is used.
         unsigned old[4];
-        int deg[4];
+        RowDesc rd[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const unsigned c = (unsigned)e[q].x;
             const bool child = e[q].y >= 0 && (unsigned)s[q] == x;
             if (child) state[c] = kInfState;
             old[q] = child ? atomicExch(&p->g.inv_tag[c], p->epoch) : p->epoch;
-            deg[q] = child ? p->g.rows[c].deg : 0;
+            rd[q] = row_if(*p, child, c);
         }
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const bool mark = old[q] != p->epoch;
             ls->marked += mark ? 1 : 0;
-            pb.add(mark, (unsigned)e[q].x, mark ? deg[q] : 0);
+            pb.add(mark, (unsigned)e[q].x, rd[q]);
             ls->edges_inv += ok[q] ? 1 : 0;
         }
         pb.flush(*p, out, *ls);
@@ -463,10 +468,10 @@ struct PullOp {
     __device__ __forceinline__ void route(bool pred, unsigned x, unsigned long long d) {
         const bool later = pred && far.T != ~0ull && (d < kDistInf ? d : __ldcg(&p->g.state[x]) >> 32) >= far.T;
         far_push(*p, far, later, x);
-        int deg;
-        const bool doit = claim_with_deg(*p, pred && !later, x, tag, deg);
+        RowDesc rd;
+        const bool doit = claim_with_row(*p, pred && !later, x, tag, rd);
         ls->frontier += doit ? 1 : 0;
-        pb.add(doit, x, deg);
+        pb.add(doit, x, rd);
         pb.flush(*p, out, *ls);
     }
 
@@ -541,59 +546,50 @@ __device__ __forceinline__ bool small_step(unsigned nt, unsigned nc) {
 // items (te edges each) in one grid-stride wave, over CTAs cta, cta + 1, ... of ncta (the
 // whole grid, or CTA 0 alone for a small step).
 template <class Op>
-__device__ void run_items(Op& op, const UpdParams& p, const uint2* tl, unsigned nt, const uint2* cl, unsigned nc,
+__device__ void run_items(Op& op, const UpdParams& p, const Item* tl, unsigned nt, const Item* cl, unsigned nc,
                           unsigned cta, unsigned ncta) {
-    const RowDesc* rows = p.g.rows;
     const unsigned lane = lane_id();
     const unsigned gtid = cta * blockDim.x + threadIdx.x;
     const unsigned nthreads = ncta * blockDim.x;
     for (unsigned t = cta; t < nc; t += ncta) {
-        const uint2 it = __ldcg(&cl[t]);
-        const RowDesc rd = rows[it.x];
-        const unsigned long long du = __shfl_sync(kFull, op.prep(it.x), 0);
+        const Item it = __ldcg(&cl[t]);
+        const unsigned long long du = __shfl_sync(kFull, op.prep(it.z), 0);
         if (op.skip(du)) continue;
-        const long long lo = (long long)it.y * p.chunk;
-        const long long hi = min((long long)rd.deg, lo + p.chunk);
-        op.begin_group(it.x);
+        const long long lo = item_lo(it), hi = lo + (long long)it.w;
+        op.begin_group(it.z);
         for (long long b = lo; b < hi; b += 4LL * blockDim.x) {
             long long j[4];
             bool ok[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-                const long long idx = b + (long long)q * blockDim.x + threadIdx.x;
-                ok[q] = idx < hi;
-                j[q] = rd.start + idx;
+                j[q] = b + (long long)q * blockDim.x + threadIdx.x;
+                ok[q] = j[q] < hi;
             }
-            op.visit4(it.x, du, j, ok);
+            op.visit4(it.z, du, j, ok);
         }
-        op.end_group(it.x);
+        op.end_group(it.z);
     }
+    // thread items: the item names its slots, so the adjacency loads go out alongside the
+    // load of the vertex's own state (prep)
     for (unsigned base = gtid - lane; base < nt; base += nthreads) {
         const unsigned i = base + lane;
         const bool has = i < nt;
-        const uint2 it = has ? __ldcg(&tl[i]) : make_uint2(0u, 0u);
-        RowDesc rd;
-        rd.start = 0;
-        rd.deg = 0;
-        rd.cap = 0;
-        if (has) rd = rows[it.x];
-        const unsigned long long du = has ? op.prep(it.x) : kDistInf;
-        const bool live = has && !op.skip(du);
-        const long long lo = (long long)it.y * p.te;
-        const long long hi = live ? min((long long)rd.deg, lo + p.te) : lo;
-        op.begin_lane(it.x);
-        for (int b = 0; b < p.te; b += 4) {
+        const Item it = has ? __ldcg(&tl[i]) : make_uint4(0u, 0u, 0u, 0u);
+        const unsigned long long du = has ? op.prep(it.z) : kDistInf;
+        const long long lo = item_lo(it);
+        const int cnt = (int)it.w;
+        op.begin_lane(it.z);
+        for (int b = 0; b < p.te; b += 4) {  // warp-uniform trip count (visit4 is warp-collective)
             long long j[4];
             bool ok[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-                const long long idx = lo + b + q;
-                ok[q] = idx < hi;
-                j[q] = rd.start + idx;
+                ok[q] = b + q < cnt;
+                j[q] = lo + b + q;
             }
-            op.visit4(it.x, du, j, ok);
+            op.visit4(it.z, du, j, ok);
         }
-        op.end_lane(it.x, live);
+        op.end_lane(it.z, has && !op.skip(du));
     }
     op.finish();
 }
@@ -797,8 +793,7 @@ __global__ void k_delete(UpdParams p) {
     const long long nthreads = (long long)gridDim.x * blockDim.x;
     unsigned long long probed = 0, roots = 0, dead = 0;
     const unsigned lane = lane_id();
-    constexpr int kRegion = 2 * kBuf;  // u32 entries of a warp's push-buffer storage
-    WarpList roots_list{reinterpret_cast<unsigned*>(s_pbuf[threadIdx.x >> 5]), kRegion, 0};
+    WarpList roots_list{s_wlist[threadIdx.x >> 5], kListRegion, 0};
     for (long long base = (long long)blockIdx.x * blockDim.x + threadIdx.x - lane; base < p.k; base += nthreads) {
         const long long i = base + lane;
         const int4 c = i < p.k ? p.chg[i] : make_int4(0, 0, 0, -1);
@@ -861,9 +856,9 @@ __global__ void k_append(UpdParams p) {
     // near-far: a batch starts with threshold 0, so every seed waits in the far list
     const bool nf = p.delta != 0 && g.far0 != nullptr && g.far1 != nullptr && g.far_tag != nullptr;
     const unsigned long long T = nf ? 0ull : ~0ull;
-    // seeds are staged per warp (half of the warp's push-buffer storage each for near and far)
-    unsigned* region = reinterpret_cast<unsigned*>(s_pbuf[threadIdx.x >> 5]);
-    WarpList near_list{region, kBuf, 0}, far_list{region + kBuf, kBuf, 0};
+    // seeds are staged per warp (half of the warp's staging region each for near and far)
+    unsigned* region = s_wlist[threadIdx.x >> 5];
+    WarpList near_list{region, kListRegion / 2, 0}, far_list{region + kListRegion / 2, kListRegion / 2, 0};
     const unsigned seed_cap = (unsigned)min(2 * p.k, (long long)g.n);  // distinct claimed ends
     LocalStats ls;
     unsigned long long killed = 0, ovf = 0, live_ins = 0;
@@ -973,7 +968,7 @@ __device__ void update_body(UpdParams& p) {
     const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned nthreads = gridDim.x * blockDim.x;
     const bool leader = gtid == 0;
-    uint2* pbuf = s_pbuf[threadIdx.x >> 5];
+    uint4* pbuf = s_pbuf[threadIdx.x >> 5];
     LocalStats ls;
     if (leader) ctl->ts[0] = globaltimer();
 
@@ -1003,13 +998,16 @@ __device__ void update_body(UpdParams& p) {
     };
 
     if (p.mode == 1) {
+        PushBuf pb{pbuf, 0};
         for (unsigned base = gtid - lane; base < (unsigned)p.nsrc; base += nthreads) {
             const unsigned i = base + lane;
             const unsigned v = i < (unsigned)p.nsrc ? (unsigned)p.srcs[i] : 0u;
             if (i < (unsigned)p.nsrc) g.push_tag[v] = tag0;
-            expand(v, i < (unsigned)p.nsrc ? g.rows[v].deg : 0, p, relax0, ls);
+            pb.add(i < (unsigned)p.nsrc, v, row_if(p, i < (unsigned)p.nsrc, v));
+            pb.flush(p, relax0, ls);
             ls.frontier += i < (unsigned)p.nsrc ? 1 : 0;
         }
+        pb.flush_cta(p, relax0, ls);
         if (!grid_sync(ctl)) return;
     } else {
         // ---- A. cut-off subtrees ------------------------------------------------------------
@@ -1023,7 +1021,7 @@ __device__ void update_body(UpdParams& p) {
             for (unsigned base = gtid - lane; base < nroots; base += nthreads) {
                 const unsigned i = base + lane;
                 const unsigned v = i < nroots ? __ldcg(&g.invq[i]) : 0u;
-                pb.add(i < nroots, v, i < nroots ? g.rows[v].deg : 0);
+                pb.add(i < nroots, v, row_if(p, i < nroots, v));
                 pb.flush(p, lvl0, ls);
             }
             pb.flush_cta(p, lvl0, ls);
@@ -1145,7 +1143,7 @@ __device__ void update_body(UpdParams& p) {
                 // through a cut-off vertex (the pull gives it its best live value again)
                 if (inv) g.state[v] = kInfState;
                 ls.marked += newinv ? 1 : 0;
-                pb.add(newinv, v, newinv ? g.rows[v].deg : 0);
+                pb.add(newinv, v, row_if(p, newinv, v));
                 pb.flush(p, pjo, ls);
             }
             pb.flush_cta(p, pjo, ls);
@@ -1163,7 +1161,7 @@ __device__ void update_body(UpdParams& p) {
             for (unsigned base = gtid - lane; base < ns; base += nthreads) {
                 const unsigned i = base + lane;
                 const unsigned v = i < ns ? __ldcg(&p.seedq[i]) : 0u;
-                pb.add(i < ns, v, i < ns ? g.rows[v].deg : 0);
+                pb.add(i < ns, v, row_if(p, i < ns, v));
                 pb.flush(p, relax0, ls);
             }
             pb.flush_cta(p, relax0, ls);
@@ -1211,10 +1209,10 @@ __device__ void update_body(UpdParams& p) {
                 const unsigned long long d = i < nfar ? __ldcg(&g.state[v]) >> 32 : 0ull;
                 const bool live = i < nfar && d >= T;
                 far_push(p, nxt, live && d >= tn, v);
-                int deg;
-                const bool doit = claim_with_deg(p, live && d < tn, v, tagr, deg);
+                RowDesc rd;
+                const bool doit = claim_with_row(p, live && d < tn, v, tagr, rd);
                 ls.frontier += doit ? 1 : 0;
-                pb.add(doit, v, deg);
+                pb.add(doit, v, rd);
                 pb.flush(p, near, ls);
             }
             pb.flush_cta(p, near, ls);
