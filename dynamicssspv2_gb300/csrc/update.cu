@@ -49,8 +49,9 @@ constexpr int kBuf = 176;                  // per-warp push buffer entries (16 b
                                            // CTAs of the update kernel stay within 100 KB of
                                            // shared memory, which leaves the L1 its 156 KB)
 constexpr int kListRegion = 512;           // per-warp u32 staging of the batch front kernels
-constexpr int kAddsPerCheck = 128;         // entries a warp may add between two flush checks
-                                           // (visit4: 4 adds of up to 32 lanes)
+constexpr int kAddsPerCheck = 32;          // entries a warp may add between two flush checks
+                                           // (one add of up to 32 lanes; visit4 reserves room
+                                           // for its four adds instead)
 static_assert(kBuf > kAddsPerCheck, "a push buffer must take one visit's adds after a check");
 constexpr unsigned kSoloWaves = 2;         // a step of at most this many CTA-waves of items
                                            // runs on CTA 0 alone (block barriers)
@@ -202,6 +203,17 @@ struct PushBuf {
     // warp-collective: expands the buffer once it could not take another kAddsPerCheck
     __device__ __forceinline__ void flush(const UpdParams& p, const Out& o, LocalStats& ls) {
         if (count <= kBuf - kAddsPerCheck) return;
+        expand_all(p, o, ls);
+    }
+
+    // warp-collective: makes room for n more entries (n warp-uniform, at most kBuf)
+    __device__ __forceinline__ void reserve(unsigned n, const UpdParams& p, const Out& o, LocalStats& ls) {
+        if ((unsigned)count + n <= (unsigned)kBuf) return;
+        expand_all(p, o, ls);
+    }
+
+    // warp-collective: splits every buffered entry into work items (one atomic per list)
+    __device__ __forceinline__ void expand_all(const UpdParams& p, const Out& o, LocalStats& ls) {
         unsigned nt, nc;
         buf_counts(buf, count, p, nt, nc);
         const unsigned it = warp_incl_scan(nt), ic = warp_incl_scan(nc);
@@ -390,19 +402,23 @@ struct RelaxOp {
             rd[q] = row_if(*p, want, c);
             ctag[q] = want ? atomicExch(&p->g.push_tag[c], tag) : tag;
         }
-        bool fl[4];
-        unsigned fc[4];
+        bool fl[4], doit[4];
+        unsigned fc[4], nadd = 0;
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             fl[q] = later[q] && ftag[q] != far.gen;
             fc[q] = (unsigned)e[q].x;
-            const bool doit = push[q] && !later[q] && ctag[q] != tag;
-            ls->frontier += doit ? 1 : 0;
-            pb.add(doit, (unsigned)e[q].x, rd[q]);
+            doit[q] = push[q] && !later[q] && ctag[q] != tag;
+            nadd += __popc(__ballot_sync(kFull, doit[q]));
+        }
+        pb.reserve(nadd, *p, out, *ls);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            ls->frontier += doit[q] ? 1 : 0;
+            pb.add(doit[q], (unsigned)e[q].x, rd[q]);
             ls->edges_relax += ok[q] && live ? 1 : 0;
         }
         far_append4(*p, far, fl, fc);
-        pb.flush(*p, out, *ls);
     }
 };
 
@@ -442,6 +458,10 @@ struct MarkOp {
             old[q] = child ? atomicExch(&p->g.inv_tag[c], p->epoch) : p->epoch;
             rd[q] = row_if(*p, child, c);
         }
+        unsigned nadd = 0;
+#pragma unroll
+        for (int q = 0; q < 4; q++) nadd += __popc(__ballot_sync(kFull, old[q] != p->epoch));
+        pb.reserve(nadd, *p, out, *ls);
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const bool mark = old[q] != p->epoch;
@@ -449,7 +469,6 @@ struct MarkOp {
             pb.add(mark, (unsigned)e[q].x, rd[q]);
             ls->edges_inv += ok[q] ? 1 : 0;
         }
-        pb.flush(*p, out, *ls);
     }
 };
 
