@@ -110,7 +110,8 @@ struct __align__(128) Ctl {
     unsigned long long fmin[2];
     // small steps run by CTA 0 alone hand their end state to the grid here
     unsigned long long solo[4];
-    unsigned long long pad4b[10];
+    unsigned solo_n[2];  // list sizes of the first round after solo relaxation rounds
+    unsigned pad4b[18];
     // line 5: barrier diagnostics (first timed-out barrier, arrivals then, CTAs that timed
     // out, max barrier count at exit, 0xFFFFFFFF - min barrier count at exit)
     unsigned diag[8];

@@ -58,6 +58,7 @@ constexpr unsigned kSoloWaves = 2;         // a step of at most this many CTA-wa
 constexpr int kSoloSteps = 256;            // consecutive solo steps before the grid re-syncs
 
 __shared__ unsigned s_nbar;        // grid barriers this CTA has passed
+__shared__ unsigned s_gen;         // barrier generation this CTA waits on next (ctl->bar_gen)
 __shared__ unsigned s_spin_limit;  // polls before a grid barrier gives up
 __shared__ uint4 s_pbuf[kMaxWarps][kBuf];  // (vertex, degree, row start) pushed, not yet expanded
 __shared__ unsigned s_wlist[kMaxWarps][kListRegion];  // k_delete / k_append list staging
@@ -69,12 +70,17 @@ struct LocalStats {
 
 // Grid-wide barrier for a cooperative launch.  The wait is bounded: on timeout the status
 // word gets DSSSP_E_TIMEOUT (with where it happened in ctl->diag) and every CTA leaves at
-// its next barrier.  Returns false when the kernel must stop (timeout or any error).
-__device__ bool grid_sync(Ctl* ctl) {
+// its next barrier.  Returns false when the kernel must stop (timeout or any error).  Each
+// CTA tracks the generation it waits on (s_gen, read once at kernel start: no barrier can
+// complete before every CTA has arrived), so arriving costs no load.  With a and b given,
+// the two counters the caller needs next are read once per CTA together with the status
+// word and returned in va and vb.
+__device__ bool grid_sync(Ctl* ctl, const unsigned* a, const unsigned* b, unsigned& va, unsigned& vb) {
     __shared__ int s_go;
+    __shared__ unsigned s_va, s_vb;
     __syncthreads();
     if (threadIdx.x == 0) {
-        const unsigned gen = ld_acquire(&ctl->bar_gen);
+        const unsigned gen = s_gen;
         __threadfence();
         const unsigned arrived = atomicAdd(&ctl->bar_count, 1u);
         if (arrived == gridDim.x - 1) {
@@ -96,11 +102,22 @@ __device__ bool grid_sync(Ctl* ctl) {
             }
         }
         __threadfence();
+        s_gen = gen + 1;
         s_nbar++;
-        s_go = __ldcg(&ctl->status) == 0;
+        const int st = __ldcg(&ctl->status);
+        s_va = a ? __ldcg(a) : 0u;
+        s_vb = b ? __ldcg(b) : 0u;
+        s_go = st == 0;
     }
     __syncthreads();
+    va = s_va;
+    vb = s_vb;
     return s_go != 0;
+}
+
+__device__ __forceinline__ bool grid_sync(Ctl* ctl) {
+    unsigned x, y;
+    return grid_sync(ctl, nullptr, nullptr, x, y);
 }
 
 // Offers distance nd through parent u to vertex c whose current word is cur.  Returns true
@@ -964,6 +981,7 @@ __device__ void update_body(UpdParams& p);
 __global__ void __launch_bounds__(256, 4) k_update(UpdParams p) {
     if (threadIdx.x == 0) {
         s_nbar = 0;
+        s_gen = ld_acquire(&p.g.ctl->bar_gen);
         const unsigned lim = __ldcg(&p.g.ctl->spin_limit);
         s_spin_limit = lim ? lim : kSpinLimit;
     }
@@ -1023,6 +1041,7 @@ __device__ void update_body(UpdParams& p) {
         return Far{which ? g.far1 : g.far0, &ctl->fc[which], g.far_tag, gen, (unsigned)g.n, thr};
     };
 
+    unsigned nT = 0, nC = 0;  // the sizes of the next relaxation round's lists
     if (p.mode == 1) {
         PushBuf pb{pbuf, 0};
         for (unsigned base = gtid - lane; base < (unsigned)p.nsrc; base += nthreads) {
@@ -1034,7 +1053,7 @@ __device__ void update_body(UpdParams& p) {
             ls.frontier += i < (unsigned)p.nsrc ? 1 : 0;
         }
         pb.flush_cta(p, relax0, ls);
-        if (!grid_sync(ctl)) return;
+        if (!grid_sync(ctl, &ctl->rcT[0], &ctl->rcC[0], nT, nC)) return;
     } else {
         // ---- A. cut-off subtrees ------------------------------------------------------------
         // Level L processes items [lo, hi) of the lists it/ic and appends the items of the
@@ -1053,8 +1072,8 @@ __device__ void update_body(UpdParams& p) {
             pb.flush_cta(p, lvl0, ls);
         }
         if (leader) ls.marked += nroots;
-        if (!grid_sync(ctl)) return;
-        unsigned loT = 0, loC = 0, hiT = __ldcg(&ctl->ltT[0]), hiC = __ldcg(&ctl->ltC[0]);
+        unsigned loT = 0, loC = 0, hiT, hiC;
+        if (!grid_sync(ctl, &ctl->ltT[0], &ctl->ltC[0], hiT, hiC)) return;
         int level = 0;
         bool need_pj = false;
         for (;;) {
@@ -1110,11 +1129,12 @@ __device__ void update_body(UpdParams& p) {
                           g.ccap - hiC},
                       PushBuf{pbuf, 0}, &ls};
             run_items(op, p, g.it + loT, hiT - loT, g.ic + loC, hiC - loC, blockIdx.x, gridDim.x);
-            if (!grid_sync(ctl)) return;
+            unsigned addT, addC;
+            if (!grid_sync(ctl, &ctl->ltT[(level + 1) % 3], &ctl->ltC[(level + 1) % 3], addT, addC)) return;
             loT = hiT;
             loC = hiC;
-            hiT += __ldcg(&ctl->ltT[(level + 1) % 3]);
-            hiC += __ldcg(&ctl->ltC[(level + 1) % 3]);
+            hiT += addT;
+            hiC += addC;
             level++;
         }
         if (leader) ctl->stat[ST_LEVELS] = (unsigned long long)level;
@@ -1196,14 +1216,14 @@ __device__ void update_body(UpdParams& p) {
             PullOp op{&p, tag0, relax0, PushBuf{pbuf, 0}, &ls, far_of(cf, fgen, T), kInfState, false};
             run_items(op, p, g.it, hiT, g.ic, hiC, blockIdx.x, gridDim.x);
         }
-        if (!grid_sync(ctl)) return;
+        if (!grid_sync(ctl, &ctl->rcT[0], &ctl->rcC[0], nT, nC)) return;
     }
     if (leader) ctl->ts[2] = globaltimer();
 
     // ---- C. relaxation rounds ---------------------------------------------------------------
     long long r = 0;
     for (;; r++) {
-        unsigned nT = __ldcg(&ctl->rcT[r % 3]), nC = __ldcg(&ctl->rcC[r % 3]);
+        // nT, nC: the sizes of round r's lists (read at the barrier before)
         if (nT == 0 && nC == 0) {
             if (!nf) break;
             // near frontier empty: advance the threshold past the least waiting distance
@@ -1246,9 +1266,7 @@ __device__ void update_body(UpdParams& p) {
             fgen++;
             cf ^= 1;
             adv++;
-            if (!grid_sync(ctl)) break;
-            nT = __ldcg(&ctl->rcT[r % 3]);
-            nC = __ldcg(&ctl->rcC[r % 3]);
+            if (!grid_sync(ctl, &ctl->rcT[r % 3], &ctl->rcC[r % 3], nT, nC)) break;
         }
         if (r >= p.max_rounds) {
             if (leader) set_status(ctl, -5 /* NO_CONVERGENCE */);
@@ -1278,9 +1296,13 @@ __device__ void update_body(UpdParams& p) {
                     c = __ldcg(&ctl->rcC[rr % 3]);
                     __syncthreads();  // every thread has read the counters before the next reset
                 }
-                if (threadIdx.x == 0) ctl->solo[3] = (unsigned long long)rr;
+                if (threadIdx.x == 0) {
+                    ctl->solo[3] = (unsigned long long)rr;
+                    ctl->solo_n[0] = t;
+                    ctl->solo_n[1] = c;
+                }
             }
-            if (!grid_sync(ctl)) break;
+            if (!grid_sync(ctl, &ctl->solo_n[0], &ctl->solo_n[1], nT, nC)) break;
             r = (long long)__ldcg(&ctl->solo[3]) - 1;  // the loop steps to the first round left
             continue;
         }
@@ -1295,7 +1317,7 @@ __device__ void update_body(UpdParams& p) {
                    PushBuf{pbuf, 0}, &ls, far_of(cf, fgen, T),
                    (unsigned long long)nT + (unsigned long long)nC * blockDim.x <= (unsigned long long)nthreads};
         run_items(op, p, odd ? g.rt1 : g.rt0, nT, odd ? g.rc1 : g.rc0, nC, blockIdx.x, gridDim.x);
-        if (!grid_sync(ctl)) break;
+        if (!grid_sync(ctl, &ctl->rcT[(r + 1) % 3], &ctl->rcC[(r + 1) % 3], nT, nC)) break;
     }
     flush_stats(ctl, ls);
     if (leader) {
