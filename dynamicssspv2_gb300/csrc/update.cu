@@ -59,6 +59,10 @@ constexpr int kSoloSteps = 256;            // consecutive solo steps before the 
 
 __shared__ unsigned s_nbar;        // grid barriers this CTA has passed
 __shared__ unsigned s_gen;         // barrier generation this CTA waits on next (ctl->bar_gen)
+// List counters of solo steps (CTA 0 alone): (thread items, CTA items) per slot, slots used
+// like the control block's three rotating counters.  Shared-memory atomics and reads save a
+// global round trip each per step.
+__shared__ unsigned s_solo_cnt[3][2];
 __shared__ unsigned s_spin_limit;  // polls before a grid barrier gives up
 __shared__ uint4 s_pbuf[kMaxWarps][kBuf];  // (vertex, degree, row start) pushed, not yet expanded
 __shared__ unsigned s_wlist[kMaxWarps][kListRegion];  // k_delete / k_append list staging
@@ -1085,23 +1089,24 @@ __device__ void update_body(UpdParams& p) {
             if (small_step(hiT - loT, hiC - loC)) {
                 // small levels: CTA 0 walks on alone while they stay small; the others wait
                 if (blockIdx.x == 0) {
+                    if (threadIdx.x < 6) s_solo_cnt[threadIdx.x / 2][threadIdx.x % 2] = 0;
+                    __syncthreads();
                     for (int steps = 0; steps < kSoloSteps; steps++) {
                         if ((loT >= hiT && loC >= hiC) || level >= p.bfs_levels || !small_step(hiT - loT, hiC - loC))
                             break;
+                        unsigned* cnt = s_solo_cnt[(level + 1) % 3];
                         if (threadIdx.x == 0) {
-                            ctl->ltT[(level + 2) % 3] = 0;
-                            ctl->ltC[(level + 2) % 3] = 0;
+                            s_solo_cnt[(level + 2) % 3][0] = 0;
+                            s_solo_cnt[(level + 2) % 3][1] = 0;
                         }
-                        MarkOp op{&p,
-                                  Out{g.it + hiT, &ctl->ltT[(level + 1) % 3], g.tcap - hiT, g.ic + hiC,
-                                      &ctl->ltC[(level + 1) % 3], g.ccap - hiC},
+                        MarkOp op{&p, Out{g.it + hiT, &cnt[0], g.tcap - hiT, g.ic + hiC, &cnt[1], g.ccap - hiC},
                                   PushBuf{pbuf, 0}, &ls};
                         run_items(op, p, g.it + loT, hiT - loT, g.ic + loC, hiC - loC, 0, 1);
                         __syncthreads();
                         loT = hiT;
                         loC = hiC;
-                        hiT += __ldcg(&ctl->ltT[(level + 1) % 3]);
-                        hiC += __ldcg(&ctl->ltC[(level + 1) % 3]);
+                        hiT += cnt[0];
+                        hiC += cnt[1];
                         level++;
                         __syncthreads();  // every thread has read the counters before the next reset
                     }
@@ -1109,6 +1114,8 @@ __device__ void update_body(UpdParams& p) {
                         ctl->solo[0] = ((unsigned long long)hiT << 32) | loT;
                         ctl->solo[1] = ((unsigned long long)hiC << 32) | loC;
                         ctl->solo[2] = (unsigned long long)level;
+                        ctl->ltT[(level + 1) % 3] = 0;  // the grid's next level appends here
+                        ctl->ltC[(level + 1) % 3] = 0;
                     }
                 }
                 if (!grid_sync(ctl)) return;
@@ -1278,28 +1285,34 @@ __device__ void update_body(UpdParams& p) {
             if (blockIdx.x == 0) {
                 long long rr = r;
                 unsigned t = nT, c = nC;
+                if (threadIdx.x < 6) s_solo_cnt[threadIdx.x / 2][threadIdx.x % 2] = 0;
+                __syncthreads();
                 for (int steps = 0; steps < kSoloSteps; steps++) {
                     if ((t == 0 && c == 0) || !small_step(t, c) || rr >= p.max_rounds) break;
+                    unsigned* cnt = s_solo_cnt[(rr + 1) % 3];
                     if (threadIdx.x == 0) {
-                        ctl->rcT[(rr + 2) % 3] = 0;
-                        ctl->rcC[(rr + 2) % 3] = 0;
+                        s_solo_cnt[(rr + 2) % 3][0] = 0;
+                        s_solo_cnt[(rr + 2) % 3][1] = 0;
                     }
                     const bool odd = (rr & 1) != 0;
                     RelaxOp op{&p, rbase + (unsigned)rr + 2u,
-                               Out{odd ? g.rt0 : g.rt1, &ctl->rcT[(rr + 1) % 3], g.tcap, odd ? g.rc0 : g.rc1,
-                                   &ctl->rcC[(rr + 1) % 3], g.ccap},
+                               Out{odd ? g.rt0 : g.rt1, &cnt[0], g.tcap, odd ? g.rc0 : g.rc1, &cnt[1], g.ccap},
                                PushBuf{pbuf, 0}, &ls, far_of(cf, fgen, T), true};
                     run_items(op, p, odd ? g.rt1 : g.rt0, t, odd ? g.rc1 : g.rc0, c, 0, 1);
                     __syncthreads();
                     rr++;
-                    t = __ldcg(&ctl->rcT[rr % 3]);
-                    c = __ldcg(&ctl->rcC[rr % 3]);
+                    t = cnt[0];
+                    c = cnt[1];
                     __syncthreads();  // every thread has read the counters before the next reset
                 }
                 if (threadIdx.x == 0) {
                     ctl->solo[3] = (unsigned long long)rr;
                     ctl->solo_n[0] = t;
                     ctl->solo_n[1] = c;
+                    ctl->rcT[rr % 3] = t;  // round rr's lists (the near-far advance appends here when empty)
+                    ctl->rcC[rr % 3] = c;
+                    ctl->rcT[(rr + 1) % 3] = 0;  // the grid's round rr appends here
+                    ctl->rcC[(rr + 1) % 3] = 0;
                 }
             }
             if (!grid_sync(ctl, &ctl->solo_n[0], &ctl->solo_n[1], nT, nC)) break;
