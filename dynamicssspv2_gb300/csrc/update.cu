@@ -158,6 +158,30 @@ __device__ __forceinline__ bool relax_to(const DevGraph& g, unsigned epoch, unsi
     return false;
 }
 
+// The two seed relaxations of an insertion (u, v, w) with w > 0: v is offered ndv = d(u) + w
+// through u and u is offered ndu = d(v) + w through v, from the states su, sv read before.
+// Both atomicMin go out before either result is used; the outcome is that of two relax_to
+// calls.  pu / pv: u / v went down and must be pushed.
+__device__ __forceinline__ void relax_both(const DevGraph& g, unsigned epoch, unsigned u, unsigned v,
+                                           unsigned long long ndv, unsigned long long ndu, unsigned long long su,
+                                           unsigned long long sv, bool& pu, bool& pv, LocalStats& ls) {
+    const bool from_u = (su >> 32) != kDistInf, from_v = (sv >> 32) != kDistInf;
+    if (from_u && ndv >= kDistInf && sv == kInfState) ls.dist_ovf++;
+    if (from_v && ndu >= kDistInf && su == kInfState) ls.dist_ovf++;
+    const unsigned long long cv = (ndv << 32) | u, cu = (ndu << 32) | v;
+    const bool tv = from_u && ndv < kDistInf && cv < sv;
+    const bool tu = from_v && ndu < kDistInf && cu < su;
+    const unsigned long long ov = tv ? atomicMin(&g.state[v], cv) : kInfState;
+    const unsigned long long ou = tu ? atomicMin(&g.state[u], cu) : kInfState;
+    pv = tv && (ov >> 32) > ndv;
+    pu = tu && (ou >> 32) > ndu;
+    ls.updates += (pv ? 1 : 0) + (pu ? 1 : 0);
+    if (g.chg_tag) {
+        if (tv && !pv && ov > cv) g.chg_tag[v] = epoch;
+        if (tu && !pu && ou > cu) g.chg_tag[u] = epoch;
+    }
+}
+
 // Destination of pushed vertices: a thread-item list and a CTA-item list with counters.
 struct Out {
     Item* tl;
@@ -777,6 +801,23 @@ __device__ bool hash_contains(const UpdParams& p, unsigned long long pair, int w
     return false;
 }
 
+// Writes the entry (col, w) at position pos of row r, described by rd (read before the degree
+// bump).  Returns its slot, or -1 after listing it for the host-side row growth when the row
+// is full (record i).
+__device__ __forceinline__ long long place_entry(const UpdParams& p, const RowDesc& rd, int pos, int r, int col,
+                                                 int w, long long i, unsigned long long& ovf) {
+    if (pos < rd.cap) {
+        const long long at = rd.start + pos;
+        p.g.adj[at] = make_int2(col, w);
+        return at;
+    }
+    const int o = atomicAdd(&p.g.ctl->ovf_count, 1);
+    p.ovf[o] = make_int4(r, col, w, (int)i);
+    ovf++;
+    atomicCAS(&p.g.ctl->status, 0, kStatusOverflowPending);
+    return -1;
+}
+
 // Tombstones the reverse entry of slot j.  A twin word outside the adjacency is an internal
 // error: it is reported in the status word and the access is skipped.
 __device__ __forceinline__ void tombstone_twin(const UpdParams& p, long long j) {
@@ -912,37 +953,28 @@ __global__ void k_append(UpdParams p) {
     for (long long base = (long long)blockIdx.x * blockDim.x + threadIdx.x - lane; base < p.k; base += nthreads) {
         const long long i = base + lane;
         const int4 c = i < p.k ? p.chg[i] : make_int4(0, 0, 0, -1);
+        // Independent accesses of one record go out together (states, rows and the deletion-set
+        // probe; both degree bumps; both seed relaxations; both claims).
         int alive = 0;
         unsigned long long sa = kInfState, sb = kInfState;
         if (c.w == 1) {
-            sa = __ldcg(&g.state[c.x]);  // issued alongside the deletion-set probe
+            sa = __ldcg(&g.state[c.x]);
             sb = __ldcg(&g.state[c.y]);
+            const RowDesc rx = g.rows[c.x], ry = g.rows[c.y];  // start and cap are fixed in this kernel
             if (hash_contains(p, dpair_key((unsigned)c.x, (unsigned)c.y), c.z)) {
                 killed++;
             } else {
                 alive = 1;
                 live_ins++;
-                long long at[2];
-#pragma unroll
-                for (int side = 0; side < 2; side++) {
-                    const int r = side ? c.y : c.x, col = side ? c.x : c.y;
-                    RowDesc* rd = &g.rows[r];
-                    const int pos = atomicAdd(&rd->deg, 1);
-                    if (pos < rd->cap) {
-                        at[side] = rd->start + pos;
-                        g.adj[at[side]] = make_int2(col, c.z);
-                    } else {
-                        at[side] = -1;
-                        const int o = atomicAdd(&ctl->ovf_count, 1);
-                        p.ovf[o] = make_int4(r, col, c.z, (int)i);
-                        ovf++;
-                        atomicCAS(&ctl->status, 0, kStatusOverflowPending);
-                    }
-                    p.slot[2 * i + side] = at[side];
-                }
+                const int pos0 = atomicAdd(&g.rows[c.x].deg, 1);
+                const int pos1 = atomicAdd(&g.rows[c.y].deg, 1);
+                const long long at0 = place_entry(p, rx, pos0, c.x, c.y, c.z, i, ovf);
+                const long long at1 = place_entry(p, ry, pos1, c.y, c.x, c.z, i, ovf);
+                p.slot[2 * i] = at0;
+                p.slot[2 * i + 1] = at1;
                 if (g.twin) {  // an overflowed end is placed (and paired) by the row growth
-                    if (at[0] >= 0) g.twin[at[0]] = at[1] >= 0 ? (unsigned)at[1] : kNoTwin;
-                    if (at[1] >= 0) g.twin[at[1]] = at[0] >= 0 ? (unsigned)at[0] : kNoTwin;
+                    if (at0 >= 0) g.twin[at0] = at1 >= 0 ? (unsigned)at1 : kNoTwin;
+                    if (at1 >= 0) g.twin[at1] = at0 >= 0 ? (unsigned)at0 : kNoTwin;
                 }
             }
         }
@@ -951,16 +983,24 @@ __global__ void k_append(UpdParams p) {
         bool pa = false, pbv = false;
         const unsigned long long ndb = (sa >> 32) + (unsigned)c.z, nda = (sb >> 32) + (unsigned)c.z;
         if (alive) {
-            if ((sa >> 32) != kDistInf) pbv = relax_to(g, p.epoch, (unsigned)c.y, ndb, (unsigned)c.x, c.z, sb, ls);
-            if ((sb >> 32) != kDistInf)
-                pa = relax_to(g, p.epoch, (unsigned)c.x, nda, (unsigned)c.y, c.z, __ldcg(&g.state[c.x]), ls);
+            if (c.z > 0) {
+                relax_both(g, p.epoch, (unsigned)c.x, (unsigned)c.y, ndb, nda, sa, sb, pa, pbv, ls);
+            } else {  // zero weight: strict improvements only (compare-and-swap)
+                if ((sa >> 32) != kDistInf) pbv = relax_to(g, p.epoch, (unsigned)c.y, ndb, (unsigned)c.x, c.z, sb, ls);
+                if ((sb >> 32) != kDistInf)
+                    pa = relax_to(g, p.epoch, (unsigned)c.x, nda, (unsigned)c.y, c.z, __ldcg(&g.state[c.x]), ls);
+            }
             ls.edges_relax += 2;
         }
+        // claim: far-list tag for an end at or above the threshold, frontier tag otherwise
         const bool lb = pbv && ndb >= T, la = pa && nda >= T;
-        const bool fb = lb && atomicExch(&g.far_tag[c.y], rbase) != rbase;
-        const bool fa = la && atomicExch(&g.far_tag[c.x], rbase) != rbase;
-        const bool db = pbv && !lb && atomicExch(&g.push_tag[c.y], tag0) != tag0;
-        const bool da = pa && !la && atomicExch(&g.push_tag[c.x], tag0) != tag0;
+        unsigned* tb = lb ? g.far_tag + c.y : g.push_tag + c.y;
+        unsigned* ta = la ? g.far_tag + c.x : g.push_tag + c.x;
+        const unsigned vb = lb ? rbase : tag0, va = la ? rbase : tag0;
+        const unsigned ob = pbv ? atomicExch(tb, vb) : vb;
+        const unsigned oa = pa ? atomicExch(ta, va) : va;
+        const bool fb = lb && ob != vb, db = pbv && !lb && ob != vb;
+        const bool fa = la && oa != va, da = pa && !la && oa != va;
         ls.frontier += (db ? 1 : 0) + (da ? 1 : 0) + (fb ? 1 : 0) + (fa ? 1 : 0);
         near_list.add(db, (unsigned)c.y);  // claimed: one entry per vertex
         near_list.add(da, (unsigned)c.x);
