@@ -25,7 +25,7 @@ from . import Graph, Opts
 CANDIDATES = [
     {},
     {"small_deg": 8},
-    {"small_deg": 4, "large_deg": 256, "chunk": 512},
+    {"small_deg": 4, "large_deg": 1024, "chunk": 1024},
     {"small_deg": 4, "large_deg": 4096, "chunk": 2048},
     {"bfs_levels": 0},
     {"bfs_levels": 8},

@@ -1244,7 +1244,7 @@ void dsssp_default_opts(dsssp_opts* o) {
     o->slack_pct = 25;
     o->slack_min = 4;
     o->small_deg = 4;
-    o->large_deg = 1024;
+    o->large_deg = 256;
     o->chunk = 1024;
     o->bfs_levels = 48;
     o->block = 256;
