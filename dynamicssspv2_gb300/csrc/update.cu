@@ -1022,7 +1022,7 @@ __global__ void k_append(UpdParams p) {
 
 __device__ void update_body(UpdParams& p);
 
-__global__ void __launch_bounds__(256, 4) k_update(UpdParams p) {
+__global__ void __launch_bounds__(256, 3) k_update(UpdParams p) {
     if (threadIdx.x == 0) {
         s_nbar = 0;
         s_gen = ld_acquire(&p.g.ctl->bar_gen);
