@@ -1022,6 +1022,10 @@ __global__ void k_append(UpdParams p) {
 
 __device__ void update_body(UpdParams& p);
 
+// 3 CTAs of 256 threads per SM: 80 registers a thread without spills.  Every walk level and
+// relaxation round waits on its slowest CTA's chain of dependent accesses, so shorter chains
+// and fewer CTAs at each barrier beat more resident warps here (4 CTAs per SM with 64
+// registers and spills was slower on every workload but the throughput-bound 256-graph batch).
 __global__ void __launch_bounds__(256, 3) k_update(UpdParams p) {
     if (threadIdx.x == 0) {
         s_nbar = 0;
