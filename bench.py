@@ -207,18 +207,37 @@ def measured_peak_hbm() -> tuple[float, str]:
     return 6800.0, "fallback"
 
 
-def profiled_traffic(workload: str):
-    """dram bytes per launch of the update kernel from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / f"k_update_{workload}.txt"
+def profiled_value(stem: str, workload: str, key: str):
+    """A `key=value` figure from the committed ncu summary profiles/<stem>_<workload>.txt."""
+    p = ROOT / "profiles" / f"{stem}_{workload}.txt"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
-        if line.startswith("dram_bytes_per_launch="):
+        if line.startswith(key + "="):
             try:
                 return float(line.split("=", 1)[1])
             except ValueError:
                 return None
     return None
+
+
+def profiled_traffic(workload: str):
+    """dram bytes per launch of the update kernel from the committed ncu summary, if any."""
+    return profiled_value("k_update", workload, "dram_bytes_per_launch")
+
+
+def front_roofline(workload: str, stats, peak: float) -> dict:
+    """The batch front kernels' DRAM bandwidth: ncu bytes per launch (committed summary) over
+    the live CUDA-event time of each kernel.  They are random-access bound, so this shows how
+    close they run to the HBM, next to the update kernel's algorithmic-byte roofline."""
+    out = {}
+    for name, field in (("k_delete", "t_delete_ms"), ("k_append", "t_append_ms")):
+        ms = statistics.mean(getattr(s, field) for s in stats)
+        traffic = profiled_value("front_kernels", workload, f"{name}_dram_bytes_per_launch")
+        rate = traffic / (ms * 1e-3) / 1e9 if traffic and ms > 0 else None
+        out[name] = {"ms_per_launch": ms, "traffic": traffic, "achieved_dram_gbs": rate,
+                     "frac_dram": rate / peak if rate else None}
+    return out
 
 
 def cpu_recompute(n, u, v, w, ch, src, reps=1):
@@ -371,6 +390,15 @@ def run_engine(args, dist: Dist) -> int:
         delta_counts.append(cnt)
     clk.__exit__(None, None, None)
     e2e_value, e2e_t = whole_job_rate(dist, batch, 1, statistics.median(e2e_times))
+
+    # the front kernels one by one: timing level 2 records events between them, in a few more
+    # batches after the timed ones, so the headline steps carry none of their cost
+    opts.timing = 2
+    g.set_opts(opts)
+    front_stats = []
+    for _ in range(5):
+        reset()
+        front_stats.append(device_step())
     delta_value, delta_t = whole_job_rate(dist, batch, 1, statistics.median(delta_times))
 
     # roofline of the dominant kernel (the persistent update kernel)
@@ -429,7 +457,8 @@ def run_engine(args, dist: Dist) -> int:
                      "alg_model": "per-unit byte model: 16 B per cut-off vertex + 4 B per child, 20 B per frontier "
                                   "vertex (pulls included) + 16 B per scanned edge, 12 B per lowering atomic",
                      "engine_bytes_per_launch": eng_bytes,
-                     "achieved_engine_count": eng_bytes / (upd_ms * 1e-3) / 1e9},
+                     "achieved_engine_count": eng_bytes / (upd_ms * 1e-3) / 1e9,
+                     "front_kernels": front_roofline(args.workload, front_stats, peak)},
         "cpu_baseline": cpu,
         "clocks": clocks,
         "detail": {

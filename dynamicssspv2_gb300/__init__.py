@@ -74,7 +74,7 @@ class Stats(C.Structure):
         for name in ("t_step1_ms", "t_inval_ms", "t_relax_ms", "t_update_ms", "t_total_ms", "bytes_alg",
                      "bytes_alg_update")
     ] + [("advances", C.c_int64), ("tombstoned", C.c_int64), ("graph_launch", C.c_int64),
-         ("bytes_engine_update", C.c_double)]
+         ("bytes_engine_update", C.c_double), ("t_delete_ms", C.c_double), ("t_append_ms", C.c_double)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}

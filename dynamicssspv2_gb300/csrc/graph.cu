@@ -23,7 +23,8 @@
 
 namespace dsssp {
 
-cudaError_t launch_front(const UpdParams& p, int grid, cudaStream_t s);
+cudaError_t launch_front(const UpdParams& p, int grid, cudaStream_t s, cudaEvent_t after_prepare,
+                         cudaEvent_t after_delete);
 cudaError_t update_occupancy(int block, int* blocks_per_sm);
 cudaError_t launch_update(const UpdParams& p, int grid, int block, cudaStream_t s);
 void batch_kernels(const void* fns[4]);
@@ -529,14 +530,15 @@ struct dsssp_graph {
     DelSlot* d_hset = nullptr;  // deletion set of the batch
     unsigned long long hcap = 0;
     Ctl* h_ctl = nullptr;  // pinned mirror of the control block
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // batch timing: 0 start, 1 before k_update, 2 end, 3 spare, 4 after k_prepare, 5 after k_delete
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     unsigned epoch = 0;
     int coop_grid = 0;
     // the batch launch sequence as an instantiated CUDA graph (opts.launch_graph)
     cudaGraph_t bgraph = nullptr;
     cudaGraphExec_t bexec = nullptr;
     cudaGraphNode_t bn_hash = nullptr, bn_kern[4] = {nullptr, nullptr, nullptr, nullptr};
-    bool bgraph_timing = false;
+    int bgraph_timing = 0;  // the timing level the instantiated graph records
     bool bgraph_failed = false;
     // pending batch
     bool pending = false;
@@ -928,6 +930,11 @@ void fill_stats(const dsssp_graph* g, const Ctl& c, dsssp_stats* st, bool events
         if (cudaEventElapsedTime(&a, g->ev[0], g->ev[1]) == cudaSuccess) st->t_step1_ms = a;
         if (cudaEventElapsedTime(&b, g->ev[1], g->ev[2]) == cudaSuccess) st->t_update_ms = b;
         if (cudaEventElapsedTime(&t, g->ev[0], g->ev[2]) == cudaSuccess) st->t_total_ms = t;
+        if (k > 0 && g->o.timing >= 2) {  // a batch: the front kernels one by one
+            float d = 0, ap = 0;
+            if (cudaEventElapsedTime(&d, g->ev[4], g->ev[5]) == cudaSuccess) st->t_delete_ms = d;
+            if (cudaEventElapsedTime(&ap, g->ev[5], g->ev[1]) == cudaSuccess) st->t_append_ms = ap;
+        }
     }
     st->n_killed = (int64_t)c.killed;
     st->work_items = (int64_t)c.stat[ST_ITEMS];
@@ -1070,8 +1077,9 @@ void drop_batch_graph(dsssp_graph* g) {
 }
 
 // Builds and instantiates the batch graph: [event 0] control-block reset, deletion-set reset,
-// k_prepare, k_delete, k_append, [event 1] k_update (cooperative), [event 2] status read.
-cudaError_t build_batch_graph(dsssp_graph* g, const BatchNodes& b, bool timing) {
+// k_prepare, [event 4], k_delete, [event 5], k_append, [event 1] k_update (cooperative),
+// [event 2] status read.  Events 0-2 are recorded at timing level 1, events 4-5 at level 2.
+cudaError_t build_batch_graph(dsssp_graph* g, const BatchNodes& b, int timing) {
     drop_batch_graph(g);
     cudaGraph_t gr = nullptr;
     cudaError_t e = cudaGraphCreate(&gr, 0);
@@ -1100,6 +1108,11 @@ cudaError_t build_batch_graph(dsssp_graph* g, const BatchNodes& b, bool timing) 
             prev = n;
         if (e != cudaSuccess) break;
         if ((e = cudaGraphAddKernelNode(&n, gr, &prev, dep(), &b.kp[i])) != cudaSuccess) break;
+        g->bn_kern[i] = n;
+        if (i < 2 && timing >= 2) {  // after k_prepare and after k_delete
+            prev = n;
+            if ((e = cudaGraphAddEventRecordNode(&n, gr, &prev, dep(), g->ev[4 + i])) != cudaSuccess) break;
+        }
         if (i == 3) {  // the update kernel's grid barrier needs all CTAs resident
             cudaLaunchAttributeValue v;
             memset(&v, 0, sizeof(v));
@@ -1107,7 +1120,6 @@ cudaError_t build_batch_graph(dsssp_graph* g, const BatchNodes& b, bool timing) 
             if ((e = cudaGraphKernelNodeSetAttribute(n, cudaLaunchAttributeCooperative, &v)) != cudaSuccess) break;
         }
         prev = n;
-        g->bn_kern[i] = n;
     }
     if (e == cudaSuccess && timing && (e = cudaGraphAddEventRecordNode(&n, gr, &prev, dep(), g->ev[2])) == cudaSuccess)
         prev = n;
@@ -1129,7 +1141,7 @@ bool launch_batch_graph(dsssp_graph* g, const UpdParams& p, unsigned long long h
     if (!g->o.launch_graph || g->bgraph_failed || p.k <= 0) return false;
     BatchNodes b;
     batch_nodes(g, p, h, b);
-    const bool timing = g->o.timing != 0;
+    const int timing = g->o.timing;
     cudaError_t e = cudaSuccess;
     if (!g->bexec || g->bgraph_timing != timing) {
         e = build_batch_graph(g, b, timing);
@@ -1170,7 +1182,8 @@ int enqueue_batch(dsssp_graph* g, const int4* d_chg, long long k, cudaStream_t s
     int rc = clear_ctl(g, s);
     if (rc) return rc;
     CK(cudaMemsetAsync(g->d_hset, 0xFF, sizeof(DelSlot) * h, s), "deletion set reset");
-    CK(launch_front(p, g->num_sms * 8, s), "insert/delete kernels");
+    const bool fev = g->o.timing >= 2;
+    CK(launch_front(p, g->num_sms * 8, s, fev ? g->ev[4] : nullptr, fev ? g->ev[5] : nullptr), "insert/delete kernels");
     if (ev) CK(cudaEventRecord(g->ev[1], s), "event");
     CK(launch_update(p, g->coop_grid, g->o.block, s), "update kernel");
     if (ev) CK(cudaEventRecord(g->ev[2], s), "event");

@@ -1392,12 +1392,16 @@ namespace dsssp {
 
 void count_launch(int n);
 
-cudaError_t launch_front(const UpdParams& p, int grid, cudaStream_t s) {
+// after_prepare / after_delete: events recorded between the kernels (nullptr = none)
+cudaError_t launch_front(const UpdParams& p, int grid, cudaStream_t s, cudaEvent_t after_prepare,
+                         cudaEvent_t after_delete) {
     if (p.k <= 0) return cudaSuccess;
     const long long need = (p.k + 255) / 256;
     const unsigned g = (unsigned)(need < grid ? need : grid);
     k_prepare<<<g, 256, 0, s>>>(p);
+    if (after_prepare) cudaEventRecord(after_prepare, s);
     k_delete<<<g, 256, 0, s>>>(p);
+    if (after_delete) cudaEventRecord(after_delete, s);
     k_append<<<g, 256, 0, s>>>(p);
     count_launch(3);
     return cudaGetLastError();

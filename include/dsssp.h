@@ -64,7 +64,9 @@ typedef struct {
     int32_t bfs_levels;   /* subtree walk levels before switching to pointer jumping */
     int32_t block;        /* threads per CTA of the update kernel (multiple of 32) */
     int32_t ctas_per_sm;  /* resident CTAs per SM of the update kernel; 0 = occupancy max */
-    int32_t timing;       /* 1 = record CUDA events and phase timestamps into the stats */
+    int32_t timing;       /* 1 = record CUDA events and phase timestamps into the stats; 2 = also
+                             events between the batch front kernels (t_delete_ms, t_append_ms),
+                             which costs a batch a few microseconds */
     int64_t max_rounds;   /* relaxation round cap; 0 = 2n + 16 */
     int32_t spare_pct;    /* extra adjacency slots, percent of the laid-out rows, into which a
                              row that runs out of slack moves (no full repack); 0..400 */
@@ -119,6 +121,9 @@ typedef struct {
     double bytes_engine_update; /* the update kernel's bytes by the engine's own count (all row
                                    scans of the subtree walk included; bytes_alg_update credits
                                    only the task byte model's units) */
+    double t_delete_ms;        /* k_delete alone (CUDA events; batches at timing level 2) */
+    double t_append_ms;        /* k_append alone, seeds included (CUDA events; batches at timing
+                                  level 2; with row growth it spans the growth too) */
 } dsssp_stats;
 
 /* ---- engine ------------------------------------------------------------------------ */

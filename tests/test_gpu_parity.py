@@ -66,6 +66,9 @@ OPTION_SETS = [
     {"delta": 25},
     {"delta": 25, "bfs_levels": 0, "small_deg": 4, "large_deg": 4, "chunk": 32},
     {"launch_graph": 0},                                   # plain stream launches
+    {"timing": 2},                                         # events between the front kernels
+    {"timing": 2, "launch_graph": 0},
+    {"timing": 0},                                         # no events, no timestamps
 ]
 
 
@@ -83,6 +86,11 @@ def test_random_er_batches(opts, seed):
     if opts.get("slack_pct") == 0:
         assert st.overflow_entries > 0
         assert st.repacks == (1 if opts.get("spare_pct") == 0 else 0)
+    if opts.get("timing") == 2:
+        assert st.t_delete_ms > 0 and st.t_append_ms > 0
+        assert st.t_delete_ms + st.t_append_ms < st.t_step1_ms
+    elif opts.get("timing", 1) == 1:
+        assert st.t_delete_ms == 0 and st.t_append_ms == 0 and st.t_update_ms > 0
 
 
 def test_zero_weights_multiedges_selfloops():
