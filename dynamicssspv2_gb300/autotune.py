@@ -82,7 +82,7 @@ class Autotuner:
         wbar = float(np.mean(live["w"])) if len(live) else 0.0
         if wbar <= 0:
             return []
-        return [{"delta": max(1, int(round(f * wbar)))} for f in (4.0, 12.0)]
+        return [{"delta": max(1, int(round(f * wbar)))} for f in (8.0, 96.0)]
 
     def tune(self, graph: Graph, changes: np.ndarray, force: bool = False) -> dict:
         """Picks the fastest candidate for (graph, changes), sets it on the graph and returns

@@ -75,7 +75,7 @@ typedef struct {
                              a threshold T, the others wait until the near frontier is empty and
                              T moves to (least waiting distance) + delta.  Same results; far
                              fewer rounds and relaxations on high-diameter graphs.  -1 (the
-                             default) = automatic: near-far with 8 x the mean edge weight once
+                             default) = automatic: near-far with 32 x the mean edge weight once
                              the last batch or tree computation needed more than 256 rounds,
                              plain rounds otherwise.  Costs 12 bytes per vertex, allocated when
                              first used. */
