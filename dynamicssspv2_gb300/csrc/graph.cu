@@ -1055,7 +1055,7 @@ void batch_nodes(const dsssp_graph* g, const UpdParams& p, unsigned long long h,
     const unsigned front = (unsigned)(need < g->num_sms * 8 ? need : g->num_sms * 8);  // as launch_front
     for (int i = 0; i < 4; i++) {
         cudaKernelNodeParams& k = b.kp[i];
-        memset(&k, 0, sizeof(k));
+        k = cudaKernelNodeParams{};
         k.func = const_cast<void*>(fns[i]);
         k.gridDim = dim3(i < 3 ? front : (unsigned)g->coop_grid);
         k.blockDim = dim3(i < 3 ? 256u : (unsigned)g->o.block);
@@ -1351,16 +1351,20 @@ int dsssp_graph_create(int32_t n, int64_t m, const int32_t* u, const int32_t* v,
     }
     dsssp_graph* g = new dsssp_graph();
     if (opts) g->o = *opts;
+    else dsssp_default_opts(&g->o);
     if (m > 0) {  // mean weight for the automatic near-far width
         double sw = 0;
 #pragma omp parallel for reduction(+ : sw)
         for (int64_t i = 0; i < m; i++) sw += (double)(w[i] > 0 ? w[i] : 0);
         g->mean_w = sw / (double)m;
     }
-    else dsssp_default_opts(&g->o);
     int rc = check_opts(g->o);
     if (rc) { delete g; return rc; }
-    if (g->o.device < 0 || g->o.device >= ndev) { delete g; return fail(DSSSP_E_INVAL, "device %d does not exist", g->o.device); }
+    if (g->o.device < 0 || g->o.device >= ndev) {
+        const int dev = g->o.device;
+        delete g;
+        return fail(DSSSP_E_INVAL, "device %d does not exist", dev);
+    }
     g->dev = g->o.device;
     g->n = n;
     rc = set_device(g);
@@ -1371,8 +1375,9 @@ int dsssp_graph_create(int32_t n, int64_t m, const int32_t* u, const int32_t* v,
     if (!coop) { delete g; return fail(DSSSP_E_COOP, "device does not support cooperative launch"); }
     int per_sm = 0;
     if (update_occupancy(g->o.block, &per_sm) != cudaSuccess || per_sm < 1) {
+        const int block = g->o.block;
         delete g;
-        return fail(DSSSP_E_COOP, "update kernel has no occupancy at block %d", g->o.block);
+        return fail(DSSSP_E_COOP, "update kernel has no occupancy at block %d", block);
     }
     if (g->o.ctas_per_sm > 0 && g->o.ctas_per_sm < per_sm) per_sm = g->o.ctas_per_sm;
     g->coop_grid = per_sm * g->num_sms;

@@ -528,3 +528,26 @@ def test_automatic_near_far_on_a_deep_graph():
         assert g.tree_compute(0).rounds < 256
         st = g.apply_batch(D.gen_changes(5000, *er, 200, 200, seed=12))
         assert st.advances == 0
+
+
+def test_create_with_null_opts_and_edgeless_graph():
+    """dsssp_graph_create with NULL options takes the defaults; an edgeless graph keeps the
+    options it is given."""
+    import ctypes as C
+
+    u, v, w = (np.ascontiguousarray(x, np.int32) for x in D.gen_er(500, 2000, 1, 50, 21))
+    h = C.c_void_p()
+    D._check(D._lib.dsssp_graph_create(500, len(u), u, v, w, None, C.byref(h)), "graph_create")
+    try:
+        got, want = D.Opts(), D.default_opts()
+        D._check(D._lib.dsssp_graph_get_opts(h, C.byref(got)), "get_opts")
+        assert {k: getattr(got, k) for k, _ in D.Opts._fields_} == {k: getattr(want, k) for k, _ in D.Opts._fields_}
+    finally:
+        D._lib.dsssp_graph_destroy(h)
+    e = np.zeros(0, np.int32)
+    with D.Graph(10, e, e, e, bfs_levels=3, small_deg=8) as g:
+        o = g.get_opts()
+        assert o.bfs_levels == 3 and o.small_deg == 8
+        g.tree_compute(0)
+        p, d = g.tree_read()
+        assert d[0] == 0 and (p[1:] == -1).all()
