@@ -1333,7 +1333,7 @@ static int check_opts(const dsssp_opts& o) {
     if (o.slack_pct < 0 || o.slack_min < 0 || o.small_deg < 4 || o.small_deg > 64 || o.small_deg % 4 ||
         o.large_deg < o.small_deg || o.chunk < 32 ||
         o.bfs_levels < 0 || o.block < 32 || o.block > 256 || o.block % 32 || o.ctas_per_sm < 0 || o.max_rounds < 0 ||
-        o.spare_pct < 0 || o.spare_pct > 400 || o.delta < -1)
+        o.spare_pct < 0 || o.spare_pct > 400 || o.delta < -1 || o.timing < 0 || o.timing > 2)
         return fail(DSSSP_E_INVAL, "invalid dsssp_opts");
     return DSSSP_OK;
 }

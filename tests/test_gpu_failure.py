@@ -39,3 +39,17 @@ def test_debug_hooks_reject_bad_values():
             with pytest.raises(D.DsssspError) as e:
                 g.debug_set(what, value)
             assert e.value.code == D.E_INVAL
+
+
+def test_invalid_options_are_refused():
+    u, v, w = D.gen_er(100, 300, seed=1)
+    for bad in ({"timing": 3}, {"timing": -1}, {"small_deg": 6}, {"block": 512}, {"delta": -2}):
+        with pytest.raises(D.DsssspError) as e:
+            D.Graph(100, u, v, w, **bad)
+        assert e.value.code == D.E_INVAL, bad
+    with D.Graph(100, u, v, w) as g:
+        o = g.get_opts()
+        o.timing = 7
+        with pytest.raises(D.DsssspError) as e:
+            g.set_opts(o)
+        assert e.value.code == D.E_INVAL
