@@ -248,7 +248,7 @@ void dsssp_free(void* p);
 /* ---- shortest-path tree without device allocation ---------------------------------- */
 
 /* Largest graph dsssp_sssp_noalloc() accepts: its work space is a fixed static device array
- * of about 5 MB that every GPU that loads this library keeps until the process exits. */
+ * of about 8.2 MB that every GPU that loads this library keeps until the process exits. */
 #define DSSSP_NOALLOC_MAX_VERTICES 65536
 #define DSSSP_NOALLOC_MAX_ENTRIES 1048576
 
