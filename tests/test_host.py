@@ -263,3 +263,25 @@ def test_reference_style_change_sampling():
     again = D.gen_changes_ref(n, u, v, w, 5000, 30, seed=11)
     assert again.tolist() == ch.tolist()
     assert D.gen_changes_ref(n, u, v, w, 5000, 30, seed=12).tolist() != ch.tolist()
+
+
+def test_bench_reads_the_committed_profiles():
+    """bench.py's roofline reads ncu figures from profiles/: the update kernel's DRAM bytes per
+    launch and the front kernels' (their bandwidth = bytes / live time, as a fraction of the
+    peak)."""
+    import bench
+
+    traffic = bench.profiled_traffic("rmat22")
+    assert traffic is not None and 1e8 < traffic < 1e9
+    assert bench.profiled_value("k_update", "no_such_workload", "dram_bytes_per_launch") is None
+
+    class S:  # stand-in for the engine's stats of two batches
+        def __init__(self, d, a):
+            self.t_delete_ms, self.t_append_ms = d, a
+
+    out = bench.front_roofline("rmat22", [S(0.14, 0.08), S(0.16, 0.10)], 6771.1)
+    dele, app = out["k_delete"], out["k_append"]
+    assert abs(dele["ms_per_launch"] - 0.15) < 1e-12 and abs(app["ms_per_launch"] - 0.09) < 1e-12
+    assert abs(dele["achieved_dram_gbs"] - dele["traffic"] / 0.15e-3 / 1e9) < 1e-6
+    assert abs(dele["frac_dram"] - dele["achieved_dram_gbs"] / 6771.1) < 1e-12
+    assert 0 < app["frac_dram"] < dele["frac_dram"] < 1
