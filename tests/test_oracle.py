@@ -98,3 +98,18 @@ def test_dijkstra_exact_mode_ignores_cap():
     assert p_cap.tolist() == [0, -1, -1]
     d, p = O.dijkstra(3, g, 0)
     assert d.tolist() == [0, 600000, 1200000] and p.tolist() == [0, 0, 1]
+
+
+def test_reference_dijkstra_timing_harness():
+    """oracle/time_ref.py times the reference's compiled djk (oracle/_ref/ref_time) and the
+    restatement on the same updated graph (here the small ER workload)."""
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parent.parent
+    if not (root / "oracle" / "_ref" / "ref_time").exists():
+        pytest.skip("the reference's sources were not available to build oracle/_ref/ref_time")
+    out = subprocess.run([sys.executable, str(root / "oracle" / "time_ref.py"), "--workload", "er10k", "--reps", "1"],
+                         capture_output=True, text=True, timeout=300, check=True).stdout
+    assert "reference djk" in out and "oracle restatement" in out
