@@ -8,7 +8,9 @@ Runs only where the reference sources are present (it builds oracle/_ref/ first)
 Case 0 is the reference's own sample (graph.txt / SSSP.txt / cE.txt, README.md:18).  The
 other cases are seeded random graphs with the edge cases the engine must handle: weight-0
 edges, parallel edges, deletions of absent edges, insert+delete of the same edge in one batch,
-disconnected vertices.  The updated-graph file given to op_ssspSeq is built here in plain
+disconnected vertices; and shaped ones: a cut-off subtree deeper than the walk's level limit,
+a hub losing many edges, a source losing all of its edges, a batch of ignored records only,
+repeated records.  The updated-graph file given to op_ssspSeq is built here in plain
 Python from the batch semantics (insertions appended, then every line matching a deletion's
 endpoint pair and weight removed), independently of oracle/oracle.c.
 
@@ -109,6 +111,39 @@ def random_case(rng: np.random.Generator, n: int, m: int, wmax: int, n_ins: int,
     return edges, [changes[i] for i in order]
 
 
+def shaped_cases(rng: np.random.Generator):
+    """Cases of a fixed shape: a long path with chords (a cut-off subtree deeper than the
+    subtree walk's level limit), a star (a hub's edges deleted, leaves joined), the source's
+    every edge deleted, a batch of ignored records only, and repeated records."""
+    cases = []
+    n = 300  # path 0-1-...-299 with a few chords; deleting (3, 4) cuts off ~290 levels, which
+    # the chord (2, 60) reaches again from the middle
+    edges = [(i, i + 1, int(rng.integers(1, 10))) for i in range(n - 1)]
+    edges += [(int(a), int(a) + int(rng.integers(5, 40)), int(rng.integers(50, 200)))
+              for a in rng.integers(0, n - 41, 12)]
+    edges.append((2, 60, 150))
+    changes = [(3, 4, edges[3][2], 0), (150, 151, edges[150][2], 0), (10, 200, 500, 1), (7, 9, 3, 1)]
+    cases.append(("deep_path", n, edges, changes))
+    n = 80  # star around 0, a few leaf-leaf edges
+    edges = [(0, i, int(rng.integers(1, 20))) for i in range(1, n)]
+    edges += [(int(a), int(b), int(rng.integers(1, 40))) for a, b in rng.integers(1, n, (30, 2)) if a != b]
+    changes = [(0, i, edges[i - 1][2], 0) for i in range(1, n, 3)]
+    changes += [(int(a), int(b), int(rng.integers(1, 40)), 1) for a, b in rng.integers(1, n, (20, 2)) if a != b]
+    cases.append(("star_hub_deletions", n, edges, [changes[i] for i in rng.permutation(len(changes))]))
+    n = 50  # every edge of the source deleted: everything else becomes unreachable
+    edges = [(int(a), int(b), int(rng.integers(1, 30))) for a, b in rng.integers(0, n, (150, 2)) if a != b]
+    changes = [(a, b, w, 0) for (a, b, w) in edges if a == 0 or b == 0]
+    cases.append(("source_isolated", n, edges, changes))
+    edges = [(int(a), int(b), int(rng.integers(1, 30))) for a, b in rng.integers(0, n, (150, 2)) if a != b]
+    cases.append(("ignored_records_only", n, edges, [(1, 2, 3, 5), (4, 5, 6, 2), (7, 8, 9, -1)]))
+    edges = [(int(a), int(b), int(rng.integers(1, 30))) for a, b in rng.integers(0, n, (150, 2)) if a != b]
+    a, b, w = edges[5]
+    c, d, x = edges[9]
+    changes = [(a, b, w, 0), (b, a, w, 0), (a, b, w, 0), (1, 40, 4, 1), (40, 1, 4, 1), (1, 40, 4, 1), (c, d, x, 0)]
+    cases.append(("repeated_records", n, edges, changes))
+    return cases
+
+
 def make_case(tmp: Path, name: str, n: int, edges, changes, sssp_rows=None):
     g = tmp / f"{name}_graph.txt"
     s = tmp / f"{name}_SSSP.txt"
@@ -159,6 +194,8 @@ def main() -> int:
         ]
         for name, n, m, wmax, ni, nd, extras in specs:
             edges, changes = random_case(rng, n, m, wmax, ni, nd, extras)
+            cases.append(make_case(tmp, name, n, edges, changes))
+        for name, n, edges, changes in shaped_cases(np.random.default_rng(20261204)):
             cases.append(make_case(tmp, name, n, edges, changes))
     out = HERE / "golden.json"
     out.write_text(json.dumps({"generator": "tests/golden/make_golden.py", "cases": cases}, separators=(",", ":")))
