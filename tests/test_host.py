@@ -285,3 +285,37 @@ def test_bench_reads_the_committed_profiles():
     assert abs(dele["achieved_dram_gbs"] - dele["traffic"] / 0.15e-3 / 1e9) < 1e-6
     assert abs(dele["frac_dram"] - dele["achieved_dram_gbs"] / 6771.1) < 1e-12
     assert 0 < app["frac_dram"] < dele["frac_dram"] < 1
+
+
+def test_serving_and_tuning_helpers():
+    """Host-side helpers of the batching and serving layers: request summaries (p50/p99,
+    refused and failed requests), random tenant batches, the autotuner's size classes, near-far
+    candidates and cache file, and the footprint estimate's growth."""
+    from dynamicssspv2_gb300.autotune import Autotuner, size_class
+    from dynamicssspv2_gb300.serve import Request, Tenant, estimate_footprint, random_batch, summarize
+
+    ch = np.zeros(10, D.CHANGE_DTYPE)
+    reqs = [Request(0, 0.001 * i, ch, epoch=i // 2, done=0.001 * i + 0.002) for i in range(10)]
+    reqs.append(Request(1, 0.0, ch, refused=True))
+    reqs.append(Request(0, 0.0, ch, error="bad vertex"))
+    s = summarize(reqs)
+    assert s["requests"] == 12 and s["served"] == 10 and s["refused"] == 1 and s["failed"] == 1
+    assert s["changes"] == 100 and abs(s["p50_ms"] - 2.0) < 1e-9 and abs(s["p99_ms"] - 2.0) < 1e-9
+    assert s["epochs"] == 5 and s["mean_requests_per_epoch"] == 2.0
+    assert summarize([])["p99_ms"] is None
+
+    u, v, w = D.gen_er(100, 300, 1, 9, seed=2)
+    t = Tenant("t", 100, u, v, w)
+    b = random_batch(np.random.default_rng(3), t, 50, ins_frac=0.4)
+    assert len(b) == 50 and (b["op"] == 1).sum() == 20 and (b["u"] != b["v"])[b["op"] == 1].all()
+    dels = b[b["op"] == 0]
+    lines = set(zip(u.tolist(), v.tolist(), w.tolist()))
+    assert all((x, y, z) in lines for x, y, z in zip(dels["u"].tolist(), dels["v"].tolist(), dels["w"].tolist()))
+
+    assert size_class(1 << 20, 1 << 24, 1000) == "v20_e24_b10"
+    wbar = float(np.mean(b["w"]))
+    cands = Autotuner.near_far_candidates(b)
+    assert [c["delta"] for c in cands] == [max(1, int(round(f * wbar))) for f in (8.0, 96.0)]
+    assert Autotuner.near_far_candidates(np.zeros(0, D.CHANGE_DTYPE)) == []
+
+    assert estimate_footprint(1000, 4000) < estimate_footprint(2000, 4000) < estimate_footprint(2000, 8000)
