@@ -7,6 +7,7 @@
 // leave stale values), and an out-of-range vertex id is an error code instead of an
 // uncaught std::out_of_range.
 #include <cerrno>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -19,6 +20,9 @@
 
 namespace dsssp {
 namespace {
+
+// "no out-of-range vertex id in this chunk" (any id a file can name, -1 included, is reported)
+constexpr long long kNoBadId = LLONG_MIN;
 
 struct FileBuf {
     std::vector<char> data;
@@ -50,7 +54,12 @@ inline bool next_int(const char*& p, const char* end, long long& out, bool* flt)
     if (*p == '-' || *p == '+') { neg = *p == '-'; p++; }
     long long v = 0;
     bool any = false;
-    while (p < end && *p >= '0' && *p <= '9') { v = v * 10 + (*p - '0'); p++; any = true; }
+    while (p < end && *p >= '0' && *p <= '9') {  // saturates: such a value is out of range anyway
+        const int d = *p - '0';
+        v = v > (LLONG_MAX - d) / 10 ? LLONG_MAX : v * 10 + d;
+        p++;
+        any = true;
+    }
     if (p < end && (*p == '.' || *p == 'e' || *p == 'E')) {
         char* q = nullptr;
         double d = strtod(s, &q);
@@ -105,7 +114,7 @@ int dsssp_read_graph_file(const char* path, int32_t n, int32_t** u, int32_t** v,
     if (rc) return rc;
     const int T = chunks_for(fb.data.size());
     std::vector<std::vector<int32_t>> A((size_t)T), B((size_t)T), W((size_t)T);
-    std::vector<long long> bad((size_t)T, -1);
+    std::vector<long long> bad((size_t)T, kNoBadId);
     parallel_lines(fb, [&](int t, const char* p, const char* end) {
         while (p < end) {
             long long x[3];
@@ -121,7 +130,7 @@ int dsssp_read_graph_file(const char* path, int32_t n, int32_t** u, int32_t** v,
         }
     }, T);
     for (int t = 0; t < T; t++)
-        if (bad[(size_t)t] != -1)
+        if (bad[(size_t)t] != kNoBadId)
             return fail(DSSSP_E_BAD_VERTEX, "%s: vertex id %lld outside 0..%d", path, bad[(size_t)t], n - 1);
     size_t tot = 0;
     for (int t = 0; t < T; t++) tot += A[(size_t)t].size();
@@ -132,6 +141,7 @@ int dsssp_read_graph_file(const char* path, int32_t n, int32_t** u, int32_t** v,
     size_t o = 0;
     for (int t = 0; t < T; t++) {
         size_t s = A[(size_t)t].size();
+        if (s == 0) continue;
         memcpy(a + o, A[(size_t)t].data(), s * 4);
         memcpy(b + o, B[(size_t)t].data(), s * 4);
         memcpy(c + o, W[(size_t)t].data(), s * 4);
@@ -148,7 +158,7 @@ int dsssp_read_changes_file(const char* path, int32_t n, dsssp_change** changes,
     if (rc) return rc;
     const int T = chunks_for(fb.data.size());
     std::vector<std::vector<dsssp_change>> C((size_t)T);
-    std::vector<long long> bad((size_t)T, -1);
+    std::vector<long long> bad((size_t)T, kNoBadId);
     parallel_lines(fb, [&](int t, const char* p, const char* end) {
         while (p < end) {
             long long x[4];
@@ -165,14 +175,18 @@ int dsssp_read_changes_file(const char* path, int32_t n, dsssp_change** changes,
         }
     }, T);
     for (int t = 0; t < T; t++)
-        if (bad[(size_t)t] != -1)
+        if (bad[(size_t)t] != kNoBadId)
             return fail(DSSSP_E_BAD_VERTEX, "%s: vertex id %lld outside 0..%d", path, bad[(size_t)t], n - 1);
     size_t tot = 0;
     for (auto& c : C) tot += c.size();
     dsssp_change* out = (dsssp_change*)malloc(sizeof(dsssp_change) * (tot ? tot : 1));
     if (!out) return fail(DSSSP_E_OOM, "read_changes: out of host memory");
     size_t o = 0;
-    for (auto& c : C) { memcpy(out + o, c.data(), c.size() * sizeof(dsssp_change)); o += c.size(); }
+    for (auto& c : C) {
+        if (c.empty()) continue;
+        memcpy(out + o, c.data(), c.size() * sizeof(dsssp_change));
+        o += c.size();
+    }
     *changes = out;
     *k = (int64_t)tot;
     return DSSSP_OK;
@@ -186,7 +200,7 @@ int dsssp_read_sssp_file(const char* path, int32_t n, int32_t* parent, int64_t* 
     if (rc) return rc;
     for (int32_t i = 0; i < n; i++) { parent[i] = -1; dist[i] = DSSSP_UNREACHABLE; }
     const int T = chunks_for(fb.data.size());
-    std::vector<long long> bad((size_t)T, -1), nflt((size_t)T, 0);
+    std::vector<long long> bad((size_t)T, kNoBadId), nflt((size_t)T, 0);
     // every vertex appears on at most one line in a well-formed file; with duplicates the
     // last line in file order wins (as in the reference), so chunks are applied in order
     std::vector<std::vector<long long>> rows((size_t)T);
@@ -207,7 +221,7 @@ int dsssp_read_sssp_file(const char* path, int32_t n, int32_t* parent, int64_t* 
         }
     }, T);
     for (int t = 0; t < T; t++)
-        if (bad[(size_t)t] != -1)
+        if (bad[(size_t)t] != kNoBadId)
             return fail(DSSSP_E_BAD_VERTEX, "%s: vertex id %lld outside 0..%d", path, bad[(size_t)t], n - 1);
     long long nl = 0;
     for (int t = 0; t < T; t++) {

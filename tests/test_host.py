@@ -143,6 +143,15 @@ def test_out_of_range_vertex_and_missing_file(tmp_path):
     assert e.value.code == D.E_BAD_VERTEX
     c.write_text("0 7 1 3\n")  # ignored op: not checked, as in the reference
     assert len(D.read_changes(str(c), 6)) == 1
+    # every out-of-range id is reported, -1 and ids beyond 64 bits included
+    for text, reader in (("-1 2 3\n", D.read_graph), ("2 -1 3\n", D.read_graph),
+                         ("1 99999999999999999999999 3\n", D.read_graph), ("-1 2 3 0\n", D.read_changes),
+                         ("0 -1 3 1\n", D.read_changes), ("-1 0 0\n", D.read_sssp)):
+        f = tmp_path / "bad.txt"
+        f.write_text("0 1 2 1\n" + text)
+        with pytest.raises(D.DsssspError) as e:
+            reader(str(f), 6)
+        assert e.value.code == D.E_BAD_VERTEX, (text, reader)
 
 
 def test_sssp_file_semantics(tmp_path):
