@@ -93,6 +93,15 @@ int read_header(FILE* f, const char* path, const char (&magic)[8], Header& h) {
     return DSSSP_OK;
 }
 
+// Bytes from the current position to the end of f (the position is kept); -1 if unknown.
+long long bytes_left(FILE* f) {
+    const long here = ftell(f);
+    if (here < 0 || fseek(f, 0, SEEK_END) != 0) return -1;
+    const long end = ftell(f);
+    if (fseek(f, here, SEEK_SET) != 0 || end < here) return -1;
+    return (long long)(end - here);
+}
+
 int read_parts(FILE* f, const char* path, const std::vector<Part>& parts, uint64_t want) {
     for (const Part& pt : parts)
         if (pt.bytes && fread(const_cast<void*>(pt.p), 1, pt.bytes, f) != pt.bytes)
@@ -120,7 +129,12 @@ int dsssp_read_graph_binary(const char* path, int32_t n, int32_t** u, int32_t** 
     Header h;
     int rc = read_header(f, path, kGraphMagic, h);
     if (!rc && h.a != n) rc = fail(DSSSP_E_IO, "%s: cached graph has %lld vertices, not %d", path, (long long)h.a, n);
-    if (!rc && h.b < 0) rc = fail(DSSSP_E_IO, "%s: bad edge count", path);
+    // the header's edge count must match the file's size before anything is allocated for it
+    if (!rc) {
+        const long long left = bytes_left(f), per_edge = 3 * (long long)sizeof(int32_t);
+        if (h.b < 0 || left < 0 || h.b > left / per_edge || h.b * per_edge != left)
+            rc = fail(DSSSP_E_IO, "%s: the edge count in the header does not match the file size", path);
+    }
     int32_t *a = nullptr, *bb = nullptr, *c = nullptr;
     if (!rc) {
         const size_t bytes = sizeof(int32_t) * (size_t)(h.b ? h.b : 1);
@@ -167,6 +181,8 @@ int dsssp_read_sssp_binary(const char* path, int32_t n, int32_t* parent, int64_t
     Header h;
     int rc = read_header(f, path, kTreeMagic, h);
     if (!rc && h.a != n) rc = fail(DSSSP_E_IO, "%s: cached tree has %lld vertices, not %d", path, (long long)h.a, n);
+    if (!rc && bytes_left(f) != (long long)(sizeof(int32_t) + sizeof(int64_t)) * n)
+        rc = fail(DSSSP_E_IO, "%s: the file size does not match a tree of %d vertices", path, n);
     if (!rc)
         rc = read_parts(f, path, {{parent, sizeof(int32_t) * (size_t)n}, {dist, sizeof(int64_t) * (size_t)n}}, h.sum);
     fclose(f);

@@ -226,6 +226,18 @@ def test_graph_binary_round_trip_and_rejections(tmp_path):
     empty = tmp_path / "e.bin"
     D.write_graph_binary(str(empty), 5, [], [], [])
     assert all(len(a) == 0 for a in D.read_graph_binary(str(empty), 5))
+    # a header whose edge count disagrees with the file (here: ~10^18 edges) is refused before
+    # anything is allocated for it; so are trailing bytes
+    data = bytearray(path.read_bytes())
+    data[16:24] = (0x0C00000000000FA0).to_bytes(8, "little")
+    bad.write_bytes(bytes(data))
+    with pytest.raises(D.DsssspError) as e:
+        D.read_graph_binary(str(bad), 1 << 12)
+    assert e.value.code == D.E_IO and "file size" in str(e.value)
+    bad.write_bytes(path.read_bytes() + b"\0" * 12)
+    with pytest.raises(D.DsssspError) as e:
+        D.read_graph_binary(str(bad), 1 << 12)
+    assert e.value.code == D.E_IO
 
 
 def test_tree_binary_round_trip(tmp_path):
