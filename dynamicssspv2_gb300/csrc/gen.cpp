@@ -5,6 +5,7 @@
 // same output on any host and with any thread count.  "Exactly m distinct pairs" is defined
 // as: draw candidates 0..D-1, deduplicate, and keep the m distinct pairs with the smallest
 // hash; D grows until at least m distinct pairs exist.
+#include <cmath>
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
@@ -86,7 +87,9 @@ void radix_sort_u64(std::vector<uint64_t>& keys) {
 }
 
 // Draws candidates with draw(i) -> key (~0ull = rejected), keeps the m distinct keys with the
-// smallest hash, returns them sorted by that hash (a random order).
+// smallest hash, returns them sorted by that hash (a random order).  Gives up (false) once the
+// draws pass 64 m + 2^20 without m distinct keys: the parameters cannot give that many (too
+// few possible pairs, or a distribution that keeps drawing the same ones).
 template <class Draw>
 static bool distinct_keys(int64_t m, const Stream& hs, Draw draw, std::vector<uint64_t>& out) {
     int64_t D = m + m / 8 + 64;
@@ -114,6 +117,7 @@ static bool distinct_keys(int64_t m, const Stream& hs, Draw draw, std::vector<ui
             return true;
         }
         D = D + D / 2 + (m - (int64_t)u) * 2;
+        if (D > 64 * m + (1 << 20)) break;
     }
     return false;
 }
@@ -191,6 +195,8 @@ int dsssp_gen_rmat(int32_t scale, int64_t m, double a, double b, double c, int32
     if (scale < 1 || scale > 30 || m < 0 || a < 0 || b < 0 || c < 0 || a + b + c > 1.0 ||
         wlo < 0 || whi < wlo || !u || !v || !w)
         return fail(DSSSP_E_INVAL, "gen_rmat: bad arguments");
+    if ((double)m > std::ldexp(1.0, scale) * (std::ldexp(1.0, scale) - 1) / 2.0)
+        return fail(DSSSP_E_INVAL, "gen_rmat: %lld pairs do not exist on 2^%d vertices", (long long)m, scale);
     Stream ps(seed, 11), hs(seed, 12), ws(seed, 13);
     const double ab = a + b, abc = a + b + c;
     std::vector<uint64_t> keys;
@@ -244,6 +250,9 @@ int dsssp_gen_grid(int32_t rows, int32_t cols, double remove_frac, int64_t n_dia
     std::vector<uint64_t> diag;
     if (n_diag > 0) {
         if (rows < 2 || cols < 2) return fail(DSSSP_E_INVAL, "gen_grid: no diagonals on a line");
+        if (n_diag > 2 * (int64_t)(rows - 1) * (cols - 1))
+            return fail(DSSSP_E_INVAL, "gen_grid: a %d x %d grid has only %lld diagonals", rows, cols,
+                        2 * (long long)(rows - 1) * (cols - 1));
         bool ok = distinct_keys(n_diag, hs, [&](uint64_t i) {
             int64_t r = ds.range(3 * i, 0, rows - 1), c = ds.range(3 * i + 1, 0, cols - 1);
             int64_t d = ds.range(3 * i + 2, 0, 3);
@@ -342,7 +351,7 @@ int dsssp_gen_changes(int32_t n, int64_t m, const int32_t* eu, const int32_t* ev
     }
     dsssp_change* res = (dsssp_change*)malloc(sizeof(dsssp_change) * (out.size() ? out.size() : 1));
     if (!res) return fail(DSSSP_E_OOM, "gen_changes: host allocation failed");
-    memcpy(res, out.data(), sizeof(dsssp_change) * out.size());
+    if (!out.empty()) memcpy(res, out.data(), sizeof(dsssp_change) * out.size());
     *changes = res;
     return DSSSP_OK;
 }
@@ -385,7 +394,7 @@ int dsssp_gen_changes_ref(int32_t n, int64_t m, const int32_t* eu, const int32_t
     }
     dsssp_change* res = (dsssp_change*)malloc(sizeof(dsssp_change) * (out.size() ? out.size() : 1));
     if (!res) return fail(DSSSP_E_OOM, "gen_changes_ref: host allocation failed");
-    memcpy(res, out.data(), sizeof(dsssp_change) * out.size());
+    if (!out.empty()) memcpy(res, out.data(), sizeof(dsssp_change) * out.size());
     *changes = res;
     return DSSSP_OK;
 }

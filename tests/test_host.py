@@ -340,3 +340,22 @@ def test_serving_and_tuning_helpers():
     assert Autotuner.near_far_candidates(np.zeros(0, D.CHANGE_DTYPE)) == []
 
     assert estimate_footprint(1000, 4000) < estimate_footprint(2000, 4000) < estimate_footprint(2000, 8000)
+
+
+def test_generators_refuse_impossible_requests():
+    """More distinct pairs than exist, or a distribution that keeps drawing the same pair, is
+    an error rather than an endless draw."""
+    for call in (lambda: D.gen_er(10, 46, 1, 5, 1),
+                 lambda: D.gen_rmat(2, 7, 0.57, 0.19, 0.19, 1, 10, 2),
+                 lambda: D.gen_rmat(1, 2, 0.57, 0.19, 0.19, 1, 10, 2),
+                 lambda: D.gen_rmat(3, 10, 1.0, 0.0, 0.0, 1, 10, 2),   # every draw is the self-loop (0, 0)
+                 lambda: D.gen_grid(3, 3, 0.0, 100, 1, 5, 3)):         # 8 diagonals exist
+        with pytest.raises(D.DsssspError) as e:
+            call()
+        assert e.value.code == D.E_INVAL
+    assert len(D.gen_rmat(2, 6, 0.57, 0.19, 0.19, 1, 10, 2)[0]) == 6   # every pair of 4 vertices
+    assert len(D.gen_grid(3, 3, 0.0, 8, 1, 5, 3)[0]) == 12 + 8
+    u, v, w = D.gen_er(20, 60, 1, 9, seed=1)
+    with pytest.raises(D.DsssspError):
+        D.gen_changes(20, u, v, w, 500, 0)   # only 130 new pairs
+    assert len(D.gen_changes(20, u, v, w, 0, 0)) == 0
