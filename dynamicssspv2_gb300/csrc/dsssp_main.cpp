@@ -16,6 +16,7 @@
 // which the reference never does.  Exit status is 0 on success, 1 on any error.
 #include <sys/stat.h>
 
+#include <cerrno>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -38,6 +39,16 @@ static bool cache_fresh(const std::string& cache, const char* text) {
     return a.st_mtime >= b.st_mtime;
 }
 
+// A whole decimal integer argument within [lo, hi] (atoi would accept "12abc" or wrap around).
+static bool parse_int(const char* s, long long lo, long long hi, long long& out) {
+    char* end = nullptr;
+    errno = 0;
+    const long long v = strtoll(s, &end, 10);
+    if (errno != 0 || end == s || *end != '\0' || v < lo || v > hi) return false;
+    out = v;
+    return true;
+}
+
 static int die(const char* what, int rc) {
     fprintf(stderr, "dsssp_main: %s failed: %s (%s)\n", what, dsssp_strerror(rc), dsssp_last_error());
     return 1;
@@ -56,23 +67,30 @@ int main(int argc, char** argv) {
     bool use_cache = false;
     dsssp_opts opts;
     dsssp_default_opts(&opts);
+    long long val = 0;
     for (int i = 6; i < argc; i++) {
-        if (!strcmp(argv[i], "--out") && i + 1 < argc) out_path = argv[++i];
-        else if (!strcmp(argv[i], "--json") && i + 1 < argc) json_path = argv[++i];
-        else if (!strcmp(argv[i], "--device") && i + 1 < argc) opts.device = atoi(argv[++i]);
-        else if (!strcmp(argv[i], "--delta") && i + 1 < argc) opts.delta = atoi(argv[++i]);
+        const bool has_value = i + 1 < argc;
+        if (!strcmp(argv[i], "--out") && has_value) out_path = argv[++i];
+        else if (!strcmp(argv[i], "--json") && has_value) json_path = argv[++i];
+        else if (!strcmp(argv[i], "--device") && has_value && parse_int(argv[i + 1], 0, 1023, val)) opts.device = (int)val, i++;
+        else if (!strcmp(argv[i], "--delta") && has_value && parse_int(argv[i + 1], -1, 2147483647, val)) opts.delta = (int)val, i++;
         else if (!strcmp(argv[i], "--cache")) use_cache = true;
         else {
-            fprintf(stderr, "dsssp_main: unknown option %s\n", argv[i]);
+            fprintf(stderr, "dsssp_main: bad option %s%s%s\n", argv[i], has_value ? " " : " (no value)",
+                    has_value ? argv[i + 1] : "");
             return 2;
         }
     }
-    const int nodes = atoi(argv[2]);
-    const long long edges_arg = atoll(argv[3]);
-    if (nodes <= 0) {
-        fprintf(stderr, "dsssp_main: number_of_nodes must be positive\n");
+    long long nodes_arg = 0, edges_arg = 0;
+    if (!parse_int(argv[2], 1, 2147483646, nodes_arg)) {
+        fprintf(stderr, "dsssp_main: number_of_nodes must be an integer in 1..2147483646, not %s\n", argv[2]);
         return 2;
     }
+    if (!parse_int(argv[3], 0, 9223372036854775807LL, edges_arg)) {
+        fprintf(stderr, "dsssp_main: number_of_edges must be a non-negative integer, not %s\n", argv[3]);
+        return 2;
+    }
+    const int nodes = (int)nodes_arg;
 
     printf("Reading input graph...\n");
     auto t0 = clk::now();

@@ -194,6 +194,15 @@ def test_cli_usage_and_errors(tmp_path):
                        text=True)
     assert r.returncode == 1 and "reading the graph" in r.stderr
     assert r.stdout.startswith("Reading input graph...")
+    g = tmp_path / "g.txt"
+    g.write_text("0 1 2\n")
+    for args, msg in ((["abc", "1"], "number_of_nodes"), (["99999999999", "1"], "number_of_nodes"),
+                      (["0", "1"], "number_of_nodes"), (["3", "-1"], "number_of_edges"), (["3", "2x"], "number_of_edges"),
+                      (["3", "1", "--delta", "x"], "bad option --delta"), (["3", "1", "--out"], "bad option --out"),
+                      (["3", "1", "--device", "7b"], "bad option --device")):
+        r = subprocess.run([str(D.CLI_PATH), str(g), args[0], args[1], "s", "c"] + args[2:], capture_output=True,
+                           text=True)
+        assert r.returncode == 2 and msg in r.stderr, (args, r.stderr)
 
 
 # ---- binary cache, the reference generator's format and sampling -----------------------------
