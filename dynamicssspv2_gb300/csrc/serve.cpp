@@ -458,17 +458,19 @@ int dsssp_submit_many(dsssp_server* s, int32_t count, const int32_t* tenants, co
                       const int64_t* sizes, int64_t* ids) {
     if (!s || count < 0 || (count > 0 && (!tenants || !batches || !sizes || !ids)))
         return fail(DSSSP_E_INVAL, "submit: bad arguments");
-    std::lock_guard<std::mutex> lk(s->mu);
+    // Validation and the copy of each batch happen before the lock: the worker takes the same
+    // lock between epochs, so holding it only to number and queue the requests keeps a large
+    // submission off the other requests' latency.  (Admission and tenant sizes are fixed.)
     const double t = s->now_us();
+    std::vector<Req*> reqs((size_t)count);
     for (int32_t i = 0; i < count; i++) {
         Req* r = new Req();
+        reqs[(size_t)i] = r;
         memset(&r->info, 0, sizeof(r->info));
-        r->info.id = s->next_id++;
         r->info.tenant = tenants[i];
         r->info.changes = sizes[i];
         r->info.arrival_us = t;
         r->info.epoch = -1;
-        ids[i] = r->info.id;
         const bool known = tenants[i] >= 0 && tenants[i] < (int32_t)s->slot.size();
         if (!known || s->slot[(size_t)tenants[i]] < 0) {
             r->info.status = DSSSP_REFUSED;
@@ -483,13 +485,23 @@ int dsssp_submit_many(dsssp_server* s, int32_t count, const int32_t* tenants, co
                 snprintf(r->info.error, sizeof r->info.error, "%s", why.c_str());
             } else {
                 r->ch.assign(batches[i], batches[i] + sizes[i]);
-                s->queues[(size_t)s->slot[(size_t)tenants[i]]].push_back(r);
-                s->pending++;
-                continue;
             }
         }
-        r->info.start_us = r->info.done_us = t;
-        s->complete(r);
+    }
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        for (int32_t i = 0; i < count; i++) {
+            Req* r = reqs[(size_t)i];
+            r->info.id = s->next_id++;
+            ids[i] = r->info.id;
+            if (r->info.status == 0) {
+                s->queues[(size_t)s->slot[(size_t)r->info.tenant]].push_back(r);
+                s->pending++;
+            } else {
+                r->info.start_us = r->info.done_us = t;
+                s->complete(r);
+            }
+        }
     }
     s->cv_work.notify_one();
     return DSSSP_OK;
