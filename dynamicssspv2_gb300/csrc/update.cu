@@ -613,9 +613,10 @@ __device__ __forceinline__ bool small_step(unsigned nt, unsigned nc) {
     return (nt + blockDim.x - 1) / blockDim.x + nc <= kSoloWaves;
 }
 
-// Processes one step's work: CTA items (one CTA per chunk of a long row), then thread
-// items (te edges each) in one grid-stride wave, over CTAs cta, cta + 1, ... of ncta (the
-// whole grid, or CTA 0 alone for a small step).
+// Processes one step's work on ncta CTAs (the whole grid, or CTA 0 alone for a small step;
+// this CTA is number cta of them): CTA items first (one CTA per chunk of a long row; CTA
+// items cta, cta + ncta, ...), then thread items (te edges each) in one grid-stride wave over
+// the ncta CTAs' threads.
 template <class Op>
 __device__ void run_items(Op& op, const UpdParams& p, const Item* tl, unsigned nt, const Item* cl, unsigned nc,
                           unsigned cta, unsigned ncta) {
