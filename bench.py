@@ -13,6 +13,15 @@ restored from a device snapshot and a 256 MB buffer is written (L2 flush); neith
            batch records already in HBM), summed over all ranks' work / max over ranks
   e2e    = the same metric through the public C ABI with host buffers: dsssp_apply_batch
            from pinned host memory + dsssp_tree_read into pinned host memory, host clock
+On one GPU the default line also carries the other halves of the metric, measured after the
+headline on the same GPU:
+  batched_over_plain      the batch256 workload: 256 graphs' batches in one launch sequence of a
+                          pooled store against the same batches applied one by one (device time)
+  serve                   the serve workload: capacity, then p50/p99 latency and throughput at
+                          offered loads of 0.25-1.1 x capacity (continuous batching)
+  served_over_one_by_one  the saturated serving stream applied one request at a time by the
+                          plain update, against the served capacity on the same stream
+(--headline-only skips them.)
 Multi-GPU (torchrun): the update of one graph does not shard, so every rank runs an
 independent replica (weak scaling, no collective on the data path).
 
@@ -417,8 +426,8 @@ def run_engine(args, dist: Dist) -> int:
                          f"of the updated graph, {ct:.2f} s, 1 of {host_cores()} host cores"}
     clocks = clk.summary()
     g.close()
-    dist.close()
     if dist.rank != 0:
+        dist.close()
         return 0
     cfg = describe(args.workload)
     cfg.update({"parallelism": f"replicas x{dist.world}", "l2": "graph restore (>1 GB written) + 256 MB flush "
@@ -471,8 +480,43 @@ def run_engine(args, dist: Dist) -> int:
             "step_ms": t_steps,
         },
     }
+    if args.workload == "rmat22" and dist.world == 1 and not args.headline_only:
+        line.update(extra_workloads(args, dist))
+    dist.close()
     print(json.dumps(line), flush=True)
     return 0
+
+
+def extra_workloads(args, dist: Dist) -> dict:
+    """The batching and serving halves of the metric, run after the headline on the same GPU
+    (one at a time; each frees its device memory before the next): batched over plain on the
+    256-graph workload, and p50/p99 under load with the served-over-one-by-one ratio on the
+    serving workload."""
+    out = {}
+    steps, warmup = max(3, min(args.steps, 10)), max(3, min(args.warmup, 3))
+    b = batching_summary("batch256", steps, warmup, dist)
+    out["batched_over_plain"] = {
+        "ratio": b["batched_over_plain"], "workload": "batch256",
+        "batched": {"value": b["value"], "unit": b["unit"], "ms_per_step": b["ms_per_step"],
+                    "wall_ms_per_step": b["batched_wall_ms_per_step"]},
+        "plain": b["plain"], "steps": b["steps"], "warmup": b["warmup"],
+        "mismatched_distances": b["mismatched_distances"], "gpu_launches": b["gpu_launches"],
+        "graphs": b["config"]["graphs"], "vertices": b["config"]["vertices"], "edges": b["config"]["edges"],
+        "changes": b["config"]["changes"], "autotuned": b["config"]["autotuned"], "clocks": b["clocks"],
+        "timed": "device time (CUDA events) of the batch kernels: one union batch through one launch sequence of "
+                 "the pooled store, against the 256 batches applied one by one to graph stores of their own; "
+                 "restore + 256 MB L2 flush before each update untimed"}
+    s = serving_summary("serve", dist)
+    keep = ("offered_load", "offered_requests_per_s", "requests", "served", "changes", "change_edges_per_s",
+            "p50_ms", "p99_ms", "mean_ms", "mean_requests_per_epoch", "certificate_violations")
+    out["serve"] = {
+        "workload": "serve", "capacity_change_edges_per_s": s["capacity"]["change_edges_per_s"],
+        "loads": [{k: ld[k] for k in keep} for ld in s["loads"]],
+        "admitted": s["config"]["admitted"], "vertices": s["config"]["vertices"], "edges": s["config"]["edges"],
+        "checked_tenants": s["checked_tenants"], "mismatched_distances": s["mismatched_distances"],
+        "clocks": s["clocks"], "timed": s["config"]["timed"]}
+    out["served_over_one_by_one"] = s["one_by_one"]
+    return out
 
 
 def make_batch_inputs(name: str):
@@ -499,6 +543,14 @@ def make_batch_inputs(name: str):
 
 
 def run_batching(args, dist: Dist) -> int:
+    line = batching_summary(args.workload, args.steps, args.warmup, dist)
+    dist.close()
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def batching_summary(workload: str, steps: int, warmup: int, dist: Dist) -> dict:
     """Many graphs: one batch per graph applied one by one with the plain update, against all
     of them together in one launch sequence on a pooled graph store (autotuned)."""
     import tempfile
@@ -512,14 +564,14 @@ def run_batching(args, dist: Dist) -> int:
     dev = dist.local
     torch.cuda.set_device(dev)
     t0 = time.perf_counter()
-    items = make_batch_inputs(args.workload)
+    items = make_batch_inputs(workload)
     t_gen = time.perf_counter() - t0
     total_changes = sum(len(it[4]) for it in items)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
 
     # plain: one graph store per graph, batches applied one after another
     plain = []
-    wl = WORKLOADS[args.workload]
+    wl = WORKLOADS[workload]
     slack = {"slack_pct": wl["slack_pct"], "slack_min": wl["slack_min"]}
     for n, u, v, wt, ch in items:
         g = D.Graph(n, u, v, wt, device=dev, **slack)
@@ -560,7 +612,7 @@ def run_batching(args, dist: Dist) -> int:
         st = pool.graph.batch_finish()
         return st.t_total_ms * 1e-3, time.perf_counter() - w0, st
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         plain_pass()
         pooled_pass()
     clk = ClockSampler(dev).__enter__()
@@ -569,7 +621,7 @@ def run_batching(args, dist: Dist) -> int:
     dist.barrier()
     pd, pw, bd, bw, stats, repacks = 0.0, 0.0, 0.0, 0.0, None, 0
     launches0 = D.launch_count()
-    for _ in range(args.steps):
+    for _ in range(steps):
         a, b = plain_pass()
         pd += a
         pw += b
@@ -586,15 +638,12 @@ def run_batching(args, dist: Dist) -> int:
         p_plain, d_plain = g.tree_read()
         p_pool, d_pool = pool.tree_read(i)
         mismatches += int((d_plain != d_pool).sum())
-    value, t_max = whole_job_rate(dist, total_changes, args.steps, bd)
-    plain_value, _ = whole_job_rate(dist, total_changes, args.steps, pd)
+    value, t_max = whole_job_rate(dist, total_changes, steps, bd)
+    plain_value, _ = whole_job_rate(dist, total_changes, steps, pd)
     for g, _, _ in plain:
         g.close()
     pool.close()
-    dist.close()
-    if dist.rank != 0:
-        return 0
-    cfg = describe(args.workload)
+    cfg = describe(workload)
     cfg.update({"vertices": int(sum(it[0] for it in items)), "edges": int(sum(len(it[1]) for it in items)),
                 "changes": int(total_changes), "autotuned": tuned["opts"], "autotune_key": tuned["key"],
                 "timed": "sum of CUDA-event intervals of the batch kernels; graph restore + 256 MB flush "
@@ -605,19 +654,19 @@ def run_batching(args, dist: Dist) -> int:
         "value": value,
         "unit": "change-edges/s",
         "n_gpus": dist.world,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": 1e3 * t_max / args.steps,
+        "steps": steps,
+        "warmup": warmup,
+        "ms_per_step": 1e3 * t_max / steps,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "int32",
         "data": "synthetic",
         "config": cfg,
-        "plain": {"value": plain_value, "unit": "change-edges/s", "ms_per_step": 1e3 * pd / args.steps,
-                  "wall_ms_per_step": 1e3 * pw / args.steps},
+        "plain": {"value": plain_value, "unit": "change-edges/s", "ms_per_step": 1e3 * pd / steps,
+                  "wall_ms_per_step": 1e3 * pw / steps},
         "batched_over_plain": value / plain_value,
-        "batched_wall_ms_per_step": 1e3 * bw / args.steps,
+        "batched_wall_ms_per_step": 1e3 * bw / steps,
         "mismatched_distances": mismatches,
         "pooled_repacks": repacks,
         "gpu_launches": launches,
@@ -626,22 +675,55 @@ def run_batching(args, dist: Dist) -> int:
                    "t_update_ms": stats.t_update_ms, "setup_gen_s": t_gen},
         "clocks": clk.summary(),
     }
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def run_serving(args, dist: Dist) -> int:
-    """Serving: resident tenants, Poisson request stream, continuous batching; capacity, then
-    p50/p99 latency and throughput at several offered loads; exactness on sampled tenants."""
+    line = serving_summary(args.workload, dist)
+    dist.close()
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def one_by_one(tenants, streams, dev: int, slack: dict):
+    """The plain single-batch update on the same request streams: every tenant in a graph
+    store of its own, each request's batch applied alone from host memory through the C ABI
+    (dsssp_apply_batch, which waits for the result).  streams = [(requests, timed)], applied
+    in arrival order.  Returns (changes, seconds) of the timed streams and the tenants' final
+    distances."""
+    import dynamicssspv2_gb300 as D
+
+    graphs = []
+    for t in tenants:
+        g = D.Graph(t.n, t.u, t.v, t.w, device=dev, **slack)
+        g.tree_compute(t.src)
+        graphs.append(g)
+    changes, secs = 0, 0.0
+    for reqs, timed in streams:
+        for r in sorted(reqs, key=lambda r: r.arrival):
+            a = np.ascontiguousarray(r.changes, D.CHANGE_DTYPE)
+            t0 = time.perf_counter()
+            graphs[r.tenant].apply_batch(a)
+            dt = time.perf_counter() - t0
+            if timed:
+                changes += len(a)
+                secs += dt
+    dists = [g.tree_read()[1] for g in graphs]
+    for g in graphs:
+        g.close()
+    return changes, secs, dists
+
+
+def make_serve_tenants(workload: str):
+    """The serving workload's tenants: the resident RMAT graph (source = its highest-degree
+    vertex) and the Erdos-Renyi tenants (source 0), seeded."""
     from concurrent.futures import ThreadPoolExecutor
 
     import dynamicssspv2_gb300 as D
-    from dynamicssspv2_gb300.serve import Request, Server, Tenant, random_batch, summarize
-    from oracle import pyoracle as O
+    from dynamicssspv2_gb300.serve import Tenant
 
-    w = WORKLOADS[args.workload]
-    dev = dist.local
-    t0 = time.perf_counter()
+    w = WORKLOADS[workload]
     rng = np.random.default_rng(0)
     ns = np.round(10 ** rng.uniform(w["tnlo"], w["tnhi"], w["tenants"])).astype(np.int64)
 
@@ -654,33 +736,72 @@ def run_serving(args, dist: Dist) -> int:
         ers = list(ex.map(er, range(w["tenants"])))
     n_r = 1 << w["rmat_scale"]
     ru, rv, rw = D.gen_rmat(w["rmat_scale"], w["rmat_m"], 0.57, 0.19, 0.19, w["wlo"], w["whi"], seed=0)
-    tenants = [Tenant("rmat", n_r, ru, rv, rw, src=D.max_degree_vertex(n_r, ru, rv))] + ers
+    return [Tenant("rmat", n_r, ru, rv, rw, src=D.max_degree_vertex(n_r, ru, rv))] + ers
+
+
+def serve_requests(workload: str, tenants, count: int, rate: float, seed: int):
+    """count requests for random tenants: Poisson arrivals at `rate` per second (0 = all at
+    once), batch sizes log-uniform in the workload's range, 50% insertions."""
+    from dynamicssspv2_gb300.serve import Request, random_batch
+
+    w = WORKLOADS[workload]
+    g = np.random.default_rng(seed)
+    sizes = np.round(10 ** g.uniform(w["blo"], w["bhi"], count)).astype(int)
+    who = g.integers(0, len(tenants), count)
+    arr = np.cumsum(g.exponential(1.0 / rate, count)) if rate else np.zeros(count)
+    return [Request(int(t), float(a), random_batch(g, tenants[int(t)], int(sz), wlo=w["wlo"], whi=w["whi"]))
+            for t, a, sz in zip(who, arr, sizes)]
+
+
+class EdgeTracker:
+    """Edge lists of some tenants, kept up to date with every request applied to them (the
+    reference's batch semantics, through the oracle), for exactness checks after serving."""
+
+    def __init__(self, tenants, which):
+        self.tenants = tenants
+        self.lines = {t: (tenants[t].u, tenants[t].v, tenants[t].w) for t in which}
+
+    def track(self, reqs) -> None:
+        from oracle import pyoracle as O
+
+        for r in sorted(reqs, key=lambda r: r.arrival):
+            if r.tenant in self.lines and not r.refused and r.error is None:
+                lines = self.lines[r.tenant]
+                _, kept = O.updated_graph(self.tenants[r.tenant].n, *lines, r.changes, return_kept=True)
+                ins = r.changes[r.changes["op"] == 1]
+                lu = np.concatenate([lines[0], ins["u"]]).astype(np.int32)
+                lv = np.concatenate([lines[1], ins["v"]]).astype(np.int32)
+                lw = np.concatenate([lines[2], ins["w"]]).astype(np.int32)
+                keep = kept[: len(lu)].astype(bool)
+                self.lines[r.tenant] = (lu[keep], lv[keep], lw[keep])
+
+
+def serving_summary(workload: str, dist: Dist, plain_baseline: bool = True) -> dict:
+    """Serving: resident tenants, Poisson request stream, continuous batching; capacity, then
+    p50/p99 latency and throughput at several offered loads; exactness on sampled tenants.
+    With plain_baseline the saturated request stream is also applied one request at a time by
+    the plain update (a graph store per tenant), which gives the served-over-one-by-one ratio
+    on the same stream and checks every tenant's distances against the served ones."""
+    from dynamicssspv2_gb300.serve import Server, summarize
+    from oracle import pyoracle as O
+
+    w = WORKLOADS[workload]
+    dev = dist.local
+    t0 = time.perf_counter()
+    tenants = make_serve_tenants(workload)
     t_gen = time.perf_counter() - t0
 
     def make_requests(count, rate, seed):
-        g = np.random.default_rng(seed)
-        sizes = np.round(10 ** g.uniform(w["blo"], w["bhi"], count)).astype(int)
-        who = g.integers(0, len(tenants), count)
-        arr = np.cumsum(g.exponential(1.0 / rate, count)) if rate else np.zeros(count)
-        return [Request(int(t), float(a), random_batch(g, tenants[int(t)], int(sz), wlo=w["wlo"], whi=w["whi"]))
-                for t, a, sz in zip(who, arr, sizes)]
+        return serve_requests(workload, tenants, count, rate, seed)
 
-    srv = Server(tenants, device=dev, slack_pct=50, slack_min=16)
+    slack = {"slack_pct": 50, "slack_min": 16}
+    srv = Server(tenants, device=dev, **slack)
     # exactness bookkeeping for the smallest ER tenants: their edge lists follow every request
     checked = sorted(range(1, len(tenants)), key=lambda t: tenants[t].n)[: w["checked"]]
-    lines = {t: (tenants[t].u, tenants[t].v, tenants[t].w) for t in checked}
+    tracker = EdgeTracker(tenants, checked)
+    track, lines = tracker.track, tracker.lines
 
-    def track(reqs):
-        for r in sorted(reqs, key=lambda r: r.arrival):
-            if r.tenant in lines and not r.refused:
-                _, kept = O.updated_graph(tenants[r.tenant].n, *lines[r.tenant], r.changes, return_kept=True)
-                ins = r.changes[r.changes["op"] == 1]
-                lu = np.concatenate([lines[r.tenant][0], ins["u"]]).astype(np.int32)
-                lv = np.concatenate([lines[r.tenant][1], ins["v"]]).astype(np.int32)
-                lw = np.concatenate([lines[r.tenant][2], ins["w"]]).astype(np.int32)
-                keep = kept[: len(lu)].astype(bool)
-                lines[r.tenant] = (lu[keep], lv[keep], lw[keep])
-
+    clk = ClockSampler(dev).__enter__()
     warm = make_requests(2 * len(tenants), 0, 1)
     srv.serve(warm, realtime=False)
     track(warm)
@@ -689,6 +810,21 @@ def run_serving(args, dist: Dist) -> int:
     track(sat)
     cap = summarize(sat)
     cap_rate = cap["served"] / cap["span_s"]
+    plain = None
+    if plain_baseline:
+        served_d = [srv.tree(t)[1] for t in range(len(tenants))]
+        ch, secs, obo_d = one_by_one(tenants, [(warm, False), (sat, True)], dev, slack)
+        differ = sum(int((a != b).sum()) for a, b in zip(served_d, obo_d))
+        del served_d, obo_d
+        rate = ch / secs if secs > 0 else 0.0
+        plain = {"value": rate, "unit": "change-edges/s", "requests": len(sat), "changes": int(ch),
+                 "seconds": secs, "served_value": cap["change_edges_per_s"],
+                 "ratio": cap["change_edges_per_s"] / rate if rate > 0 else None,
+                 "distances_differing_from_served": differ,
+                 "how": "the saturated request stream applied one request at a time by the plain update "
+                        "(each tenant in a graph store of its own, dsssp_apply_batch from host memory, host "
+                        "clock per call, summed), after the same warm-up requests; ratio = served capacity "
+                        "over this rate"}
     loads = []
     for i, load in enumerate(w["loads"]):
         reqs = make_requests(w["requests"], load * cap_rate, 10 + i)
@@ -700,6 +836,7 @@ def run_serving(args, dist: Dist) -> int:
         # device certificate of every tenant's tree after this load (untimed)
         st["certificate_violations"] = srv.validate()["violations"]
         loads.append(st)
+    clk.__exit__(None, None, None)
     mism = 0
     for t in checked:
         p, d = srv.tree(t)
@@ -707,10 +844,7 @@ def run_serving(args, dist: Dist) -> int:
         od, op = O.dijkstra(n, O.csr(n, *lines[t]), tenants[t].src)
         mism += int((od != d).sum())
     srv.close()
-    dist.close()
-    if dist.rank != 0:
-        return 0
-    cfg = describe(args.workload)
+    cfg = describe(workload)
     cfg.update({"admitted": len(srv.admitted), "vertices": int(sum(t.n for t in tenants)),
                 "edges": int(sum(len(t.u) for t in tenants)), "setup_gen_s": t_gen,
                 "timed": "host clock from arrival to completion of each request (includes queueing, host batch "
@@ -730,12 +864,13 @@ def run_serving(args, dist: Dist) -> int:
         "data": "synthetic",
         "config": cfg,
         "capacity": cap,
+        "one_by_one": plain,
         "loads": loads,
         "checked_tenants": len(checked),
         "mismatched_distances": mism,
+        "clocks": clk.summary(),
     }
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def main() -> int:
@@ -746,6 +881,8 @@ def main() -> int:
     ap.add_argument("--impl", choices=["dsssp", "reference"], default="dsssp")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="rmat22")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="rmat22: skip the batching and serving workloads that the default line also carries")
     args = ap.parse_args()
     dist = Dist()
     if args.impl == "reference":

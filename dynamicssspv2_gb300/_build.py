@@ -24,7 +24,6 @@ BUILD = ROOT / "_build"
 LIB = PKG / "_lib"
 INCLUDE = ROOT / "include"
 ORACLE = ROOT / "oracle"
-REFERENCE = Path(os.environ.get("DSSSP_REFERENCE", "/root/reference"))
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp"]
@@ -93,10 +92,9 @@ def build_library(verbose: bool = False) -> Path:
 
 
 def build_oracle() -> None:
-    """Compiles the CPU oracle; also the reference's own code where its sources exist."""
-    subprocess.run(["make", "-s", "-C", str(ORACLE), "all"], check=True)
-    if (REFERENCE / "seqSSSPwithDist_undir.cpp").exists():
-        subprocess.run(["make", "-s", "-C", str(ORACLE), "ref", f"REF={REFERENCE}"], check=True)
+    """Compiles the CPU oracle; also the reference's own code where its sources exist (the
+    oracle's Makefile knows where they lie; DSSSP_REFERENCE overrides it)."""
+    subprocess.run(["make", "-s", "-C", str(ORACLE), "all", "ref-if-present"], check=True)
 
 
 def build_all(verbose: bool = False) -> None:

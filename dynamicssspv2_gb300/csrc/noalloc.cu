@@ -152,7 +152,10 @@ extern "C" int dsssp_sssp_noalloc(int32_t n, int64_t nnz, const int64_t* d_row_o
         return fail(DSSSP_E_INVAL, "sssp_noalloc: %lld adjacency entries outside 0..%lld (DSSSP_NOALLOC_MAX_ENTRIES)",
                     (long long)nnz, kMaxE);
     if (src < 0 || src >= n) return fail(DSSSP_E_BAD_VERTEX, "sssp_noalloc: source %d outside 0..%d", src, n - 1);
-    if (!d_row_off || (nnz > 0 && !d_adj) || !d_parent || !d_dist || ((uintptr_t)d_adj & 7))
+    // every array is read or written with its natural alignment: a misaligned one would be a
+    // device fault, so it is refused here, before any launch
+    if (!d_row_off || (nnz > 0 && !d_adj) || !d_parent || !d_dist || ((uintptr_t)d_adj & 7) ||
+        ((uintptr_t)d_row_off & 7) || ((uintptr_t)d_dist & 7) || ((uintptr_t)d_parent & 3))
         return fail(DSSSP_E_INVAL, "sssp_noalloc: NULL or misaligned device pointer");
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);

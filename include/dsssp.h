@@ -263,9 +263,14 @@ void dsssp_free(void* p);
  *              undirected edge appears in both rows
  *   d_parent   n int32 outputs (-1 = unreachable, src is its own parent)
  *   d_dist     n int64 outputs (DSSSP_UNREACHABLE = -1 for unreachable vertices)
- * All pointers are device addresses on the current device; stream is a cudaStream_t (NULL =
+ * All pointers are device addresses on the current device, each aligned to its element size
+ * (d_row_off, d_adj and d_dist to 8 bytes, d_parent to 4); stream is a cudaStream_t (NULL =
  * legacy default stream).  n <= DSSSP_NOALLOC_MAX_VERTICES and nnz <=
- * DSSSP_NOALLOC_MAX_ENTRIES, else DSSSP_E_INVAL.  Waits for the result on stream.
+ * DSSSP_NOALLOC_MAX_ENTRIES, else DSSSP_E_INVAL; so is a NULL or misaligned pointer (refused
+ * before anything is launched) and a malformed CSR (offsets not monotone from 0 to nnz, a
+ * column outside 0..n-1 or a negative weight; found on the device, outputs then undefined).
+ * The call is blocking: it synchronizes stream and copies the status word to the host before
+ * it returns, so the calling thread waits for the whole computation.
  * It calls no cudaMalloc, cudaFree or other allocating routine.  The first call on a device
  * looks up the work space's device address (cudaGetSymbolAddress) and the update kernel's
  * occupancy; make that first call before any stream capture.  All calls on a device share

@@ -17,7 +17,7 @@
  * plus a shortest-path-tree validator.
  *
  * Pinning: 2 and 3 are checked against the reference itself, compiled here from its own
- * sources (oracle/build_ref.sh -> oracle/_ref/), through the golden fixtures in
+ * sources (`make -C oracle ref` -> oracle/_ref/), through the golden fixtures in
  * tests/golden/ and the test tests/test_oracle.py.
  */
 #ifndef DSSSP_ORACLE_H

@@ -1,7 +1,7 @@
 /*
  * ref_harness.cpp -- runs the reference's own update path on the CPU (test infrastructure).
  *
- * Compiled by oracle/build_ref.sh against the reference sources where they lie
+ * Compiled by `make -C oracle ref` against the reference sources where they lie
  * (all_structure_undir.cuh, gpuFunctions_undir.cuh) with the host stand-ins of
  * oracle/ref_shim/ in place of the CUDA headers.  Every kernel launch of
  * SSSPmainForUndirected.cu:196-281 is replayed as a loop over (block, thread) in index order,

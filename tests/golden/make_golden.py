@@ -14,11 +14,12 @@ repeated records.  The updated-graph file given to op_ssspSeq is built here in p
 Python from the batch semantics (insertions appended, then every line matching a deletion's
 endpoint pair and weight removed), independently of oracle/oracle.c.
 
-usage: python tests/golden/make_golden.py
+usage: DSSSP_REFERENCE=<reference source dir> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
 import json
+import os
 import subprocess
 import sys
 import tempfile
@@ -28,11 +29,12 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
-REF = Path("/root/reference")
+REF = Path(os.environ.get("DSSSP_REFERENCE", ""))
 REFBIN = ROOT / "oracle" / "_ref"
 
 
 def build_ref() -> None:
+    """oracle/_ref/ from the reference's sources in DSSSP_REFERENCE."""
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "all", "ref", f"REF={REF}"], check=True)
 
 
@@ -171,8 +173,8 @@ def make_case(tmp: Path, name: str, n: int, edges, changes, sssp_rows=None):
 
 
 def main() -> int:
-    if not (REF / "seqSSSPwithDist_undir.cpp").exists():
-        print("reference sources not present; nothing to do", file=sys.stderr)
+    if not os.environ.get("DSSSP_REFERENCE") or not (REF / "seqSSSPwithDist_undir.cpp").exists():
+        print("set DSSSP_REFERENCE to the reference's source directory", file=sys.stderr)
         return 1
     build_ref()
     cases = []

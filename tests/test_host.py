@@ -368,3 +368,22 @@ def test_generators_refuse_impossible_requests():
     with pytest.raises(D.DsssspError):
         D.gen_changes(20, u, v, w, 500, 0)   # only 130 new pairs
     assert len(D.gen_changes(20, u, v, w, 0, 0)) == 0
+
+
+def test_noalloc_refuses_bad_pointers_before_any_launch():
+    """dsssp_sssp_noalloc checks its pointers on the host: NULL or misaligned (d_row_off,
+    d_adj, d_dist to 8 bytes, d_parent to 4) gives DSSSP_E_INVAL before any CUDA call, so
+    these never reach a device (none is needed here)."""
+    good8, good4 = 1 << 20, 1 << 20
+    cases = [
+        (0, good8, good4, good8),            # NULL row offsets
+        (good8 + 4, good8, good4, good8),    # row offsets on 4 bytes
+        (good8, good8 + 4, good4, good8),    # adjacency on 4 bytes
+        (good8, good8, good4 + 2, good8),    # parents on 2 bytes
+        (good8, good8, good4, good8 + 4),    # distances on 4 bytes
+        (good8, good8, 0, good8),            # NULL parents
+    ]
+    for off, adj, par, dist in cases:
+        with pytest.raises(D.DsssspError) as e:
+            D.sssp_noalloc(100, 10, off, adj, 0, par, dist)
+        assert e.value.code == D.E_INVAL
