@@ -57,7 +57,7 @@ class Opts(C.Structure):
         ("spare_pct", C.c_int32),
         ("delta", C.c_int32),
         ("launch_graph", C.c_int32),
-        ("reserved1", C.c_int32),
+        ("recover", C.c_int32),
     ]
 
 
@@ -74,7 +74,8 @@ class Stats(C.Structure):
         for name in ("t_step1_ms", "t_inval_ms", "t_relax_ms", "t_update_ms", "t_total_ms", "bytes_alg",
                      "bytes_alg_update")
     ] + [("advances", C.c_int64), ("tombstoned", C.c_int64), ("graph_launch", C.c_int64),
-         ("bytes_engine_update", C.c_double), ("t_delete_ms", C.c_double), ("t_append_ms", C.c_double)]
+         ("bytes_engine_update", C.c_double), ("t_delete_ms", C.c_double), ("t_append_ms", C.c_double),
+         ("recovered_from", C.c_int64), ("t_recompute_ms", C.c_double)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -104,6 +105,8 @@ _sig("dsssp_tree_load", C.c_int, _P, _i32p, _i64p)
 _sig("dsssp_tree_compute", C.c_int, _P, C.c_int32, C.POINTER(Stats))
 _sig("dsssp_tree_compute_multi", C.c_int, _P, _i32p, C.c_int32, C.POINTER(Stats))
 _sig("dsssp_forest_load", C.c_int, _P, _i32p, _i64p)
+_sig("dsssp_tree_add_sources", C.c_int, _P, _i32p, C.c_int32, C.POINTER(Stats))
+_sig("dsssp_graph_clear_range", C.c_int, _P, C.c_int32, C.c_int32)
 _sig("dsssp_tree_read", C.c_int, _P, _P, _P)
 _sig("dsssp_tree_read_changed", C.c_int, _P, _P, _P, _P, C.c_int64, C.POINTER(C.c_int64))
 _sig("dsssp_tree_validate", C.c_int, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32))
@@ -119,6 +122,7 @@ class ServerOpts(C.Structure):
         ("record", C.c_int32),
         ("compact_dead_frac", C.c_double),
         ("compact_spare_frac", C.c_double),
+        ("reserve_vertices", C.c_int64),
     ]
 
 
@@ -137,10 +141,18 @@ class RequestInfo(C.Structure):
 
 
 REFUSED = 1
+W_RECOMPUTED = 2  # a batch recovered by recomputing the trees (a success code)
+TENANT_WAITING, TENANT_ADMITTED, TENANT_REMOVED = 0, 1, 2
 _PP = C.POINTER(C.c_void_p)
 _sig("dsssp_tree_read_range", C.c_int, _P, C.c_int32, C.c_int32, _P, _P)
 _sig("dsssp_pool_create", C.c_int, C.c_int32, _P, _P, _PP, _PP, _PP, C.POINTER(Opts), C.POINTER(_P))
 _sig("dsssp_pool_destroy", None, _P)
+_sig("dsssp_pool_create_reserved", C.c_int, C.c_int32, _P, _P, _PP, _PP, _PP, C.c_int64, C.POINTER(Opts),
+     C.POINTER(_P))
+_sig("dsssp_pool_add_graph", C.c_int, _P, C.c_int32, C.c_int64, _P, _P, _P, C.c_int32, C.POINTER(C.c_int32))
+_sig("dsssp_pool_remove_graph", C.c_int, _P, C.c_int32)
+_sig("dsssp_pool_graph_range", C.c_int, _P, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_int32))
+_sig("dsssp_pool_capacity", C.c_int, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64))
 _sig("dsssp_pool_graph", _P, _P)
 _sig("dsssp_pool_offsets", C.c_int, _P, _P)
 _sig("dsssp_pool_tree_compute", C.c_int, _P, _P, C.POINTER(Stats))
@@ -154,6 +166,11 @@ _sig("dsssp_server_create", C.c_int, C.c_int32, _P, _P, _PP, _PP, _PP, _P, C.POI
      C.POINTER(_P))
 _sig("dsssp_server_destroy", None, _P)
 _sig("dsssp_server_slot", C.c_int, _P, C.c_int32)
+_sig("dsssp_server_tenant_state", C.c_int, _P, C.c_int32)
+_sig("dsssp_server_add_tenant", C.c_int, _P, C.c_int32, C.c_int64, _P, _P, _P, C.c_int32, C.POINTER(C.c_int32))
+_sig("dsssp_server_remove_tenant", C.c_int, _P, C.c_int32)
+_sig("dsssp_server_recovered_epochs", C.c_int, _P, C.POINTER(C.c_int64))
+_sig("dsssp_server_debug_set", C.c_int, _P, C.c_int32, C.c_int64)
 _sig("dsssp_submit", C.c_int, _P, C.c_int32, _P, C.c_int64, C.POINTER(C.c_int64))
 _sig("dsssp_submit_many", C.c_int, _P, C.c_int32, _P, _PP, _P, _P)
 _sig("dsssp_poll", C.c_int, _P, C.POINTER(RequestInfo), C.c_int32, C.c_int32, C.POINTER(C.c_int32))
@@ -221,13 +238,18 @@ EXPORTED = [
     "dsssp_estimate_footprint", "dsssp_default_server_opts", "dsssp_server_create", "dsssp_server_destroy",
     "dsssp_server_slot", "dsssp_submit", "dsssp_submit_many", "dsssp_poll", "dsssp_server_drain",
     "dsssp_server_result", "dsssp_server_tree_read", "dsssp_server_info", "dsssp_server_pool",
-    "dsssp_server_set_record", "dsssp_server_validate",
+    "dsssp_server_set_record", "dsssp_server_validate", "dsssp_tree_add_sources", "dsssp_graph_clear_range",
+    "dsssp_pool_create_reserved", "dsssp_pool_add_graph", "dsssp_pool_remove_graph", "dsssp_pool_graph_range",
+    "dsssp_pool_capacity", "dsssp_server_tenant_state", "dsssp_server_add_tenant", "dsssp_server_remove_tenant",
+    "dsssp_server_recovered_epochs", "dsssp_server_debug_set",
 ]
 
 
-def _check(rc: int, what: str) -> None:
-    if rc != OK:
+def _check(rc: int, what: str) -> int:
+    """Raises on a negative status; returns 0 or a positive success code (W_RECOMPUTED)."""
+    if rc < 0:
         raise DsssspError(rc, what)
+    return rc
 
 
 def _take_i32(p: C.c_void_p, n: int) -> np.ndarray:
@@ -331,6 +353,17 @@ class Graph:
         st = Stats()
         _check(_lib.dsssp_tree_compute_multi(self._h, srcs, len(srcs), C.byref(st)), "tree_compute_multi")
         return st
+
+    def tree_add_sources(self, srcs) -> Stats:
+        """New roots joined to the resident forest (relaxation from them; nothing recomputed)."""
+        srcs = np.ascontiguousarray(srcs, np.int32)
+        st = Stats()
+        _check(_lib.dsssp_tree_add_sources(self._h, srcs, len(srcs), C.byref(st)), "tree_add_sources")
+        return st
+
+    def clear_range(self, first: int, count: int) -> None:
+        """Removes every edge of ids [first, first + count) (closed under adjacency)."""
+        _check(_lib.dsssp_graph_clear_range(self._h, int(first), int(count)), "clear_range")
 
     def forest_load(self, parent, dist) -> None:
         parent = np.ascontiguousarray(parent, np.int32)

@@ -162,7 +162,9 @@ int main(int argc, char** argv) {
 
     dsssp_stats st;
     rc = dsssp_apply_batch(g, ch, k, nullptr, &st);
-    if (rc) return die("applying the change batch", rc);
+    if (rc < 0) return die("applying the change batch", rc);
+    if (rc == DSSSP_W_RECOMPUTED)
+        fprintf(stderr, "dsssp_main: note: %s (the updated tree is exact)\n", dsssp_last_error());
     printf("**Time taken for SSSP update STEP1: %g milliseconds**\n", st.t_step1_ms);
     printf("**Time taken for updateNeighbors_del: %g milliseconds**\n", st.t_inval_ms);
     printf("**Time taken for updateNeighbors: %g milliseconds**\n", st.t_relax_ms);

@@ -442,6 +442,43 @@ __global__ void k_validate_cycles(const unsigned* jm, int n, unsigned long long*
     }
 }
 
+// Rows [first, first + count): live entries whose column lies outside the range (out[0]).
+__global__ void k_range_crossing(const RowDesc* rows, const int2* adj, int first, int count,
+                                 unsigned long long* out) {
+    const unsigned lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    unsigned long long cross = 0;
+    for (long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < count; i += warps) {
+        const RowDesc rd = rows[first + i];
+        for (int j = (int)lane; j < rd.deg; j += 32) {
+            const int2 e = adj[rd.start + j];
+            if (e.y >= 0 && (e.x < first || (long long)e.x >= (long long)first + count)) cross++;
+        }
+    }
+    if (cross) atomicAdd(&out[0], cross);
+}
+
+// Tombstones every live entry of rows [first, first + count) -- both directions of each edge
+// lie in the range -- and makes the range's vertices unreachable.  out[1] counts the entries.
+__global__ void k_range_clear(unsigned long long* state, const RowDesc* rows, int2* adj, int first, int count,
+                              unsigned long long* out) {
+    const unsigned lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    unsigned long long dead = 0;
+    for (long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < count; i += warps) {
+        const RowDesc rd = rows[first + i];
+        for (int j = (int)lane; j < rd.deg; j += 32) {
+            int2* e = &adj[rd.start + j];
+            if (e->y >= 0) {
+                e->y = -1;
+                dead++;
+            }
+        }
+        if (lane == 0) state[first + i] = kInfState;
+    }
+    if (dead) atomicAdd(&out[1], dead);
+}
+
 __global__ void k_state_reset(unsigned long long* state, int n) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v < n) state[v] = kInfState;
@@ -572,6 +609,10 @@ struct dsssp_graph {
     bool s_has_tree = false;
     int* d_srcs = nullptr;  // sources of the last from-scratch computation
     int srcs_cap = 0;
+    // the roots of the resident forest (vertices that are their own parent), kept on the host
+    // so that a failed batch can be recovered by recomputing the trees from them
+    std::vector<int> roots;
+    std::vector<int> s_roots;  // with the snapshot
 };
 
 namespace dsssp {
@@ -1194,6 +1235,51 @@ int enqueue_batch(dsssp_graph* g, const int4* d_chg, long long k, cudaStream_t s
     return DSSSP_OK;
 }
 
+// Statuses of the update kernel that leave the batch's adjacency edits in place and the tree
+// unfinished: a timed-out grid barrier, the round cap, an internal list capacity, a parent
+// cycle found by pointer jumping.  (Refused records, found before anything is modified, and a
+// distance overflow, which a recomputation would meet again, are not among them.)
+bool recoverable(int dev_status) {
+    return dev_status == DSSSP_E_TIMEOUT || dev_status == DSSSP_E_NO_CONVERGENCE || dev_status == -4 ||
+           dev_status == DSSSP_E_BAD_TREE;
+}
+
+// After a recoverable failure the graph holds the whole batch (every deletion and insertion
+// is in the adjacency) but the tree is unfinished.  With opts.recover the trees are computed
+// again from the roots on the updated graph, which gives exactly the result of a successful
+// batch: DSSSP_W_RECOMPUTED, and st->recovered_from names the failure.  If that computation
+// fails too, the tree is marked unusable (later batches are refused until a tree is loaded or
+// computed) and the original error is returned.  Without opts.recover the error is returned
+// and the tree is left as the kernel left it.
+int recover_after_failure(dsssp_graph* g, int rc, dsssp_stats* st) {
+    if (!g->o.recover || g->roots.empty()) {
+        if (g->o.recover) g->has_tree = false;
+        return rc;
+    }
+    char why[200];
+    snprintf(why, sizeof why, "%s", dsssp_last_error());
+    const std::vector<int> roots = g->roots;
+    dsssp_stats rs;
+    // the recomputation runs with the default round cap (2n + 16): after round r of a
+    // computation from the sources every vertex with a shortest path of at most r edges is
+    // final, so it needs fewer than n rounds
+    const long long cap = g->o.max_rounds;
+    g->o.max_rounds = 0;
+    const int rr = dsssp_tree_compute_multi(g, roots.data(), (int32_t)roots.size(), &rs);
+    g->o.max_rounds = cap;
+    if (rr != DSSSP_OK) {
+        g->has_tree = false;
+        return fail(rc, "%s; recomputing the trees from %zu roots failed too (%d): the tree must be loaded or "
+                        "computed again", why, roots.size(), rr);
+    }
+    if (st) {
+        st->recovered_from = rc;
+        st->t_recompute_ms = rs.t_total_ms;
+    }
+    return fail(DSSSP_W_RECOMPUTED, "%s; the batch is applied and the trees were recomputed from %zu roots", why,
+                roots.size());
+}
+
 int finish_batch(dsssp_graph* g, dsssp_stats* st) {
     if (!g->pending) {
         if (st) memset(st, 0, sizeof(*st));
@@ -1233,16 +1319,21 @@ int finish_batch(dsssp_graph* g, dsssp_stats* st) {
     g->delta_lo = g->pend_rb0;
     g->delta_hi = g->h_ctl->round_base;
     g->delta_epoch = g->epoch;
-    if (g->h_ctl->status != 0) reset_tags(g, s);
-    if (g->h_ctl->stat[ST_DIST_OVF] > 0 && g->h_ctl->status == 0) return status_code(DSSSP_E_OVERFLOW);
-    if (g->h_ctl->status == DSSSP_E_TIMEOUT) {
+    const int dev_status = g->h_ctl->status;
+    if (dev_status != 0) reset_tags(g, s);
+    if (g->h_ctl->stat[ST_DIST_OVF] > 0 && dev_status == 0) return status_code(DSSSP_E_OVERFLOW);
+    int rc;
+    if (dev_status == DSSSP_E_TIMEOUT) {
         const unsigned* d = g->h_ctl->diag;
-        return fail(DSSSP_E_TIMEOUT,
-                    "grid barrier #%u timed out with %u of %d CTAs arrived; %u CTAs timed out; "
-                    "CTA barrier counts at exit: min %u max %u",
-                    d[0], d[1], g->coop_grid, d[2], 0xFFFFFFFFu - d[4], d[3]);
+        rc = fail(DSSSP_E_TIMEOUT,
+                  "grid barrier #%u timed out with %u of %d CTAs arrived; %u CTAs timed out; "
+                  "CTA barrier counts at exit: min %u max %u",
+                  d[0], d[1], g->coop_grid, d[2], 0xFFFFFFFFu - d[4], d[3]);
+    } else {
+        rc = status_code(dev_status);
     }
-    return status_code(g->h_ctl->status);
+    if (rc == DSSSP_OK || !recoverable(dev_status)) return rc;
+    return recover_after_failure(g, rc, st);
 }
 
 }  // namespace
@@ -1270,7 +1361,7 @@ void dsssp_default_opts(dsssp_opts* o) {
     o->spare_pct = 12;
     o->delta = -1;
     o->launch_graph = 1;
-    o->reserved1 = 0;
+    o->recover = 1;
 }
 
 const char* dsssp_strerror(int code) {
@@ -1288,6 +1379,7 @@ const char* dsssp_strerror(int code) {
         case DSSSP_E_BAD_WEIGHT: return "negative edge weight";
         case DSSSP_E_NO_DEVICE: return "no CUDA device";
         case DSSSP_E_COOP: return "persistent kernel cannot be co-resident";
+        case DSSSP_W_RECOMPUTED: return "batch applied; tree recomputed after a failed update";
         default: return "unknown error";
     }
 }
@@ -1333,7 +1425,8 @@ static int check_opts(const dsssp_opts& o) {
     if (o.slack_pct < 0 || o.slack_min < 0 || o.small_deg < 4 || o.small_deg > 64 || o.small_deg % 4 ||
         o.large_deg < o.small_deg || o.chunk < 32 ||
         o.bfs_levels < 0 || o.block < 32 || o.block > 256 || o.block % 32 || o.ctas_per_sm < 0 || o.max_rounds < 0 ||
-        o.spare_pct < 0 || o.spare_pct > 400 || o.delta < -1 || o.timing < 0 || o.timing > 2)
+        o.spare_pct < 0 || o.spare_pct > 400 || o.delta < -1 || o.timing < 0 || o.timing > 2 || o.recover < 0 ||
+        o.recover > 1)
         return fail(DSSSP_E_INVAL, "invalid dsssp_opts");
     return DSSSP_OK;
 }
@@ -1525,6 +1618,9 @@ static int tree_load_impl(dsssp_graph* g, const int32_t* parent, const int64_t* 
     g->src = (int)g->h_ctl->stat[1];
     g->has_tree = true;
     g->delta_ok = false;
+    g->roots.clear();
+    for (int v = 0; v < g->n; v++)
+        if (parent[v] == v) g->roots.push_back(v);
     return DSSSP_OK;
 }
 
@@ -1536,7 +1632,21 @@ int dsssp_forest_load(dsssp_graph* g, const int32_t* parent, const int64_t* dist
     return tree_load_impl(g, parent, dist, true);
 }
 
+static int compute_from_sources(dsssp_graph* g, const int32_t* srcs, int32_t k, dsssp_stats* st, bool reset);
+
 int dsssp_tree_compute_multi(dsssp_graph* g, const int32_t* srcs, int32_t k, dsssp_stats* st) {
+    return compute_from_sources(g, srcs, k, st, true);
+}
+
+int dsssp_tree_add_sources(dsssp_graph* g, const int32_t* srcs, int32_t k, dsssp_stats* st) {
+    return compute_from_sources(g, srcs, k, st, false);
+}
+
+// reset: every vertex starts unreachable (a computation from scratch); otherwise the current
+// distances stay as upper bounds (each is the length of a real path from a root) and the new
+// sources join the roots: relaxation from them lowers what they improve, which converges to the
+// exact distances from the enlarged set of roots.
+static int compute_from_sources(dsssp_graph* g, const int32_t* srcs, int32_t k, dsssp_stats* st, bool reset) {
     if (!g || k < 1 || !srcs) return fail(DSSSP_E_INVAL, "tree_compute: NULL graph or no source");
     int rc = set_device(g);
     if (rc) return rc;
@@ -1562,9 +1672,12 @@ int dsssp_tree_compute_multi(dsssp_graph* g, const int32_t* srcs, int32_t k, dss
     CK(cudaMemcpyAsync(g->d_srcs, uniq.data(), sizeof(int) * (size_t)nsrc, cudaMemcpyHostToDevice, s), "sources");
     const bool ev = g->o.timing != 0;
     if (ev) CK(cudaEventRecord(g->ev[0], s), "event");
-    k_state_reset<<<blocks_for(g->n), kThreads, 0, s>>>(g->dg.state, g->n);
+    if (reset) {
+        k_state_reset<<<blocks_for(g->n), kThreads, 0, s>>>(g->dg.state, g->n);
+        count_launch(1);
+    }
     k_set_sources<<<blocks_for(nsrc), kThreads, 0, s>>>(g->dg.state, g->n, g->d_srcs, nsrc, g->dg.ctl);
-    count_launch(2);
+    count_launch(1);
     if (ev) CK(cudaEventRecord(g->ev[1], s), "event");
     if (effective_delta(g) > 0) {
         rc = ensure_far(g);
@@ -1576,7 +1689,17 @@ int dsssp_tree_compute_multi(dsssp_graph* g, const int32_t* srcs, int32_t k, dss
     if (ev) CK(cudaEventRecord(g->ev[2], s), "event");
     CK(cudaMemcpyAsync(g->h_ctl, g->dg.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s), "status read");
     CK(cudaStreamSynchronize(s), "tree compute");
-    g->src = uniq[0];
+    if (reset || !g->has_tree) {
+        g->src = uniq[0];
+        g->roots = uniq;
+    } else {
+        std::vector<int> all(g->roots);
+        all.insert(all.end(), uniq.begin(), uniq.end());
+        std::sort(all.begin(), all.end());
+        all.erase(std::unique(all.begin(), all.end()), all.end());
+        g->roots.swap(all);
+        g->src = g->roots[0];
+    }
     g->has_tree = g->h_ctl->status == 0;
     g->last_rounds = (long long)g->h_ctl->stat[ST_ROUNDS];
     g->delta_ok = false;
@@ -1823,6 +1946,7 @@ int dsssp_graph_snapshot(dsssp_graph* g) {
     g->s_dead = g->dead;
     g->s_src = g->src;
     g->s_has_tree = g->has_tree;
+    g->s_roots = g->roots;
     g->has_snap = true;
     return DSSSP_OK;
 }
@@ -1857,6 +1981,7 @@ int dsssp_graph_restore(dsssp_graph* g, void* stream) {
     g->spare_top = (long long)g->s_spare[0];
     g->src = g->s_src;
     g->has_tree = g->s_has_tree;
+    g->roots = g->s_roots;
     g->delta_ok = false;  // the tags name batches after the snapshot
     return DSSSP_OK;
 }
@@ -1868,6 +1993,48 @@ int dsssp_graph_health(const dsssp_graph* g, int64_t* live_entries, int64_t* dea
     if (dead_entries) *dead_entries = g->dead;
     if (spare_used) *spare_used = g->spare_top - g->spare_lo;
     if (spare_total) *spare_total = g->cap_total - g->spare_lo;
+    return DSSSP_OK;
+}
+
+int dsssp_graph_clear_range(dsssp_graph* g, int32_t first, int32_t count) {
+    if (!g || first < 0 || count < 0 || (long long)first + count > g->n)
+        return fail(DSSSP_E_INVAL, "clear_range: bad arguments");
+    int rc = set_device(g);
+    if (rc) return rc;
+    if (g->pending) return fail(DSSSP_E_INVAL, "clear_range: a batch is still pending");
+    if (count == 0) return DSSSP_OK;
+    cudaStream_t s = g->stream;
+    unsigned long long* d_out = nullptr;
+    rc = dalloc(&d_out, 2, "range counters");
+    if (rc) return rc;
+    unsigned long long out[2] = {0, 0};
+    const unsigned grid = (unsigned)(g->num_sms * 8);
+    cudaError_t e = cudaMemsetAsync(d_out, 0, sizeof(out), s);
+    if (e == cudaSuccess) {
+        k_range_crossing<<<grid, kThreads, 0, s>>>(g->dg.rows, g->dg.adj, first, count, d_out);
+        count_launch(1);
+        e = cudaMemcpyAsync(out, d_out, sizeof(out), cudaMemcpyDeviceToHost, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess && out[0] == 0) {
+        k_range_clear<<<grid, kThreads, 0, s>>>(g->dg.state, g->dg.rows, g->dg.adj, first, count, d_out);
+        count_launch(1);
+        e = cudaMemcpyAsync(out, d_out, sizeof(out), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    }
+    dfree(d_out);
+    if (e != cudaSuccess) return cuda_fail(e, "clear_range");
+    if (out[0] != 0)
+        return fail(DSSSP_E_INVAL, "clear_range: %llu live entries join [%d, %lld) to the rest of the graph", out[0],
+                    first, (long long)first + count);
+    g->entries -= (long long)out[1];
+    g->dead += (long long)out[1];
+    std::vector<int> keep;
+    for (int r : g->roots)
+        if (r < first || (long long)r >= (long long)first + count) keep.push_back(r);
+    g->roots.swap(keep);
+    if (g->src >= first && (long long)g->src < (long long)first + count) g->src = g->roots.empty() ? -1 : g->roots[0];
+    g->delta_ok = false;
     return DSSSP_OK;
 }
 

@@ -1053,9 +1053,11 @@ __device__ void update_body(UpdParams& p) {
     const unsigned stall_us = __ldcg(&ctl->stall_us);
     if (stall_us && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
         // test hook (failure detection): arrive late at the first barrier so that the others
-        // run out of polls; a bounded wait (at most 2^21 sleeps of 1 us)
+        // run out of polls; a bounded wait (at most 2^21 sleeps of 1 us).  One launch only: the
+        // hook clears itself, so a recomputation after the failed batch runs normally.
         const unsigned long long t0 = globaltimer();
         for (unsigned i = 0; i < (1u << 21) && globaltimer() - t0 < 1000ull * stall_us; i++) __nanosleep(1000);
+        ctl->stall_us = 0;
     }
     const unsigned lane = lane_id();
     const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;

@@ -51,29 +51,61 @@ class _PoolGraph(Graph):
 
 
 class GraphPool:
-    def __init__(self, graphs, opts: Opts | None = None, **kw):
-        """graphs: sequence of (n_i, u_i, v_i, w_i) edge lists with local vertex ids."""
+    def __init__(self, graphs, opts: Opts | None = None, reserve_vertices: int = 0, **kw):
+        """graphs: sequence of (n_i, u_i, v_i, w_i) edge lists with local vertex ids;
+        reserve_vertices: spare ids for graphs added later (add_graph)."""
         n = np.asarray([int(g[0]) for g in graphs], np.int32)
         us = [np.ascontiguousarray(g[1], np.int32) for g in graphs]
         vs = [np.ascontiguousarray(g[2], np.int32) for g in graphs]
         ws = [np.ascontiguousarray(g[3], np.int32) for g in graphs]
         m = np.asarray([len(a) for a in us], np.int64)
-        if len(n) == 0:
-            raise ValueError("a pool needs at least one graph")
+        if len(n) == 0 and reserve_vertices <= 0:
+            raise ValueError("a pool needs at least one graph or a vertex reserve")
         o = opts if opts is not None else default_opts(**kw)
         h = _P()
-        _check(_lib.dsssp_pool_create(len(n), n.ctypes.data, m.ctypes.data, _ptrs(us), _ptrs(vs), _ptrs(ws),
-                                      C.byref(o), C.byref(h)), "pool_create")
+        _check(_lib.dsssp_pool_create_reserved(len(n), n.ctypes.data, m.ctypes.data, _ptrs(us), _ptrs(vs),
+                                               _ptrs(ws), int(reserve_vertices), C.byref(o), C.byref(h)),
+               "pool_create")
         self._h = h
         self.sizes = n.astype(np.int64)
         self.offsets = np.empty(len(n) + 1, np.int64)
         _check(_lib.dsssp_pool_offsets(h, self.offsets.ctypes.data), "pool_offsets")
-        self.n = int(self.offsets[-1])
+        cap = C.c_int64()
+        _check(_lib.dsssp_pool_capacity(h, C.byref(cap), None, None), "pool_capacity")
+        self.n = int(cap.value)
         self.edges = [int(x) for x in m]
         self.graph = _PoolGraph(_lib.dsssp_pool_graph(h), self.n)
 
     def __len__(self) -> int:
         return len(self.sizes)
+
+    def add_graph(self, n: int, u, v, w, src: int = 0) -> int:
+        """A graph in free reserved ids: its tree is built on the device from its edges (the
+        other graphs are untouched).  Returns its index."""
+        u = np.ascontiguousarray(u, np.int32)
+        v = np.ascontiguousarray(v, np.int32)
+        w = np.ascontiguousarray(w, np.int32)
+        gi = C.c_int32()
+        _check(_lib.dsssp_pool_add_graph(self._h, int(n), len(u), u.ctypes.data if len(u) else None,
+                                         v.ctypes.data if len(v) else None, w.ctypes.data if len(w) else None,
+                                         int(src), C.byref(gi)), "pool_add_graph")
+        self.sizes = np.append(self.sizes, int(n))
+        self.edges.append(len(u))
+        return gi.value
+
+    def remove_graph(self, graph: int) -> None:
+        _check(_lib.dsssp_pool_remove_graph(self._h, int(graph)), "pool_remove_graph")
+        self.sizes[graph] = 0
+
+    def graph_range(self, graph: int) -> tuple[int, int]:
+        first, n = C.c_int64(), C.c_int32()
+        _check(_lib.dsssp_pool_graph_range(self._h, int(graph), C.byref(first), C.byref(n)), "pool_graph_range")
+        return first.value, n.value
+
+    def capacity(self) -> dict:
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        _check(_lib.dsssp_pool_capacity(self._h, C.byref(a), C.byref(b), C.byref(c)), "pool_capacity")
+        return {"vertices": a.value, "free": b.value, "largest_free": c.value}
 
     def close(self) -> None:
         if getattr(self, "_h", None) and self._h.value:
@@ -112,6 +144,9 @@ class GraphPool:
         """Trees with local ids: a list of (parent, dist), or one tree for graph `which`."""
         out = []
         for i in (range(len(self)) if which is None else [which]):
+            if self.sizes[i] == 0:  # removed
+                out.append((np.zeros(0, np.int32), np.zeros(0, np.int64)))
+                continue
             p = np.empty(int(self.sizes[i]), np.int32)
             d = np.empty(int(self.sizes[i]), np.int64)
             _check(_lib.dsssp_pool_tree_read(self._h, int(i), p.ctypes.data, d.ctypes.data), "pool_tree_read")

@@ -15,6 +15,13 @@ admitted are refused, and a request whose batch names a vertex outside its tenan
 inserts a negative weight fails on arrival (`error` says why) without touching the epoch it
 would have joined.
 
+Tenants that do not fit the memory budget wait, with their vertex ids reserved, and are
+admitted when a removal frees memory; tenants can be added (`add_tenant`) and removed
+(`remove_tenant`) while the server runs.  A new tenant's tree is built on the device from its
+edges without touching the others.  An epoch whose update kernel fails (a device wait that
+times out, for instance) is recovered by recomputing the trees on the device: its requests are
+served with `recomputed` set and every tenant's tree stays exact.
+
 Storage upkeep runs between epochs, only while no request waits: when the store's tombstoned
 entries exceed `compact_dead_frac` of its live entries, or the spare region that overflowing
 rows move into is more than `compact_spare_frac` used, the store is compacted (tombstones
@@ -30,7 +37,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import CHANGE_DTYPE, REFUSED, RequestInfo, ServerOpts, _check, _lib, default_opts
+from . import (CHANGE_DTYPE, REFUSED, TENANT_ADMITTED, W_RECOMPUTED, RequestInfo, ServerOpts, _check, _lib,
+               default_opts)
 from .pool import _ptrs
 
 
@@ -60,6 +68,7 @@ class Request:
     start: float = float("nan")
     done: float = float("nan")
     refused: bool = False
+    recomputed: bool = False  # served by an epoch recovered by recomputing the trees
     error: str | None = None
     result: tuple | None = field(default=None, repr=False)
 
@@ -70,9 +79,11 @@ class Request:
 
 class Server:
     def __init__(self, tenants, memory_budget: int | None = None, max_epoch_requests: int | None = None,
-                 compact_dead_frac: float | None = 0.25, compact_spare_frac: float = 0.75, **opts):
+                 compact_dead_frac: float | None = 0.25, compact_spare_frac: float = 0.75,
+                 reserve_vertices: int = 0, **opts):
         self.tenants = list(tenants)
         o = default_opts(**opts)
+        self._slack = (o.slack_pct, o.slack_min)
         self.footprints = [estimate_footprint(t.n, len(t.u), o.slack_pct, o.slack_min) for t in self.tenants]
         so = ServerOpts()
         _lib.dsssp_default_server_opts(C.byref(so))
@@ -80,6 +91,7 @@ class Server:
         so.max_epoch_requests = int(max_epoch_requests or 0)
         so.compact_dead_frac = -1.0 if compact_dead_frac is None else float(compact_dead_frac)
         so.compact_spare_frac = float(compact_spare_frac)
+        so.reserve_vertices = int(reserve_vertices)
         n = np.asarray([t.n for t in self.tenants], np.int32)
         us = [np.ascontiguousarray(t.u, np.int32) for t in self.tenants]
         vs = [np.ascontiguousarray(t.v, np.int32) for t in self.tenants]
@@ -90,13 +102,58 @@ class Server:
         _check(_lib.dsssp_server_create(len(n), n.ctypes.data, m.ctypes.data, _ptrs(us), _ptrs(vs), _ptrs(ws),
                                         src.ctypes.data, C.byref(so), C.byref(o), C.byref(h)), "server_create")
         self._h = h
-        self.admitted = [t for t in range(len(self.tenants)) if _lib.dsssp_server_slot(h, t) >= 0]
-        self.slot = {t: _lib.dsssp_server_slot(h, t) for t in self.admitted}
         self.reserved = sum(self.footprints[t] for t in self.admitted)
+
+    @property
+    def admitted(self) -> list[int]:
+        """Tenants in the pool now (in tenant order); after close, those at close."""
+        if not (getattr(self, "_h", None) and self._h.value):
+            return list(getattr(self, "_admitted_final", []))
+        return [t for t in range(len(self.tenants)) if self.state(t) == TENANT_ADMITTED]
+
+    @property
+    def slot(self) -> dict:
+        return {t: _lib.dsssp_server_slot(self._h, t) for t in self.admitted}
+
+    def state(self, tenant: int) -> int:
+        """TENANT_WAITING, TENANT_ADMITTED or TENANT_REMOVED."""
+        return _check(_lib.dsssp_server_tenant_state(self._h, int(tenant)), "server_tenant_state")
+
+    def add_tenant(self, tenant: Tenant) -> int:
+        """Adds a tenant while the server runs: admitted at once when its footprint fits the
+        budget and free vertex ids exist (its tree is built on the device), else it waits for
+        a removal to free memory.  Returns its tenant id."""
+        u = np.ascontiguousarray(tenant.u, np.int32)
+        v = np.ascontiguousarray(tenant.v, np.int32)
+        w = np.ascontiguousarray(tenant.w, np.int32)
+        t = C.c_int32()
+        _check(_lib.dsssp_server_add_tenant(self._h, int(tenant.n), len(u), u.ctypes.data if len(u) else None,
+                                            v.ctypes.data if len(v) else None, w.ctypes.data if len(w) else None,
+                                            int(tenant.src), C.byref(t)), "server_add_tenant")
+        assert t.value == len(self.tenants)
+        self.tenants.append(tenant)
+        self.footprints.append(estimate_footprint(tenant.n, len(u), *self._slack))
+        return t.value
+
+    def remove_tenant(self, tenant: int) -> None:
+        """Removes a tenant after the running epoch: its queued requests are refused, its memory
+        is released and waiting tenants that now fit are admitted."""
+        _check(_lib.dsssp_server_remove_tenant(self._h, int(tenant)), "server_remove_tenant")
+
+    @property
+    def recovered_epochs(self) -> int:
+        e = C.c_int64()
+        _check(_lib.dsssp_server_recovered_epochs(self._h, C.byref(e)), "server_recovered_epochs")
+        return e.value
+
+    def debug_set(self, what: int, value: int) -> None:
+        """Failure-detection test hooks on the pool's graph, applied between epochs."""
+        _check(_lib.dsssp_server_debug_set(self._h, int(what), int(value)), "server_debug_set")
 
     def close(self) -> None:
         if getattr(self, "_h", None) and self._h.value:
             self._final = self._info()  # counters stay readable after close
+            self._admitted_final = self.admitted
             _lib.dsssp_server_destroy(self._h)
             self._h = C.c_void_p()
 
@@ -184,8 +241,9 @@ class Server:
                 r.start = r.arrival + (info.start_us - info.arrival_us) * 1e-6
                 r.done = r.arrival + (info.done_us - info.arrival_us) * 1e-6
                 r.refused = info.status == REFUSED
-                r.error = None if info.status in (0, REFUSED) else info.error.decode(errors="replace")
-                if record and info.status == 0:
+                r.recomputed = info.status == W_RECOMPUTED
+                r.error = None if info.status in (0, REFUSED, W_RECOMPUTED) else info.error.decode(errors="replace")
+                if record and info.status in (0, W_RECOMPUTED):
                     t = self.tenants[r.tenant]
                     p = np.empty(t.n, np.int32)
                     d = np.empty(t.n, np.int64)
@@ -203,6 +261,7 @@ def summarize(reqs) -> dict:
         "requests": len(reqs),
         "served": len(served),
         "refused": sum(1 for r in reqs if r.refused),
+        "recomputed": sum(1 for r in reqs if r.recomputed),
         "failed": sum(1 for r in reqs if r.error is not None),
         "changes": int(changes),
         "span_s": span,

@@ -9,7 +9,8 @@
  *
  * Conventions
  *   - Every function that can fail returns 0 (DSSSP_OK) or a negative DSSSP_E* code;
- *     dsssp_last_error() gives a message for the calling thread's last failure.
+ *     dsssp_last_error() gives a message for the calling thread's last failure.  A batch
+ *     may also return the positive DSSSP_W_RECOMPUTED: it succeeded by a slower route.
  *   - Host buffers are owned by the caller; device memory is owned by the library.
  *   - Vertex ids are 0..n-1.  Weights are int32 >= 0.  A distance is an integer below
  *     2^32-1; an unreachable vertex has parent -1 and distance DSSSP_UNREACHABLE.
@@ -39,6 +40,13 @@ extern "C" {
 #define DSSSP_E_BAD_WEIGHT (-10)    /* negative weight on an edge that is added */
 #define DSSSP_E_NO_DEVICE (-11)     /* no usable CUDA device */
 #define DSSSP_E_COOP (-12)          /* the persistent update kernel could not be co-resident */
+
+/* A batch whose update kernel failed (a timed-out device wait, the round cap, an internal list
+ * capacity or a parent cycle) after its edits reached the adjacency, recovered by computing
+ * the trees again from the roots on the updated graph (opts.recover): the graph and tree are
+ * exactly what a successful batch gives; stats.recovered_from holds the failure's code and
+ * dsssp_last_error() describes it.  A success code, not an error. */
+#define DSSSP_W_RECOMPUTED 2
 
 #define DSSSP_UNREACHABLE (-1)
 
@@ -84,7 +92,11 @@ typedef struct {
                              instantiated CUDA graph whose node parameters are updated per
                              batch; 0 = plain stream launches.  Falls back to plain launches
                              if the graph cannot be built. */
-    int32_t reserved1;
+    int32_t recover;      /* 1 (the default) = a batch whose update kernel fails after its edits
+                             reached the adjacency recomputes the trees from the roots and returns
+                             DSSSP_W_RECOMPUTED (or, if that fails too, the error, and the tree
+                             must be loaded or computed before the next batch); 0 = return the
+                             error and leave the tree as the kernel left it (unfinished) */
 } dsssp_opts;
 
 /* Counters of one batch (or one tree computation), read back from the device. */
@@ -124,6 +136,8 @@ typedef struct {
     double t_delete_ms;        /* k_delete alone (CUDA events; batches at timing level 2) */
     double t_append_ms;        /* k_append alone, seeds included (CUDA events; batches at timing
                                   level 2; with row growth it spans the growth too) */
+    int64_t recovered_from;    /* DSSSP_W_RECOMPUTED: the code of the failure recovered from */
+    double t_recompute_ms;     /* DSSSP_W_RECOMPUTED: the recomputation of the trees (CUDA events) */
 } dsssp_stats;
 
 /* ---- engine ------------------------------------------------------------------------ */
@@ -158,6 +172,20 @@ int dsssp_tree_compute(dsssp_graph* g, int32_t src, dsssp_stats* st);
  * reference (its Dijkstra has one hard-coded source, seqSSSPwithDist_undir.cpp:196). */
 int dsssp_tree_compute_multi(dsssp_graph* g, const int32_t* srcs, int32_t k, dsssp_stats* st);
 
+/* Adds k sources to the resident forest without recomputing it: each becomes a root
+ * (distance 0, its own parent) and relaxation from them lowers every distance they improve,
+ * so the result is the exact forest from the old roots and the new ones together (the current
+ * distances stay valid upper bounds).  On a graph with no tree yet it is dsssp_tree_compute_multi.
+ * Used to bring a new tenant's part of a pooled store to life.  No counterpart in the reference. */
+int dsssp_tree_add_sources(dsssp_graph* g, const int32_t* srcs, int32_t k, dsssp_stats* st);
+
+/* Removes every edge of the vertex range [first, first + count) and makes its vertices
+ * unreachable (roots in it stop being roots); the range must be closed under adjacency (no
+ * live edge between it and the rest: DSSSP_E_INVAL otherwise, nothing changed).  The entries
+ * become tombstones that dsssp_graph_compact reclaims.  Used to retire a tenant's part of a
+ * pooled store.  No counterpart in the reference. */
+int dsssp_graph_clear_range(dsssp_graph* g, int32_t first, int32_t count);
+
 /* Like dsssp_tree_load, but any number (>= 1) of roots: a forest of shortest-path trees,
  * e.g. one per tenant graph of a pooled graph store. */
 int dsssp_forest_load(dsssp_graph* g, const int32_t* parent, const int64_t* dist);
@@ -169,9 +197,10 @@ int dsssp_tree_read(dsssp_graph* g, int32_t* parent, int64_t* dist);
 /* Test hooks for failure detection (not for production use).
  * DSSSP_DEBUG_SPIN_LIMIT: polls of about 1 us before a grid barrier of the update kernel
  *   gives up with DSSSP_E_TIMEOUT (0 = the default 2^20, about 1 s).
- * DSSSP_DEBUG_STALL_US: the last CTA of the update kernel waits this many microseconds
- *   (0..1,000,000; 0 = off) before its first grid barrier, so that a small spin limit runs
- *   out: the batch fails with DSSSP_E_TIMEOUT and the device stays usable. */
+ * DSSSP_DEBUG_STALL_US: the last CTA of the next launch of the update kernel waits this many
+ *   microseconds (0..1,000,000; 0 = off) before its first grid barrier, so that a small spin
+ *   limit runs out: the batch fails with DSSSP_E_TIMEOUT and the device stays usable.  The
+ *   hook applies to one launch and then clears itself. */
 #define DSSSP_DEBUG_SPIN_LIMIT 1
 #define DSSSP_DEBUG_STALL_US 2
 int dsssp_debug_set(dsssp_graph* g, int32_t what, int64_t value);
@@ -376,7 +405,9 @@ int dsssp_pool_create(int32_t count, const int32_t* n, const int64_t* m, const i
 void dsssp_pool_destroy(dsssp_pool* p);
 /* The underlying engine graph (options, snapshots, statistics); owned by the pool. */
 dsssp_graph* dsssp_pool_graph(dsssp_pool* p);
-/* count + 1 offsets of the graphs in the pool's id space. */
+/* count + 1 offsets: offsets[i] = first id of graph i, offsets[count] = the end of the last
+ * graph (graphs created with the pool are contiguous: graph i has offsets[i + 1] - offsets[i]
+ * vertices; dsssp_pool_graph_range gives any graph's range). */
 int dsssp_pool_offsets(const dsssp_pool* p, int64_t* offsets);
 /* sources[i] = source of graph i (local id). */
 int dsssp_pool_tree_compute(dsssp_pool* p, const int32_t* sources, dsssp_stats* st);
@@ -386,23 +417,49 @@ int dsssp_pool_forest_load(dsssp_pool* p, const int32_t* const* parent, const in
  * out (cap records); *k = its size.  out may be NULL to validate and size it only. */
 int dsssp_pool_union(dsssp_pool* p, int32_t nb, const int32_t* graphs, const dsssp_change* const* batches,
                      const int64_t* sizes, dsssp_change* out, int64_t cap, int64_t* k);
-/* Applies the union batch of nb batches in one launch sequence and waits for it. */
+/* Applies the union batch of nb batches in one launch sequence and waits for it (returns what
+ * dsssp_apply_batch returns, DSSSP_W_RECOMPUTED included). */
 int dsssp_pool_apply(dsssp_pool* p, int32_t nb, const int32_t* graphs, const dsssp_change* const* batches,
                      const int64_t* sizes, dsssp_stats* st);
 /* The tree of one graph (n[graph] entries, local ids). */
 int dsssp_pool_tree_read(dsssp_pool* p, int32_t graph, int32_t* parent, int64_t* dist);
+/* A pool with reserve_vertices spare vertex ids after its graphs (count may be 0 when the
+ * reserve is not): room for graphs added later with dsssp_pool_add_graph. */
+int dsssp_pool_create_reserved(int32_t count, const int32_t* n, const int64_t* m, const int32_t* const* u,
+                               const int32_t* const* v, const int32_t* const* w, int64_t reserve_vertices,
+                               const dsssp_opts* o, dsssp_pool** out);
+/* Adds a graph (local ids, source src) in the lowest free id range of at least n ids: its source
+ * becomes a new root and its edges go in as one insertion batch, whose relaxation builds its tree
+ * (the other graphs are not touched).  *graph = its index.  DSSSP_E_OOM when no free range is
+ * large enough (nothing changed). */
+int dsssp_pool_add_graph(dsssp_pool* p, int32_t n, int64_t m, const int32_t* u, const int32_t* v,
+                         const int32_t* w, int32_t src, int32_t* graph);
+/* Removes graph `graph`: its edges become tombstones (dsssp_graph_compact reclaims them), its
+ * vertices unreachable, its ids a free range for later graphs.  Its index is not reused. */
+int dsssp_pool_remove_graph(dsssp_pool* p, int32_t graph);
+/* First id and vertex count (0 once removed) of a graph in the pool's id space. */
+int dsssp_pool_graph_range(const dsssp_pool* p, int32_t graph, int64_t* first, int32_t* n);
+/* Vertex ids of the store, the free ones, and the largest free range; any may be NULL. */
+int dsssp_pool_capacity(const dsssp_pool* p, int64_t* vertices, int64_t* free_vertices, int64_t* largest_free);
 /* Device bytes the engine needs for a graph of n vertices and m undirected edges (admission). */
 int64_t dsssp_estimate_footprint(int32_t n, int64_t m, int32_t slack_pct, int32_t slack_min);
 
 /* ---- serving: a request loop with continuous batching ----------------------------
  * Tenants are admitted in order while their estimated footprint fits memory_budget and live
- * in one pool.  dsssp_submit queues a request and returns; a worker thread runs epochs back to
- * back, each taking the oldest waiting request of every tenant (oldest first, at most
- * max_epoch_requests) and applying them as one union batch.  A tenant's requests apply in
- * arrival order and each result equals applying that batch alone.  While no request waits,
- * the worker compacts the store once its tombstones exceed compact_dead_frac of the live
- * entries (< 0: never) or its spare region is more than compact_spare_frac used.  Completed
- * requests are collected with dsssp_poll.  Submitting, polling and reading are thread-safe. */
+ * in one pool; a tenant that does not fit waits (its vertex ids are reserved) and is admitted
+ * when a removal frees memory.  Tenants can also be added and removed while the server runs.
+ * dsssp_submit validates a request, queues a copy of its batch and returns; a worker thread
+ * runs epochs back to back, each taking the oldest waiting request of every admitted tenant
+ * (oldest first, at most max_epoch_requests), copying their records once into a pinned buffer
+ * (ids shifted into the pool's id space) and applying them as one union batch.  A tenant's
+ * requests apply in arrival order and each result equals applying that batch alone.
+ * Requests for a waiting or removed tenant are refused.  An epoch whose update kernel fails
+ * is recovered on the device (DSSSP_W_RECOMPUTED, see dsssp_opts.recover): its requests are
+ * served with that status and every tenant's tree stays exact.  While no request waits, the
+ * worker compacts the store once its tombstones exceed compact_dead_frac of the live entries
+ * (< 0: never) or its spare region is more than compact_spare_frac used.  Completed requests
+ * are collected with dsssp_poll.  Submitting, polling, reading, adding and removing tenants
+ * are thread-safe. */
 typedef struct dsssp_server dsssp_server;
 typedef struct {
     int64_t memory_budget;       /* device bytes for tenants; 0 = no limit */
@@ -410,9 +467,18 @@ typedef struct {
     int32_t record;              /* 1 = keep the tenant's tree after each request (dsssp_server_result) */
     double compact_dead_frac;    /* default 0.25 */
     double compact_spare_frac;   /* default 0.75 */
+    int64_t reserve_vertices;    /* spare vertex ids for tenants added later (beyond the ids that
+                                    tenants waiting at creation hold); default 0 */
 } dsssp_server_opts;
 
-#define DSSSP_REFUSED 1 /* request status: its tenant was not admitted */
+#define DSSSP_REFUSED 1 /* request status: its tenant is not admitted (waiting, removed, unknown) */
+/* request status DSSSP_W_RECOMPUTED (2): served; its epoch's update kernel failed and the trees
+ * were recomputed (error says why) */
+
+/* tenant states (dsssp_server_tenant_state) */
+#define DSSSP_TENANT_WAITING 0  /* does not fit the memory budget or the free ids yet */
+#define DSSSP_TENANT_ADMITTED 1
+#define DSSSP_TENANT_REMOVED 2
 
 typedef struct {
     int64_t id;
@@ -427,15 +493,32 @@ typedef struct {
 } dsssp_request_info;
 
 void dsssp_default_server_opts(dsssp_server_opts* so);
-/* Tenant t: graph (n[t], m[t], u[t], v[t], w[t]) with source sources[t]; trees are computed
- * on the device before the worker starts. */
+/* Tenant t: graph (n[t], m[t], u[t], v[t], w[t]) with source sources[t]; trees of the admitted
+ * tenants are computed on the device before the worker starts.  count may be 0 when
+ * so->reserve_vertices is not (tenants then come with dsssp_server_add_tenant). */
 int dsssp_server_create(int32_t count, const int32_t* n, const int64_t* m, const int32_t* const* u,
                         const int32_t* const* v, const int32_t* const* w, const int32_t* sources,
                         const dsssp_server_opts* so, const dsssp_opts* o, dsssp_server** out);
 /* Finishes the queued requests, stops the worker and frees everything. */
 void dsssp_server_destroy(dsssp_server* s);
-/* Pool graph of a tenant, -1 if it was not admitted. */
+/* Pool graph of a tenant, -1 if it is not admitted (waiting or removed). */
 int dsssp_server_slot(const dsssp_server* s, int32_t tenant);
+/* DSSSP_TENANT_WAITING / _ADMITTED / _REMOVED, or DSSSP_E_INVAL for no such tenant. */
+int dsssp_server_tenant_state(const dsssp_server* s, int32_t tenant);
+/* Adds a tenant (graph n, m, u, v, w with source src; the arrays are copied if it has to wait)
+ * and returns its id in *tenant.  It is admitted at once (after the running epoch) when its
+ * footprint fits the budget and a free range of n vertex ids exists -- its tree is built on the
+ * device from its edges -- and waits otherwise. */
+int dsssp_server_add_tenant(dsssp_server* s, int32_t n, int64_t m, const int32_t* u, const int32_t* v,
+                            const int32_t* w, int32_t src, int32_t* tenant);
+/* Removes a tenant after the running epoch: its queued requests are refused, its edges and ids
+ * are released (the edges' slots at the next compaction), its footprint leaves the budget, and
+ * waiting tenants that now fit are admitted in the order they came. */
+int dsssp_server_remove_tenant(dsssp_server* s, int32_t tenant);
+/* Epochs that were recovered by recomputing the trees (DSSSP_W_RECOMPUTED). */
+int dsssp_server_recovered_epochs(dsssp_server* s, int64_t* epochs);
+/* dsssp_debug_set on the pool's graph, between epochs (failure-detection tests). */
+int dsssp_server_debug_set(dsssp_server* s, int32_t what, int64_t value);
 /* Queues a copy of the batch; *id identifies the request in dsssp_poll. */
 int dsssp_submit(dsssp_server* s, int32_t tenant, const dsssp_change* changes, int64_t k, int64_t* id);
 /* Queues several requests at one instant (they can share an epoch). */

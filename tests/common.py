@@ -46,3 +46,16 @@ def check_against_oracle(n, u, v, w, changes, src, parent, dist, where=""):
     assert len(diff) == 0, f"{where}: {len(diff)} distances differ, e.g. v={diff[:5]} got {dist[diff[:5]]} want {od[diff[:5]]}"
     res = O.validate(n, g, src, dist, parent)
     assert res == 0, f"{where}: invalid tree: {res}"
+
+
+def lines_after(n, u, v, w, changes):
+    """The edge lines of the graph after a batch (the reference's semantics: insertions
+    appended, then every line matching a deletion's pair and weight removed), for chaining
+    batches in the oracle."""
+    _, kept = O.updated_graph(n, u, v, w, changes, return_kept=True)
+    ins = changes[changes["op"] == 1]
+    lu = np.concatenate([u, ins["u"]]).astype(np.int32)
+    lv = np.concatenate([v, ins["v"]]).astype(np.int32)
+    lw = np.concatenate([w, ins["w"]]).astype(np.int32)
+    keep = kept[: len(lu)].astype(bool)
+    return lu[keep], lv[keep], lw[keep]
