@@ -68,17 +68,21 @@ def test_round_cap_is_recovered_exactly():
     n, m = 5000, 20000
     u, v, w = D.gen_er(n, m, 1, 100, 71)
     ch = D.gen_changes(n, u, v, w, 800, 800, seed=72)
-    with D.Graph(n, u, v, w, max_rounds=1) as g:
-        g.tree_compute(0)
-        st = g.apply_batch(ch)
-        assert st.recovered_from == D.E_NO_CONVERGENCE
-        p, d = g.tree_read()
-        check_against_oracle(n, u, v, w, ch, 0, p, d, "round cap")
-    with D.Graph(n, u, v, w, max_rounds=1, recover=0) as g:
-        g.tree_compute(0)
-        with pytest.raises(D.DsssspError) as e:
-            g.apply_batch(ch)
-        assert e.value.code == D.E_NO_CONVERGENCE
+    for recover in (1, 0):
+        with D.Graph(n, u, v, w, recover=recover) as g:
+            g.tree_compute(0)
+            o = g.get_opts()
+            o.max_rounds = 1
+            g.set_opts(o)
+            if recover:
+                st = g.apply_batch(ch)
+                assert st.recovered_from == D.E_NO_CONVERGENCE
+                p, d = g.tree_read()
+                check_against_oracle(n, u, v, w, ch, 0, p, d, "round cap")
+            else:
+                with pytest.raises(D.DsssspError) as e:
+                    g.apply_batch(ch)
+                assert e.value.code == D.E_NO_CONVERGENCE
 
 
 def test_debug_hooks_reject_bad_values():

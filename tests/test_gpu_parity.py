@@ -391,18 +391,26 @@ def test_errors_leave_graph_unchanged():
 
 def test_parent_cycle_is_reported():
     """A tree with a parent cycle below a cut-off vertex: pointer jumping gives up after a
-    bounded number of passes and reports DSSSP_E_BAD_TREE."""
+    bounded number of passes and reports DSSSP_E_BAD_TREE (recovery off); with recovery on the
+    batch is finished by recomputing the tree from the root, which is exact."""
     n = 6
     u = np.array([0, 1, 2, 3, 4], np.int32)
     v = np.array([1, 2, 3, 4, 5], np.int32)
     w = np.ones(5, np.int32)
     parent = np.array([0, 0, 1, 4, 3, 4], np.int32)  # 3 <-> 4 cycle
     dist = np.array([0, 1, 2, 3, 4, 5], np.int64)
-    with D.Graph(n, u, v, w, bfs_levels=0) as g:
+    ch = D.make_changes([0], [1], [1], [0])
+    with D.Graph(n, u, v, w, bfs_levels=0, recover=0) as g:
         g.tree_load(parent, dist)
         with pytest.raises(D.DsssspError) as e:
-            g.apply_batch(D.make_changes([0], [1], [1], [0]))
+            g.apply_batch(ch)
         assert e.value.code == D.E_BAD_TREE
+    with D.Graph(n, u, v, w, bfs_levels=0) as g:
+        g.tree_load(parent, dist)
+        st = g.apply_batch(ch)
+        assert st.recovered_from == D.E_BAD_TREE
+        p, d = g.tree_read()
+        check_against_oracle(n, u, v, w, ch, 0, p, d, "parent cycle recovered")
 
 
 @pytest.mark.parametrize("opts", [{}, {"bfs_levels": 0}, {"bfs_levels": 1}, {"delta": 2}])

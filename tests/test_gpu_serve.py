@@ -160,7 +160,7 @@ def test_tenants_join_and_leave_while_serving():
     removal frees memory; a tenant added at run time is admitted into free ids; a removed
     tenant's later requests are refused.  Every served request's result equals its tenant's
     batches applied alone, and the oracle's tree."""
-    sizes = [1500, 3000, 1200, 1000, 800]
+    sizes = [2000, 12000, 1500, 3000, 2500]
     ten = []
     for i, n in enumerate(sizes):
         u, v, w = D.gen_er(n, 3 * n, 1, 100, 500 + i)
