@@ -184,6 +184,7 @@ _sig("dsssp_server_set_record", C.c_int, _P, C.c_int32)
 _sig("dsssp_server_validate", C.c_int, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int64))
 _sig("dsssp_apply_batch", C.c_int, _P, _P, C.c_int64, _P, C.POINTER(Stats))
 _sig("dsssp_apply_batch_async", C.c_int, _P, _P, C.c_int64, _P)
+_sig("dsssp_apply_batch_host_async", C.c_int, _P, _P, C.c_int64, _P)
 _sig("dsssp_batch_finish", C.c_int, _P, C.POINTER(Stats))
 _sig("dsssp_graph_set_opts", C.c_int, _P, C.POINTER(Opts))
 _sig("dsssp_graph_get_opts", C.c_int, _P, C.POINTER(Opts))
@@ -241,7 +242,7 @@ EXPORTED = [
     "dsssp_server_set_record", "dsssp_server_validate", "dsssp_tree_add_sources", "dsssp_graph_clear_range",
     "dsssp_pool_create_reserved", "dsssp_pool_add_graph", "dsssp_pool_remove_graph", "dsssp_pool_graph_range",
     "dsssp_pool_capacity", "dsssp_server_tenant_state", "dsssp_server_add_tenant", "dsssp_server_remove_tenant",
-    "dsssp_server_recovered_epochs", "dsssp_server_debug_set",
+    "dsssp_server_recovered_epochs", "dsssp_server_debug_set", "dsssp_apply_batch_host_async",
 ]
 
 

@@ -1866,18 +1866,23 @@ int dsssp_batch_finish(dsssp_graph* g, dsssp_stats* st) {
     return finish_batch(g, st);
 }
 
-int dsssp_apply_batch(dsssp_graph* g, const dsssp_change* changes, int64_t k, void* stream, dsssp_stats* st) {
+int dsssp_apply_batch_host_async(dsssp_graph* g, const dsssp_change* changes, int64_t k, void* stream) {
     if (!g || k < 0 || (k > 0 && !changes)) return fail(DSSSP_E_INVAL, "apply_batch: bad arguments");
     int rc = set_device(g);
     if (rc) return rc;
-    if (st) memset(st, 0, sizeof(*st));
+    if (g->pending) return fail(DSSSP_E_INVAL, "apply_batch: previous batch not finished");
     if (k == 0) return DSSSP_OK;
     rc = ensure_batch(g, k);
     if (rc) return rc;
     cudaStream_t s = stream ? (cudaStream_t)stream : g->stream;
     CK(cudaMemcpyAsync(g->d_chg, changes, sizeof(int4) * (size_t)k, cudaMemcpyHostToDevice, s), "batch upload");
-    rc = dsssp_apply_batch_async(g, (const dsssp_change*)g->d_chg, k, s);
-    if (rc) return rc;
+    return dsssp_apply_batch_async(g, (const dsssp_change*)g->d_chg, k, s);
+}
+
+int dsssp_apply_batch(dsssp_graph* g, const dsssp_change* changes, int64_t k, void* stream, dsssp_stats* st) {
+    if (st) memset(st, 0, sizeof(*st));
+    const int rc = dsssp_apply_batch_host_async(g, changes, k, stream);
+    if (rc || k == 0) return rc;
     return finish_batch(g, st);
 }
 

@@ -494,9 +494,97 @@ struct dsssp_server {
         cv_done.notify_all();
     }
 
-    void run() {
-        std::vector<Req*> ep;
+    // An epoch: its requests and the id shift of each (its tenant's first id in the pool).
+    struct Epoch {
+        std::vector<Req*> reqs;
         std::vector<int32_t> shift;
+        int64_t total = 0;
+        double start = 0;
+    };
+    dsssp_change* stage[2] = {nullptr, nullptr};  // pinned staging of two epochs' records
+    int64_t stage_cap[2] = {0, 0};
+    std::atomic<int> dev_waiters{0};  // threads waiting for the device between epochs
+
+    // The oldest waiting request of every admitted tenant, oldest first (with dev held).
+    void form(Epoch& e) {
+        e.reqs.clear();
+        e.shift.clear();
+        e.total = 0;
+        std::lock_guard<std::mutex> lk(mu);
+        std::vector<std::pair<double, int32_t>> order;
+        for (int32_t t = 0; t < (int32_t)tenants.size(); t++)
+            if (!tenants[(size_t)t].queue.empty()) order.emplace_back(tenants[(size_t)t].queue.front()->info.arrival_us, t);
+        std::sort(order.begin(), order.end());
+        if (so.max_epoch_requests > 0 && (int32_t)order.size() > so.max_epoch_requests)
+            order.resize((size_t)so.max_epoch_requests);
+        for (auto& o : order) {
+            TenantRec& tr = tenants[(size_t)o.second];
+            e.reqs.push_back(tr.queue.front());
+            tr.queue.pop_front();
+            e.shift.push_back((int32_t)pool->first[(size_t)tr.graph]);
+            e.total += (int64_t)e.reqs.back()->ch.size();
+        }
+        pending -= (int64_t)e.reqs.size();
+        inflight += (int64_t)e.reqs.size();
+    }
+
+    // One pass over the records: copied into pinned stage b with ids shifted into the pool's
+    // id space (they were validated at submission).
+    int assemble(const Epoch& e, int b) {
+        if (e.total > stage_cap[b]) {
+            if (stage[b]) dsssp_host_free(stage[b]);
+            stage_cap[b] = 0;
+            const int64_t cap = e.total + e.total / 2 + 4096;
+            stage[b] = (dsssp_change*)dsssp_host_alloc(sizeof(dsssp_change) * (size_t)cap);
+            if (!stage[b]) return fail(DSSSP_E_OOM, "server: pinned staging buffer of %lld records", (long long)cap);
+            stage_cap[b] = cap;
+        }
+        int64_t at = 0;
+        for (size_t i = 0; i < e.reqs.size(); i++) {
+            copy_shifted(e.reqs[i]->ch.data(), (int64_t)e.reqs[i]->ch.size(), e.shift[i], stage[b] + at);
+            at += (int64_t)e.reqs[i]->ch.size();
+        }
+        return DSSSP_OK;
+    }
+
+    // Completes an epoch's requests with status rc (with dev held).
+    void complete_epoch(Epoch& e, int rc, double end) {
+        char why[96] = {0};
+        if (rc) snprintf(why, sizeof why, "%s", dsssp_last_error());
+        if (rc >= 0 && record.load()) {
+            for (Req* r : e.reqs) {
+                const int32_t gi = tenants[(size_t)r->info.tenant].graph, nn = pool->size(gi);
+                std::vector<int32_t> par((size_t)nn);
+                std::vector<int64_t> dist((size_t)nn);
+                if (dsssp_pool_tree_read(pool, gi, par.data(), dist.data()) == DSSSP_OK) {
+                    std::lock_guard<std::mutex> lk(mu);
+                    results[r->info.id] = {std::move(par), std::move(dist)};
+                }
+            }
+        }
+        std::lock_guard<std::mutex> lk(mu);
+        for (Req* r : e.reqs) {
+            r->info.epoch = epochs;
+            r->info.start_us = e.start;
+            r->info.done_us = end;
+            r->info.status = rc;
+            if (rc) snprintf(r->info.error, sizeof r->info.error, "%s", why);
+            std::vector<dsssp_change>().swap(r->ch);
+            complete(r);
+        }
+        if (rc == DSSSP_W_RECOMPUTED) recovered++;
+        epochs++;
+        inflight -= (int64_t)e.reqs.size();
+        e.reqs.clear();
+    }
+
+    // Epochs are pipelined: while epoch i runs on the device, the host forms epoch i + 1 and
+    // copies its records into the other pinned buffer; then it waits for epoch i, completes its
+    // requests (reading recorded trees) and enqueues epoch i + 1.  The device mutex is held
+    // while epochs are in flight and released between them as soon as another thread waits
+    // for it (reads, admission, removal) or no request is left.
+    void run() {
+        Epoch ep[2];
         for (;;) {
             {
                 std::unique_lock<std::mutex> lk(mu);
@@ -506,71 +594,32 @@ struct dsssp_server {
                 }
                 if (pending == 0 && stop) return;
             }
+            while (dev_waiters.load() > 0) std::this_thread::sleep_for(std::chrono::microseconds(20));
             std::lock_guard<std::mutex> d(dev);  // before mu: no admission or removal mid-epoch
-            {
-                std::lock_guard<std::mutex> lk(mu);
-                // the epoch: the oldest waiting request of every admitted tenant, oldest first
-                std::vector<std::pair<double, int32_t>> order;
-                for (int32_t t = 0; t < (int32_t)tenants.size(); t++)
-                    if (!tenants[(size_t)t].queue.empty())
-                        order.emplace_back(tenants[(size_t)t].queue.front()->info.arrival_us, t);
-                std::sort(order.begin(), order.end());
-                if (so.max_epoch_requests > 0 && (int32_t)order.size() > so.max_epoch_requests)
-                    order.resize((size_t)so.max_epoch_requests);
-                ep.clear();
-                shift.clear();
-                for (auto& o : order) {
-                    TenantRec& tr = tenants[(size_t)o.second];
-                    ep.push_back(tr.queue.front());
-                    tr.queue.pop_front();
-                    shift.push_back((int32_t)pool->first[(size_t)tr.graph]);
+            int cur = 0;
+            bool flying = false;  // ep[cur ^ 1] is on the device
+            for (;;) {
+                const bool more = dev_waiters.load() == 0;
+                if (more) form(ep[cur]);
+                const int arc = ep[cur].reqs.empty() ? DSSSP_OK : assemble(ep[cur], cur);
+                if (flying) {
+                    dsssp_stats st;
+                    const int rc = dsssp_batch_finish(pool->g, &st);
+                    complete_epoch(ep[cur ^ 1], rc, now_us());
+                    flying = false;
                 }
-                pending -= (int64_t)ep.size();
-                inflight = (int64_t)ep.size();
-            }
-            if (ep.empty()) continue;
-            // one pass over the records: copied into the pinned stage with ids shifted into the
-            // pool's id space (they were validated at submission)
-            int64_t total = 0;
-            for (Req* r : ep) total += (int64_t)r->ch.size();
-            int rc = pool->ensure_stage(total);
-            double start = now_us(), end = start;
-            char why[96] = {0};
-            if (!rc) {
-                int64_t at = 0;
-                for (size_t i = 0; i < ep.size(); i++) {
-                    copy_shifted(ep[i]->ch.data(), (int64_t)ep[i]->ch.size(), shift[i], pool->stage + at);
-                    at += (int64_t)ep[i]->ch.size();
+                if (ep[cur].reqs.empty()) break;
+                ep[cur].start = now_us();
+                int rc = arc;
+                if (!rc) rc = dsssp_apply_batch_host_async(pool->g, stage[cur], ep[cur].total, nullptr);
+                if (rc) {  // nothing was enqueued
+                    complete_epoch(ep[cur], rc, now_us());
+                    break;
                 }
-                dsssp_stats st;
-                rc = dsssp_apply_batch(pool->g, pool->stage, total, nullptr, &st);
-                end = now_us();
-            }
-            if (rc) snprintf(why, sizeof why, "%s", dsssp_last_error());
-            if (rc >= 0 && record.load()) {
-                for (Req* r : ep) {
-                    const int32_t gi = tenants[(size_t)r->info.tenant].graph, nn = pool->size(gi);
-                    std::vector<int32_t> par((size_t)nn);
-                    std::vector<int64_t> dist((size_t)nn);
-                    if (dsssp_pool_tree_read(pool, gi, par.data(), dist.data()) == DSSSP_OK) {
-                        std::lock_guard<std::mutex> lk(mu);
-                        results[r->info.id] = {std::move(par), std::move(dist)};
-                    }
-                }
+                flying = true;
+                cur ^= 1;
             }
             std::lock_guard<std::mutex> lk(mu);
-            for (Req* r : ep) {
-                r->info.epoch = epochs;
-                r->info.start_us = start;
-                r->info.done_us = end;
-                r->info.status = rc;
-                if (rc) snprintf(r->info.error, sizeof r->info.error, "%s", why);
-                std::vector<dsssp_change>().swap(r->ch);
-                complete(r);
-            }
-            if (rc == DSSSP_W_RECOMPUTED) recovered++;
-            epochs++;
-            inflight = 0;
             upkeep = pending == 0;  // the idle upkeep comes next; drain waits for it
         }
     }
@@ -585,9 +634,27 @@ struct dsssp_server {
         for (auto& t : tenants)
             for (Req* r : t.queue) delete r;
         for (Req* r : done) delete r;
+        for (auto* b : stage)
+            if (b) dsssp_host_free(b);
         dsssp_pool_destroy(pool);
     }
 };
+
+namespace {
+
+// Takes the server's device mutex from a thread other than the worker: announced first, so
+// that the worker leaves its epoch pipeline after the epoch in flight.
+struct DevLock {
+    dsssp_server* s;
+    explicit DevLock(dsssp_server* sv) : s(sv) {
+        s->dev_waiters.fetch_add(1);
+        s->dev.lock();
+        s->dev_waiters.fetch_sub(1);
+    }
+    ~DevLock() { s->dev.unlock(); }
+};
+
+}  // namespace
 
 extern "C" {
 
@@ -708,7 +775,7 @@ int dsssp_server_add_tenant(dsssp_server* s, int32_t n, int64_t m, const int32_t
     r.m = m;
     r.src = src;
     r.footprint = dsssp_estimate_footprint(n, m, s->slack_pct, s->slack_min);
-    std::lock_guard<std::mutex> d(s->dev);  // after any running epoch
+    DevLock d(s);  // after any running epoch
     int32_t t;
     {
         std::lock_guard<std::mutex> lk(s->mu);
@@ -727,7 +794,7 @@ int dsssp_server_add_tenant(dsssp_server* s, int32_t n, int64_t m, const int32_t
 
 int dsssp_server_remove_tenant(dsssp_server* s, int32_t tenant) {
     if (!s) return fail(DSSSP_E_INVAL, "server_remove_tenant: NULL server");
-    std::lock_guard<std::mutex> d(s->dev);  // after any running epoch
+    DevLock d(s);  // after any running epoch
     int32_t gi = -1;
     int64_t fp = 0;
     {
@@ -769,9 +836,10 @@ int dsssp_submit_many(dsssp_server* s, int32_t count, const int32_t* tenants, co
                       const int64_t* sizes, int64_t* ids) {
     if (!s || count < 0 || (count > 0 && (!tenants || !batches || !sizes || !ids)))
         return fail(DSSSP_E_INVAL, "submit: bad arguments");
-    // Validation and the copy of each batch happen before the queue lock (a tenant's size is
-    // fixed; only its admission state is read under the lock), so a large submission stays off
-    // the other requests' latency.
+    // Requests are taken in chunks (up to 64 requests or about 2^20 records): a chunk is
+    // validated and copied outside the queue lock and then queued, so the worker starts on the
+    // first chunk while the later ones are still being copied, and a large submission stays
+    // off the other requests' latency.  Every request carries the call's arrival time.
     const double t = s->now_us();
     std::vector<int32_t> tn((size_t)count, -1);
     {
@@ -779,56 +847,67 @@ int dsssp_submit_many(dsssp_server* s, int32_t count, const int32_t* tenants, co
         for (int32_t i = 0; i < count; i++)
             if (tenants[i] >= 0 && tenants[i] < (int32_t)s->tenants.size()) tn[(size_t)i] = s->tenants[(size_t)tenants[i]].n;
     }
-    std::vector<Req*> reqs((size_t)count);
-    for (int32_t i = 0; i < count; i++) {
-        Req* r = new Req();
-        reqs[(size_t)i] = r;
-        memset(&r->info, 0, sizeof(r->info));
-        r->info.tenant = tenants[i];
-        r->info.changes = sizes[i];
-        r->info.arrival_us = t;
-        r->info.epoch = -1;
-        if (tn[(size_t)i] < 0) {
-            r->info.status = DSSSP_REFUSED;
-            snprintf(r->info.error, sizeof r->info.error, "no such tenant");
-        } else if (sizes[i] < 0 || (sizes[i] > 0 && !batches[i])) {
-            r->info.status = DSSSP_E_INVAL;
-            snprintf(r->info.error, sizeof r->info.error, "bad batch");
-        } else {
-            const std::string why = check_batch(batches[i], sizes[i], tn[(size_t)i]);
-            if (!why.empty()) {
-                r->info.status = why.find("weight") != std::string::npos ? DSSSP_E_BAD_WEIGHT : DSSSP_E_BAD_VERTEX;
-                snprintf(r->info.error, sizeof r->info.error, "%s", why.c_str());
-            } else {
-                r->ch.assign(batches[i], batches[i] + sizes[i]);
-            }
+    int32_t a = 0;
+    while (a < count) {
+        int32_t b = a;
+        int64_t recs = 0;
+        while (b < count && b - a < 64 && (b == a || recs + (sizes[b] > 0 ? sizes[b] : 0) <= (1 << 20))) {
+            recs += sizes[b] > 0 ? sizes[b] : 0;
+            b++;
         }
-    }
-    {
-        std::lock_guard<std::mutex> lk(s->mu);
-        for (int32_t i = 0; i < count; i++) {
-            Req* r = reqs[(size_t)i];
-            r->info.id = s->next_id++;
-            ids[i] = r->info.id;
-            if (r->info.status == 0) {
-                TenantRec& tr = s->tenants[(size_t)r->info.tenant];
-                if (tr.state != kAdmitted) {
-                    r->info.status = DSSSP_REFUSED;
-                    snprintf(r->info.error, sizeof r->info.error, "%s",
-                             tr.state == kWaiting ? "tenant not admitted (waiting for memory)" : "tenant removed");
-                    std::vector<dsssp_change>().swap(r->ch);
+        std::vector<Req*> reqs;
+        reqs.reserve((size_t)(b - a));
+        for (int32_t i = a; i < b; i++) {
+            Req* r = new Req();
+            reqs.push_back(r);
+            memset(&r->info, 0, sizeof(r->info));
+            r->info.tenant = tenants[i];
+            r->info.changes = sizes[i];
+            r->info.arrival_us = t;
+            r->info.epoch = -1;
+            if (tn[(size_t)i] < 0) {
+                r->info.status = DSSSP_REFUSED;
+                snprintf(r->info.error, sizeof r->info.error, "no such tenant");
+            } else if (sizes[i] < 0 || (sizes[i] > 0 && !batches[i])) {
+                r->info.status = DSSSP_E_INVAL;
+                snprintf(r->info.error, sizeof r->info.error, "bad batch");
+            } else {
+                const std::string why = check_batch(batches[i], sizes[i], tn[(size_t)i]);
+                if (!why.empty()) {
+                    r->info.status = why.find("weight") != std::string::npos ? DSSSP_E_BAD_WEIGHT : DSSSP_E_BAD_VERTEX;
+                    snprintf(r->info.error, sizeof r->info.error, "%s", why.c_str());
+                } else {
+                    r->ch.assign(batches[i], batches[i] + sizes[i]);
                 }
             }
-            if (r->info.status == 0) {
-                s->tenants[(size_t)r->info.tenant].queue.push_back(r);
-                s->pending++;
-            } else {
-                r->info.start_us = r->info.done_us = t;
-                s->complete(r);
+        }
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            for (int32_t i = a; i < b; i++) {
+                Req* r = reqs[(size_t)(i - a)];
+                r->info.id = s->next_id++;
+                ids[i] = r->info.id;
+                if (r->info.status == 0) {
+                    TenantRec& tr = s->tenants[(size_t)r->info.tenant];
+                    if (tr.state != kAdmitted) {
+                        r->info.status = DSSSP_REFUSED;
+                        snprintf(r->info.error, sizeof r->info.error, "%s",
+                                 tr.state == kWaiting ? "tenant not admitted (waiting for memory)" : "tenant removed");
+                        std::vector<dsssp_change>().swap(r->ch);
+                    }
+                }
+                if (r->info.status == 0) {
+                    s->tenants[(size_t)r->info.tenant].queue.push_back(r);
+                    s->pending++;
+                } else {
+                    r->info.start_us = r->info.done_us = t;
+                    s->complete(r);
+                }
             }
         }
+        s->cv_work.notify_one();
+        a = b;
     }
-    s->cv_work.notify_one();
     return DSSSP_OK;
 }
 
@@ -873,7 +952,7 @@ int dsssp_server_result(dsssp_server* s, int64_t id, int32_t* parent, int64_t* d
 
 int dsssp_server_tree_read(dsssp_server* s, int32_t tenant, int32_t* parent, int64_t* dist) {
     if (!s) return fail(DSSSP_E_INVAL, "server_tree_read: NULL server");
-    std::lock_guard<std::mutex> d(s->dev);
+    DevLock d(s);
     const int32_t gi = dsssp_server_slot(s, tenant);
     if (gi < 0) return fail(DSSSP_E_INVAL, "server_tree_read: tenant %d is not served", tenant);
     return dsssp_pool_tree_read(s->pool, gi, parent, dist);
@@ -901,7 +980,7 @@ dsssp_pool* dsssp_server_pool(dsssp_server* s) { return s ? s->pool : nullptr; }
 
 int dsssp_server_validate(dsssp_server* s, int64_t* violations, int64_t* roots) {
     if (!s || !violations) return fail(DSSSP_E_INVAL, "server_validate: bad arguments");
-    std::lock_guard<std::mutex> d(s->dev);
+    DevLock d(s);
     return dsssp_tree_validate(s->pool->g, violations, roots, nullptr);
 }
 
@@ -917,7 +996,7 @@ int dsssp_server_set_record(dsssp_server* s, int32_t on) {
 
 int dsssp_server_debug_set(dsssp_server* s, int32_t what, int64_t value) {
     if (!s) return fail(DSSSP_E_INVAL, "server_debug_set: NULL server");
-    std::lock_guard<std::mutex> d(s->dev);  // between epochs
+    DevLock d(s);  // between epochs
     return dsssp_debug_set(s->pool->g, what, value);
 }
 

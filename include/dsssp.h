@@ -237,6 +237,12 @@ int dsssp_tree_read_changed(dsssp_graph* g, int32_t* vertex, int32_t* parent, in
 int dsssp_apply_batch(dsssp_graph* g, const dsssp_change* changes, int64_t k, void* stream,
                       dsssp_stats* st);
 
+/* Asynchronous form of dsssp_apply_batch: enqueues the copy of the k host records and the
+ * update on stream and returns without waiting; dsssp_batch_finish() waits and reports.  The
+ * records must stay unchanged until then (the copy runs on the stream; pinned memory makes it
+ * truly asynchronous), so the caller can prepare its next batch meanwhile. */
+int dsssp_apply_batch_host_async(dsssp_graph* g, const dsssp_change* changes, int64_t k, void* stream);
+
 /* Asynchronous form for callers that keep the batch on the device: enqueues the update
  * of k records at device address d_changes on stream and returns without waiting.
  * dsssp_batch_finish() waits, handles a slack overflow and reports the status. */
