@@ -58,6 +58,10 @@ class Opts(C.Structure):
         ("delta", C.c_int32),
         ("launch_graph", C.c_int32),
         ("recover", C.c_int32),
+        ("warp_agg", C.c_int32),
+        ("solo_waves", C.c_int32),
+        ("auto_rounds", C.c_int32),
+        ("reserved2", C.c_int32),
     ]
 
 

@@ -182,6 +182,8 @@ struct UpdParams {
     const int* srcs;  // mode 1: the sources (every root is its own parent)
     int nsrc;
     long long max_rounds;
+    unsigned solo_waves;  // steps of at most this many CTA-waves of items run on CTA 0 alone
+    int warp_agg;         // 1 = warp-aggregated distance offers (one atomicMin per target and warp)
 };
 
 // ---- memory-order helpers -------------------------------------------------------------

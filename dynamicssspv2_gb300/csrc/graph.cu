@@ -28,6 +28,7 @@ cudaError_t launch_front(const UpdParams& p, int grid, cudaStream_t s, cudaEvent
 cudaError_t update_occupancy(int block, int* blocks_per_sm);
 cudaError_t launch_update(const UpdParams& p, int grid, int block, cudaStream_t s);
 void batch_kernels(const void* fns[4]);
+const void* update_kernel(bool warp_agg);
 
 static std::atomic<long long> g_launches{0};
 void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
@@ -576,6 +577,7 @@ struct dsssp_graph {
     cudaGraphExec_t bexec = nullptr;
     cudaGraphNode_t bn_hash = nullptr, bn_kern[4] = {nullptr, nullptr, nullptr, nullptr};
     int bgraph_timing = 0;  // the timing level the instantiated graph records
+    int bgraph_agg = 0;     // the update kernel it launches (opts.warp_agg)
     bool bgraph_failed = false;
     // pending batch
     bool pending = false;
@@ -652,12 +654,11 @@ int ensure_far(dsssp_graph* g) {
 
 // Near-far bucket width of the next batch or tree computation.  delta > 0 is used as given;
 // delta < 0 (automatic) turns near-far rounds on with 32 times the mean edge weight once the
-// last batch or tree computation needed more than kAutoRounds rounds (a high-diameter graph);
+// last batch or tree computation needed more than opts.auto_rounds rounds (a high-diameter graph);
 // 0 keeps plain rounds.
-constexpr long long kAutoRounds = 256;
 unsigned long long effective_delta(const dsssp_graph* g) {
     if (g->o.delta > 0) return (unsigned long long)g->o.delta;
-    if (g->o.delta < 0 && g->last_rounds > kAutoRounds) {
+    if (g->o.delta < 0 && g->last_rounds > (long long)g->o.auto_rounds) {
         // wide buckets: a round costs a dependent chain and a grid barrier whatever its size,
         // so fewer rounds beat fewer relaxations (the 4096^2 grid: 103 ms at 8x, 87 ms at 32x,
         // 83 ms at 64-96x with 4-6x the relaxations)
@@ -902,6 +903,8 @@ UpdParams make_params(const dsssp_graph* g, const int4* chg, long long k, int mo
     p.srcs = g->d_srcs;
     p.nsrc = 0;
     p.max_rounds = g->o.max_rounds > 0 ? g->o.max_rounds : 2LL * g->n + 16;
+    p.solo_waves = (unsigned)g->o.solo_waves;
+    p.warp_agg = g->o.warp_agg;
     return p;
 }
 
@@ -1090,6 +1093,7 @@ struct BatchNodes {
 void batch_nodes(const dsssp_graph* g, const UpdParams& p, unsigned long long h, BatchNodes& b) {
     const void* fns[4];
     batch_kernels(fns);
+    fns[3] = update_kernel(p.warp_agg != 0);
     b.p = p;
     b.args[0] = &b.p;
     const long long need = (p.k + 255) / 256;
@@ -1177,6 +1181,7 @@ cudaError_t build_batch_graph(dsssp_graph* g, const BatchNodes& b, int timing) {
         cudaGetLastError();
     }
     g->bgraph_timing = timing;
+    g->bgraph_agg = b.p.warp_agg;
     return e;
 }
 
@@ -1187,7 +1192,7 @@ bool launch_batch_graph(dsssp_graph* g, const UpdParams& p, unsigned long long h
     batch_nodes(g, p, h, b);
     const int timing = g->o.timing;
     cudaError_t e = cudaSuccess;
-    if (!g->bexec || g->bgraph_timing != timing) {
+    if (!g->bexec || g->bgraph_timing != timing || g->bgraph_agg != p.warp_agg) {
         e = build_batch_graph(g, b, timing);
     } else {
         e = cudaGraphExecMemsetNodeSetParams(g->bexec, g->bn_hash, &b.hash);
@@ -1362,6 +1367,10 @@ void dsssp_default_opts(dsssp_opts* o) {
     o->delta = -1;
     o->launch_graph = 1;
     o->recover = 1;
+    o->warp_agg = 0;
+    o->solo_waves = 2;
+    o->auto_rounds = 256;
+    o->reserved2 = 0;
 }
 
 const char* dsssp_strerror(int code) {
@@ -1426,7 +1435,8 @@ static int check_opts(const dsssp_opts& o) {
         o.large_deg < o.small_deg || o.chunk < 32 ||
         o.bfs_levels < 0 || o.block < 32 || o.block > 256 || o.block % 32 || o.ctas_per_sm < 0 || o.max_rounds < 0 ||
         o.spare_pct < 0 || o.spare_pct > 400 || o.delta < -1 || o.timing < 0 || o.timing > 2 || o.recover < 0 ||
-        o.recover > 1)
+        o.recover > 1 || o.warp_agg < 0 || o.warp_agg > 1 || o.solo_waves < 0 || o.solo_waves > 64 ||
+        o.auto_rounds < 0)
         return fail(DSSSP_E_INVAL, "invalid dsssp_opts");
     return DSSSP_OK;
 }

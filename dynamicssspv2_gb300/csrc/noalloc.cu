@@ -196,6 +196,7 @@ extern "C" int dsssp_sssp_noalloc(int32_t n, int64_t nnz, const int64_t* d_row_o
     p.srcs = reinterpret_cast<const int*>(base + kOffSrc);
     p.nsrc = 1;
     p.max_rounds = 2LL * n + 16;
+    p.solo_waves = 2;
     e = launch_update(p, ds->grid, kBlock, s);
     if (e != cudaSuccess) return fail(DSSSP_E_CUDA, "sssp_noalloc: update kernel: %s", cudaGetErrorString(e));
     const unsigned ob = (unsigned)((n + kBlock - 1) / kBlock < 1024 ? (n + kBlock - 1) / kBlock : 1024);

@@ -53,8 +53,6 @@ constexpr int kAddsPerCheck = 32;          // entries a warp may add between two
                                            // (one add of up to 32 lanes; visit4 reserves room
                                            // for its four adds instead)
 static_assert(kBuf > kAddsPerCheck, "a push buffer must take one visit's adds after a check");
-constexpr unsigned kSoloWaves = 2;         // a step of at most this many CTA-waves of items
-                                           // runs on CTA 0 alone (block barriers)
 constexpr int kSoloSteps = 256;            // consecutive solo steps before the grid re-syncs
 
 __shared__ unsigned s_nbar;        // grid barriers this CTA has passed
@@ -381,9 +379,29 @@ __device__ __forceinline__ void far_append4(const UpdParams& p, const Far& f, co
         if (pred[q]) f.list[at++] = c[q];
 }
 
+// Warp-aggregated offers: lanes offering to the same vertex c (offer set) are grouped with
+// __match_any_sync; the group's least candidate word goes to its lowest lane (lead), the only
+// one that issues the atomicMin, so a vertex offered by several lanes of a warp takes one
+// atomic instead of one per lane.  Warp-collective; the loop runs (largest group - 1) times.
+__device__ __forceinline__ void warp_agg_min(bool offer, unsigned c, unsigned long long& best, bool& lead) {
+    const unsigned lane = lane_id();
+    if (!__any_sync(kFull, offer)) return;
+    // lanes without an offer get keys no vertex id takes (ids are below 2^31)
+    const unsigned grp = __match_any_sync(kFull, offer ? c : 0x80000000u | lane);
+    unsigned rem = grp & ~(1u << lane);
+    while (__any_sync(kFull, rem != 0)) {
+        const int src = rem ? __ffs(rem) - 1 : (int)lane;
+        const unsigned long long o = __shfl_sync(kFull, best, src);
+        best = o < best ? o : best;
+        rem &= rem - 1;
+    }
+    lead = offer && (__ffs(grp) - 1) == (int)lane;
+}
+
 // ---- per-edge operations ---------------------------------------------------------------
 // visit4 handles up to four adjacency entries per lane and is called by all 32 lanes.
 
+template <bool kAgg>
 struct RelaxOp {
     const UpdParams* p;
     unsigned tag;
@@ -418,31 +436,64 @@ struct RelaxOp {
         // adjacency loads above were issued alongside the load of du (an unreachable u offers
         // nothing).
         const bool live = du < kDistInf;
-        unsigned long long old[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const unsigned long long nd = du + (unsigned)e[q].y;
-            const bool offer = live && e[q].y > 0 && nd < kDistInf && ((nd << 32) | u) < cur[q];
-            if (live && e[q].y > 0 && nd >= kDistInf &&
-                (direct ? __ldcg(&state[e[q].x]) : cur[q]) == kInfState)
-                ls->dist_ovf++;
-            old[q] = offer ? atomicMin(&state[e[q].x], (nd << 32) | u) : 0ull;
-        }
         bool push[4], later[4];
+        if constexpr (!kAgg) {
+            unsigned long long old[4];
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const unsigned long long nd = du + (unsigned)e[q].y;
-            const unsigned long long cand = (nd << 32) | u;
-            push[q] = false;
-            if (live && e[q].y > 0 && nd < kDistInf && cand < cur[q]) {
-                push[q] = (old[q] >> 32) > nd;
-                if (push[q]) ls->updates++;
-                else if (old[q] > cand && p->g.chg_tag) p->g.chg_tag[e[q].x] = p->epoch;
-            } else if (live && e[q].y == 0) {  // zero weight: strict improvements only (compare-and-swap)
-                push[q] = relax_to(p->g, p->epoch, (unsigned)e[q].x, nd, u, 0,
-                                   direct ? __ldcg(&state[e[q].x]) : cur[q], *ls);
+            for (int q = 0; q < 4; q++) {
+                const unsigned long long nd = du + (unsigned)e[q].y;
+                const bool offer = live && e[q].y > 0 && nd < kDistInf && ((nd << 32) | u) < cur[q];
+                if (live && e[q].y > 0 && nd >= kDistInf &&
+                    (direct ? __ldcg(&state[e[q].x]) : cur[q]) == kInfState)
+                    ls->dist_ovf++;
+                old[q] = offer ? atomicMin(&state[e[q].x], (nd << 32) | u) : 0ull;
             }
-            later[q] = push[q] && nd >= far.T;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const unsigned long long nd = du + (unsigned)e[q].y;
+                const unsigned long long cand = (nd << 32) | u;
+                push[q] = false;
+                if (live && e[q].y > 0 && nd < kDistInf && cand < cur[q]) {
+                    push[q] = (old[q] >> 32) > nd;
+                    if (push[q]) ls->updates++;
+                    else if (old[q] > cand && p->g.chg_tag) p->g.chg_tag[e[q].x] = p->epoch;
+                } else if (live && e[q].y == 0) {  // zero weight: strict improvements only (compare-and-swap)
+                    push[q] = relax_to(p->g, p->epoch, (unsigned)e[q].x, nd, u, 0,
+                                       direct ? __ldcg(&state[e[q].x]) : cur[q], *ls);
+                }
+                later[q] = push[q] && nd >= far.T;
+            }
+        } else {
+            // the lanes' offers to one vertex are reduced in the warp first: only the group's
+            // least candidate word is issued, by the group's lowest lane
+            unsigned long long old[4], best[4];
+            bool lead[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const unsigned long long nd = du + (unsigned)e[q].y;
+                const bool offer = live && e[q].y > 0 && nd < kDistInf && ((nd << 32) | u) < cur[q];
+                if (live && e[q].y > 0 && nd >= kDistInf &&
+                    (direct ? __ldcg(&state[e[q].x]) : cur[q]) == kInfState)
+                    ls->dist_ovf++;
+                best[q] = offer ? (nd << 32) | u : kInfState;
+                lead[q] = offer;
+                warp_agg_min(offer, (unsigned)e[q].x, best[q], lead[q]);
+                old[q] = lead[q] ? atomicMin(&state[e[q].x], best[q]) : 0ull;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const unsigned long long nd = best[q] >> 32;  // the group's least distance
+                push[q] = false;
+                if (lead[q]) {
+                    push[q] = (old[q] >> 32) > nd;
+                    if (push[q]) ls->updates++;
+                    else if (old[q] > best[q] && p->g.chg_tag) p->g.chg_tag[e[q].x] = p->epoch;
+                } else if (live && e[q].y == 0) {  // zero weight: strict improvements only (compare-and-swap)
+                    push[q] = relax_to(p->g, p->epoch, (unsigned)e[q].x, du, u, 0,
+                                       direct ? __ldcg(&state[e[q].x]) : cur[q], *ls);
+                }
+                later[q] = push[q] && (e[q].y == 0 ? du : nd) >= far.T;
+            }
         }
         unsigned ftag[4], ctag[4];
         RowDesc rd[4];
@@ -606,11 +657,11 @@ struct PullOp {
     }
 };
 
-// A step of nt thread items and nc CTA items is small when CTA 0 alone finishes it in a few
-// waves: then it skips the grid barrier, whose cost (~2.5 us plus the wait for the slowest
-// CTA) exceeds the work.
-__device__ __forceinline__ bool small_step(unsigned nt, unsigned nc) {
-    return (nt + blockDim.x - 1) / blockDim.x + nc <= kSoloWaves;
+// A step of nt thread items and nc CTA items is small when CTA 0 alone finishes it in at most
+// `solo` waves (opts.solo_waves, default 2): then it skips the grid barrier, whose cost (~2.5 us
+// plus the wait for the slowest CTA) exceeds the work.  solo 0: every step runs on the grid.
+__device__ __forceinline__ bool small_step(unsigned nt, unsigned nc, unsigned solo) {
+    return solo > 0 && (nt + blockDim.x - 1) / blockDim.x + nc <= solo;
 }
 
 // Processes one step's work on ncta CTAs (the whole grid, or CTA 0 alone for a small step;
@@ -1021,12 +1072,16 @@ __global__ void k_append(UpdParams p) {
     if (lane_id() == 0 && kk) atomicAdd(&ctl->killed, (unsigned)kk);
 }
 
+template <bool kAgg>
 __device__ void update_body(UpdParams& p);
 
 // 3 CTAs of 256 threads per SM: 80 registers a thread without spills.  Every walk level and
 // relaxation round waits on its slowest CTA's chain of dependent accesses, so shorter chains
 // and fewer CTAs at each barrier beat more resident warps here (4 CTAs per SM with 64
 // registers and spills was slower on every workload but the throughput-bound 256-graph batch).
+// kAgg: warp-aggregated distance offers (opts.warp_agg), compiled as its own kernel so that
+// the default kernel keeps its register allocation.
+template <bool kAgg>
 __global__ void __launch_bounds__(256, 3) k_update(UpdParams p) {
     if (threadIdx.x == 0) {
         s_nbar = 0;
@@ -1035,7 +1090,7 @@ __global__ void __launch_bounds__(256, 3) k_update(UpdParams p) {
         s_spin_limit = lim ? lim : kSpinLimit;
     }
     __syncthreads();
-    update_body(p);
+    update_body<kAgg>(p);
     __syncthreads();
     if (threadIdx.x == 0) {
         atomicMax(&p.g.ctl->diag[3], s_nbar);
@@ -1043,6 +1098,7 @@ __global__ void __launch_bounds__(256, 3) k_update(UpdParams p) {
     }
 }
 
+template <bool kAgg>
 __device__ void update_body(UpdParams& p) {
     Ctl* ctl = p.g.ctl;
     DevGraph& g = p.g;
@@ -1133,13 +1189,13 @@ __device__ void update_body(UpdParams& p) {
                 need_pj = true;
                 break;
             }
-            if (small_step(hiT - loT, hiC - loC)) {
+            if (small_step(hiT - loT, hiC - loC, p.solo_waves)) {
                 // small levels: CTA 0 walks on alone while they stay small; the others wait
                 if (blockIdx.x == 0) {
                     if (threadIdx.x < 6) s_solo_cnt[threadIdx.x / 2][threadIdx.x % 2] = 0;
                     __syncthreads();
                     for (int steps = 0; steps < kSoloSteps; steps++) {
-                        if ((loT >= hiT && loC >= hiC) || level >= p.bfs_levels || !small_step(hiT - loT, hiC - loC))
+                        if ((loT >= hiT && loC >= hiC) || level >= p.bfs_levels || !small_step(hiT - loT, hiC - loC, p.solo_waves))
                             break;
                         unsigned* cnt = s_solo_cnt[(level + 1) % 3];
                         if (threadIdx.x == 0) {
@@ -1326,7 +1382,7 @@ __device__ void update_body(UpdParams& p) {
             if (leader) set_status(ctl, -5 /* NO_CONVERGENCE */);
             break;
         }
-        if (small_step(nT, nC)) {
+        if (small_step(nT, nC, p.solo_waves)) {
             // small rounds: CTA 0 relaxes on alone while they stay small; the others wait.  An
             // empty frontier goes back to the grid (near-far advance or the end).
             if (blockIdx.x == 0) {
@@ -1335,14 +1391,14 @@ __device__ void update_body(UpdParams& p) {
                 if (threadIdx.x < 6) s_solo_cnt[threadIdx.x / 2][threadIdx.x % 2] = 0;
                 __syncthreads();
                 for (int steps = 0; steps < kSoloSteps; steps++) {
-                    if ((t == 0 && c == 0) || !small_step(t, c) || rr >= p.max_rounds) break;
+                    if ((t == 0 && c == 0) || !small_step(t, c, p.solo_waves) || rr >= p.max_rounds) break;
                     unsigned* cnt = s_solo_cnt[(rr + 1) % 3];
                     if (threadIdx.x == 0) {
                         s_solo_cnt[(rr + 2) % 3][0] = 0;
                         s_solo_cnt[(rr + 2) % 3][1] = 0;
                     }
                     const bool odd = (rr & 1) != 0;
-                    RelaxOp op{&p, rbase + (unsigned)rr + 2u,
+                    RelaxOp<kAgg> op{&p, rbase + (unsigned)rr + 2u,
                                Out{odd ? g.rt0 : g.rt1, &cnt[0], g.tcap, odd ? g.rc0 : g.rc1, &cnt[1], g.ccap},
                                PushBuf{pbuf, 0}, &ls, far_of(cf, fgen, T), true};
                     run_items(op, p, odd ? g.rt1 : g.rt0, t, odd ? g.rc1 : g.rc0, c, 0, 1);
@@ -1371,7 +1427,7 @@ __device__ void update_body(UpdParams& p) {
             ctl->rcC[(r + 2) % 3] = 0;
         }
         const bool odd = (r & 1) != 0;
-        RelaxOp op{&p, rbase + (unsigned)r + 2u,
+        RelaxOp<kAgg> op{&p, rbase + (unsigned)r + 2u,
                    Out{odd ? g.rt0 : g.rt1, &ctl->rcT[(r + 1) % 3], g.tcap, odd ? g.rc0 : g.rc1,
                        &ctl->rcC[(r + 1) % 3], g.ccap},
                    PushBuf{pbuf, 0}, &ls, far_of(cf, fgen, T),
@@ -1415,18 +1471,26 @@ void batch_kernels(const void* fns[4]) {
     fns[0] = (const void*)k_prepare;
     fns[1] = (const void*)k_delete;
     fns[2] = (const void*)k_append;
-    fns[3] = (const void*)k_update;
+    fns[3] = (const void*)k_update<false>;
+}
+
+const void* update_kernel(bool warp_agg) {
+    return warp_agg ? (const void*)k_update<true> : (const void*)k_update<false>;
 }
 
 cudaError_t update_occupancy(int block, int* blocks_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_update, block, 0);
+    int a = 0, b = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_update<false>, block, 0);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_update<true>, block, 0);
+    *blocks_per_sm = a < b ? a : b;
+    return e;
 }
 
 cudaError_t launch_update(const UpdParams& p, int grid, int block, cudaStream_t s) {
     UpdParams copy = p;
     void* args[] = {&copy};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_update, dim3((unsigned)grid), dim3((unsigned)block),
-                                                args, 0, s);
+    cudaError_t e = cudaLaunchCooperativeKernel(update_kernel(p.warp_agg != 0), dim3((unsigned)grid),
+                                                dim3((unsigned)block), args, 0, s);
     count_launch(1);
     return e;
 }

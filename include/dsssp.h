@@ -84,8 +84,8 @@ typedef struct {
                              T moves to (least waiting distance) + delta.  Same results; far
                              fewer rounds and relaxations on high-diameter graphs.  -1 (the
                              default) = automatic: near-far with 32 x the mean edge weight once
-                             the last batch or tree computation needed more than 256 rounds,
-                             plain rounds otherwise.  Costs 12 bytes per vertex, allocated when
+                             the last batch or tree computation needed more than auto_rounds
+                             rounds, plain rounds otherwise.  Costs 12 bytes per vertex, allocated when
                              first used. */
     int32_t launch_graph; /* 1 = a batch's launch sequence (control-block reset, deletion-set
                              reset, the four kernels, the status read) is replayed from an
@@ -97,6 +97,16 @@ typedef struct {
                              DSSSP_W_RECOMPUTED (or, if that fails too, the error, and the tree
                              must be loaded or computed before the next batch); 0 = return the
                              error and leave the tree as the kernel left it (unfinished) */
+    int32_t warp_agg;     /* 1 = warp-aggregated distance offers: lanes of a warp offering to the
+                             same vertex are grouped (__match_any_sync) and only the least offer
+                             is issued as a 64-bit atomicMin; 0 (the default) = one atomicMin per
+                             improving offer.  Same results either way. */
+    int32_t solo_waves;   /* a walk level or relaxation round with at most this many CTA-waves of
+                             work items runs on one CTA with block barriers instead of the whole
+                             grid (0..64; 0 = never; default 2) */
+    int32_t auto_rounds;  /* delta = -1: near-far rounds start once the last batch or tree
+                             computation needed more than this many rounds (default 256) */
+    int32_t reserved2;
 } dsssp_opts;
 
 /* Counters of one batch (or one tree computation), read back from the device. */

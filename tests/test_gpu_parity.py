@@ -91,6 +91,10 @@ OPTION_SETS = [
     {"timing": 2},                                         # events between the front kernels
     {"timing": 2, "launch_graph": 0},
     {"timing": 0},                                         # no events, no timestamps
+    {"warp_agg": 1},                                       # warp-aggregated offers
+    {"warp_agg": 1, "delta": 25, "small_deg": 64, "large_deg": 1 << 20},
+    {"solo_waves": 0},                                     # every step on the whole grid
+    {"solo_waves": 16},                                    # long stretches on CTA 0
 ]
 
 
@@ -134,7 +138,7 @@ def test_zero_weights_multiedges_selfloops():
     ch = D.make_changes(np.concatenate([u[idx], ins_u]), np.concatenate([v[idx], ins_v]),
                         np.concatenate([w[idx], rng.integers(0, 3, 200)]), np.concatenate([np.zeros(300), np.ones(200)]))
     ch = ch[rng.permutation(len(ch))]
-    for opts in ({}, {"bfs_levels": 0}, {"delta": 1}, {"delta": 2, "bfs_levels": 0}):
+    for opts in ({}, {"bfs_levels": 0}, {"delta": 1}, {"delta": 2, "bfs_levels": 0}, {"warp_agg": 1}):
         p, d, _ = run_engine(n, u, v, w, ch, parent, dist, **opts)
         check_against_oracle(n, u, v, w, ch, 0, p, d, f"zero weights {opts}")
 
