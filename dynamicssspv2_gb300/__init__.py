@@ -61,7 +61,8 @@ class Opts(C.Structure):
         ("warp_agg", C.c_int32),
         ("solo_waves", C.c_int32),
         ("auto_rounds", C.c_int32),
-        ("reserved2", C.c_int32),
+        ("group_ctas", C.c_int32),
+        ("group_waves", C.c_int32),
     ]
 
 

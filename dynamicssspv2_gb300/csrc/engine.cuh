@@ -83,7 +83,8 @@ struct __align__(128) Ctl {
     unsigned round_base;
     unsigned spin_limit;  // grid-barrier poll limit (0 = default); persistent, set by the host
     unsigned stall_us;    // test hook: the last CTA of k_update waits this long before its first barrier
-    unsigned pad0[28];
+    unsigned grp_gen;     // generation of the group barrier (the first group_ctas CTAs)
+    unsigned pad0[27];
     // line 1
     int status;
     int ovf_count;
@@ -94,6 +95,9 @@ struct __align__(128) Ctl {
     // line 2
     unsigned bar_count;
     unsigned pad2[31];
+    // line 2b: arrivals at the group barrier (its own line: the grid's CTAs poll bar_gen meanwhile)
+    unsigned grp_count;
+    unsigned pad2b[31];
     // line 3: relaxation lists, round r reads slot r%3
     unsigned rcT[3];
     unsigned rcC[3];
@@ -183,6 +187,8 @@ struct UpdParams {
     int nsrc;
     long long max_rounds;
     unsigned solo_waves;  // steps of at most this many CTA-waves of items run on CTA 0 alone
+    unsigned group_ctas;  // mid-size steps run on CTAs [0, group_ctas) with a group barrier (0 = off)
+    unsigned group_waves; // ... a step is mid-size up to group_ctas * group_waves CTA-waves of items
     int warp_agg;         // 1 = warp-aggregated distance offers (one atomicMin per target and warp)
 };
 

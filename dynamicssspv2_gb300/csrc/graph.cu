@@ -904,6 +904,8 @@ UpdParams make_params(const dsssp_graph* g, const int4* chg, long long k, int mo
     p.nsrc = 0;
     p.max_rounds = g->o.max_rounds > 0 ? g->o.max_rounds : 2LL * g->n + 16;
     p.solo_waves = (unsigned)g->o.solo_waves;
+    p.group_ctas = (unsigned)g->o.group_ctas;
+    p.group_waves = (unsigned)g->o.group_waves;
     p.warp_agg = g->o.warp_agg;
     return p;
 }
@@ -1370,7 +1372,8 @@ void dsssp_default_opts(dsssp_opts* o) {
     o->warp_agg = 0;
     o->solo_waves = 2;
     o->auto_rounds = 256;
-    o->reserved2 = 0;
+    o->group_ctas = 0;
+    o->group_waves = 2;
 }
 
 const char* dsssp_strerror(int code) {
@@ -1436,7 +1439,7 @@ static int check_opts(const dsssp_opts& o) {
         o.bfs_levels < 0 || o.block < 32 || o.block > 256 || o.block % 32 || o.ctas_per_sm < 0 || o.max_rounds < 0 ||
         o.spare_pct < 0 || o.spare_pct > 400 || o.delta < -1 || o.timing < 0 || o.timing > 2 || o.recover < 0 ||
         o.recover > 1 || o.warp_agg < 0 || o.warp_agg > 1 || o.solo_waves < 0 || o.solo_waves > 64 ||
-        o.auto_rounds < 0)
+        o.auto_rounds < 0 || o.group_ctas < 0 || o.group_ctas > 1024 || o.group_waves < 1 || o.group_waves > 64)
         return fail(DSSSP_E_INVAL, "invalid dsssp_opts");
     return DSSSP_OK;
 }

@@ -57,6 +57,7 @@ constexpr int kSoloSteps = 256;            // consecutive solo steps before the 
 
 __shared__ unsigned s_nbar;        // grid barriers this CTA has passed
 __shared__ unsigned s_gen;         // barrier generation this CTA waits on next (ctl->bar_gen)
+__shared__ unsigned s_ggen;        // group-barrier generation this CTA waits on next (ctl->grp_gen)
 // List counters of solo steps (CTA 0 alone): (thread items, CTA items) per slot, slots used
 // like the control block's three rotating counters.  Shared-memory atomics and reads save a
 // global round trip each per step.
@@ -65,9 +66,11 @@ __shared__ unsigned s_spin_limit;  // polls before a grid barrier gives up
 __shared__ uint4 s_pbuf[kMaxWarps][kBuf];  // (vertex, degree, row start) pushed, not yet expanded
 __shared__ unsigned s_wlist[kMaxWarps][kListRegion];  // k_delete / k_append list staging
 
+// Per-thread counters (32 bits: a thread's share stays far below 2^32 in any run; the block
+// sums in flush_stats are 64-bit), few registers in the register-bound update kernel.
 struct LocalStats {
-    unsigned long long edges_relax = 0, edges_inv = 0, updates = 0, dist_ovf = 0, frontier = 0, items = 0,
-                       marked = 0, edges_pull = 0;
+    unsigned edges_relax = 0, edges_inv = 0, updates = 0, dist_ovf = 0, frontier = 0, items = 0, marked = 0,
+             edges_pull = 0;
 };
 
 // Grid-wide barrier for a cooperative launch.  The wait is bounded: on timeout the status
@@ -109,6 +112,48 @@ __device__ bool grid_sync(Ctl* ctl, const unsigned* a, const unsigned* b, unsign
         const int st = __ldcg(&ctl->status);
         s_va = a ? __ldcg(a) : 0u;
         s_vb = b ? __ldcg(b) : 0u;
+        s_go = st == 0;
+    }
+    __syncthreads();
+    va = s_va;
+    vb = s_vb;
+    return s_go != 0;
+}
+
+// Barrier of the first G CTAs (a group running mid-size steps while the others wait at the
+// next grid barrier): like grid_sync, bounded, with the counters the caller needs next read
+// once per CTA after the release.  Every CTA of the group calls it the same number of times.
+__device__ bool group_sync(Ctl* ctl, unsigned G, const unsigned* a, const unsigned* b, unsigned& va, unsigned& vb) {
+    __shared__ int s_go;
+    __shared__ unsigned s_va, s_vb;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned gen = s_ggen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(&ctl->grp_count, 1u);
+        if (arrived == G - 1) {
+            atomicExch(&ctl->grp_count, 0u);
+            __threadfence();
+            st_release(&ctl->grp_gen, gen + 1);
+        } else {
+            unsigned spins = 0;
+            while (ld_acquire(&ctl->grp_gen) == gen) {
+                if (++spins > s_spin_limit) {
+                    if (atomicCAS(&ctl->status, 0, -6 /* DSSSP_E_TIMEOUT */) == 0) {
+                        ctl->diag[0] = 0x80000000u | s_nbar;  // high bit: a group barrier
+                        ctl->diag[1] = atomicAdd(&ctl->grp_count, 0u);
+                    }
+                    atomicAdd(&ctl->diag[2], 1u);
+                    break;
+                }
+                if (spins > 32) __nanosleep(spins < 4096 ? 64 : 1000);
+            }
+        }
+        __threadfence();
+        s_ggen = gen + 1;
+        const int st = __ldcg(&ctl->status);
+        s_va = __ldcg(a);
+        s_vb = __ldcg(b);
         s_go = st == 0;
     }
     __syncthreads();
@@ -664,6 +709,15 @@ __device__ __forceinline__ bool small_step(unsigned nt, unsigned nc, unsigned so
     return solo > 0 && (nt + blockDim.x - 1) / blockDim.x + nc <= solo;
 }
 
+// A step is mid-size when the group (the first G CTAs) finishes it in at most p.group_waves
+// waves: it runs there with the group barrier, shorter than the grid's and waiting for the
+// slowest of G chains instead of all CTAs'.
+__device__ __forceinline__ bool group_step(const UpdParams& p, unsigned nt, unsigned nc) {
+    const unsigned G = p.group_ctas;
+    if (G < 2 || G >= gridDim.x || small_step(nt, nc, p.solo_waves)) return false;
+    return (unsigned long long)(nt + blockDim.x - 1) / blockDim.x + nc <= (unsigned long long)G * p.group_waves;
+}
+
 // Processes one step's work on ncta CTAs (the whole grid, or CTA 0 alone for a small step;
 // this CTA is number cta of them): CTA items first (one CTA per chunk of a long row; CTA
 // items cta, cta + ncta, ...), then thread items (te edges each) in one grid-stride wave over
@@ -1086,6 +1140,7 @@ __global__ void __launch_bounds__(256, 3) k_update(UpdParams p) {
     if (threadIdx.x == 0) {
         s_nbar = 0;
         s_gen = ld_acquire(&p.g.ctl->bar_gen);
+        s_ggen = ld_acquire(&p.g.ctl->grp_gen);
         const unsigned lim = __ldcg(&p.g.ctl->spin_limit);
         s_spin_limit = lim ? lim : kSpinLimit;
     }
@@ -1409,6 +1464,49 @@ __device__ void update_body(UpdParams& p) {
                     __syncthreads();  // every thread has read the counters before the next reset
                 }
                 if (threadIdx.x == 0) {
+                    ctl->solo[3] = (unsigned long long)rr;
+                    ctl->solo_n[0] = t;
+                    ctl->solo_n[1] = c;
+                    ctl->rcT[rr % 3] = t;  // round rr's lists (the near-far advance appends here when empty)
+                    ctl->rcC[rr % 3] = c;
+                    ctl->rcT[(rr + 1) % 3] = 0;  // the grid's round rr appends here
+                    ctl->rcC[(rr + 1) % 3] = 0;
+                }
+            }
+            if (!grid_sync(ctl, &ctl->solo_n[0], &ctl->solo_n[1], nT, nC)) break;
+            r = (long long)__ldcg(&ctl->solo[3]) - 1;  // the loop steps to the first round left
+            continue;
+        }
+        if (group_step(p, nT, nC)) {
+            // mid-size rounds: the group relaxes on with its own barrier while they stay
+            // mid-size (at most kSoloSteps); the others wait at the next grid barrier.  Lists and
+            // counters are the grid's, so the hand-over is the same as after solo rounds.
+            const unsigned G = p.group_ctas;
+            if (blockIdx.x < G) {
+                long long rr = r;
+                unsigned t = nT, c = nC;
+                for (int steps = 0; steps < kSoloSteps; steps++) {
+                    if ((t == 0 && c == 0) || !group_step(p, t, c) || rr >= p.max_rounds) break;
+                    if (blockIdx.x == 0 && threadIdx.x == 0) {
+                        ctl->rcT[(rr + 2) % 3] = 0;
+                        ctl->rcC[(rr + 2) % 3] = 0;
+                    }
+                    const bool odd = (rr & 1) != 0;
+                    RelaxOp<kAgg> op{&p, rbase + (unsigned)rr + 2u,
+                                     Out{odd ? g.rt0 : g.rt1, &ctl->rcT[(rr + 1) % 3], g.tcap, odd ? g.rc0 : g.rc1,
+                                         &ctl->rcC[(rr + 1) % 3], g.ccap},
+                                     PushBuf{pbuf, 0}, &ls, far_of(cf, fgen, T),
+                                     (unsigned long long)t + (unsigned long long)c * blockDim.x <=
+                                         (unsigned long long)G * blockDim.x};
+                    run_items(op, p, odd ? g.rt1 : g.rt0, t, odd ? g.rc1 : g.rc0, c, blockIdx.x, G);
+                    unsigned t2, c2;
+                    const bool go = group_sync(ctl, G, &ctl->rcT[(rr + 1) % 3], &ctl->rcC[(rr + 1) % 3], t2, c2);
+                    rr++;
+                    t = t2;
+                    c = c2;
+                    if (!go) break;
+                }
+                if (blockIdx.x == 0 && threadIdx.x == 0) {
                     ctl->solo[3] = (unsigned long long)rr;
                     ctl->solo_n[0] = t;
                     ctl->solo_n[1] = c;

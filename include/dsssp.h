@@ -106,7 +106,14 @@ typedef struct {
                              grid (0..64; 0 = never; default 2) */
     int32_t auto_rounds;  /* delta = -1: near-far rounds start once the last batch or tree
                              computation needed more than this many rounds (default 256) */
-    int32_t reserved2;
+    int32_t group_ctas;   /* a relaxation round too large for one CTA (solo_waves) but at most
+                             group_waves CTA-waves on group_ctas CTAs runs on the first group_ctas
+                             CTAs with a barrier of their own while the other CTAs wait: a shorter
+                             barrier and the slowest of group_ctas dependent chains instead of all
+                             CTAs' (high-diameter graphs run thousands of such rounds); 0 (the
+                             default) = off: measured slower, the rounds wait on their items'
+                             dependent chains more than on the barrier */
+    int32_t group_waves;  /* see group_ctas (1..64, default 2) */
 } dsssp_opts;
 
 /* Counters of one batch (or one tree computation), read back from the device. */

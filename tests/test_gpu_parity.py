@@ -95,6 +95,9 @@ OPTION_SETS = [
     {"warp_agg": 1, "delta": 25, "small_deg": 64, "large_deg": 1 << 20},
     {"solo_waves": 0},                                     # every step on the whole grid
     {"solo_waves": 16},                                    # long stretches on CTA 0
+    {"solo_waves": 0, "group_ctas": 4, "group_waves": 16},  # mid-size rounds on a group of 4 CTAs
+    {"solo_waves": 1, "group_ctas": 2, "group_waves": 64, "delta": 25},
+    {"group_ctas": 0},                                     # no group rounds
 ]
 
 
@@ -227,6 +230,9 @@ def test_near_far_same_tree_on_grid(delta):
     assert st0.n_invalidated > n // 4 and (d1 >= 0).all()
     if delta <= 40:
         assert st1.edges_relaxed < st0.edges_relaxed
+    # the same rounds on a group of CTAs with their own barrier (nothing solo) give the same tree
+    p2, d2, _ = run_engine(n, u, v, w, ch, parent, dist, delta=delta, solo_waves=0, group_ctas=8, group_waves=64)
+    assert np.array_equal(d1, d2) and np.array_equal(p1, p2)
 
 
 @pytest.mark.parametrize("delta", [0, 16])
