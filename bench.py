@@ -584,7 +584,7 @@ def batching_summary(workload: str, steps: int, warmup: int, dist: Dist) -> dict
     pool.tree_compute([0] * len(items))
     union = pool.union_batch([(i, it[4]) for i, it in enumerate(items)])
     d_union = torch.from_numpy(union.view(np.int32).reshape(-1)).to(f"cuda:{dev}")
-    cache = os.environ.get("DSSSP_AUTOTUNE_CACHE") or os.path.join(tempfile.gettempdir(), "dsssp_autotune.json")
+    cache = os.environ.get("DSSSP_AUTOTUNE_CACHE") or os.path.join(tempfile.gettempdir(), "dsssp_autotune.txt")
     tuned = Autotuner(cache).tune(pool.graph, union)
     pool.graph.snapshot()
 

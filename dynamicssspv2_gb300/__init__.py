@@ -128,6 +128,7 @@ class ServerOpts(C.Structure):
         ("compact_dead_frac", C.c_double),
         ("compact_spare_frac", C.c_double),
         ("reserve_vertices", C.c_int64),
+        ("tune_cache", C.c_char_p),
     ]
 
 
@@ -248,6 +249,7 @@ EXPORTED = [
     "dsssp_pool_create_reserved", "dsssp_pool_add_graph", "dsssp_pool_remove_graph", "dsssp_pool_graph_range",
     "dsssp_pool_capacity", "dsssp_server_tenant_state", "dsssp_server_add_tenant", "dsssp_server_remove_tenant",
     "dsssp_server_recovered_epochs", "dsssp_server_debug_set", "dsssp_apply_batch_host_async",
+    "dsssp_autotune", "dsssp_autotune_lookup", "dsssp_tune_size_class", "dsssp_tune_candidates",
 ]
 
 

@@ -30,7 +30,7 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-Wno-unused-function"]
 
 CUDA_UNITS = ["update.cu", "graph.cu", "noalloc.cu"]
-HOST_UNITS = ["gen.cpp", "textio.cpp", "binio.cpp", "serve.cpp"]
+HOST_UNITS = ["gen.cpp", "textio.cpp", "binio.cpp", "serve.cpp", "autotune.cpp"]
 HEADERS = ["engine.cuh", "host_common.h"]
 
 

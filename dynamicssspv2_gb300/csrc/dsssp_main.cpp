@@ -1,11 +1,13 @@
 // dsssp_main.cpp -- drop-in command line for SSSPmainForUndirected.cu (README.md:13-18):
 //
 //   dsssp_main <graph> <N> <M> <SSSP> <changes> [--out FILE] [--json FILE] [--device D]
-//              [--delta W] [--cache]
+//              [--delta W] [--cache] [--autotune CACHE]
 //
 // --cache keeps a binary image of the graph and of the SSSP file next to them (<file>.dsssp.bin,
 // include/dsssp.h binary cache) and reads it instead of the text when it is at least as new as
-// the text; --delta sets the near-far bucket width of the relaxation rounds.
+// the text; --delta sets the near-far bucket width of the relaxation rounds; --autotune takes
+// the settings that the autotuner cache CACHE holds for this size class, or tunes them on the
+// batch (on snapshots of the graph) and adds them to CACHE, before the batch is applied.
 //
 // Reads the three text formats, builds the device graph, loads the tree, applies the change
 // batch through the C ABI and prints the reference's stdout lines (SSSPmainForUndirected.cu:
@@ -58,13 +60,14 @@ int main(int argc, char** argv) {
     if (argc < 6) {
         fprintf(stderr,
                 "usage: %s <graph> <number_of_nodes> <number_of_edges> <SSSP> <change_edges> "
-                "[--out FILE] [--json FILE] [--device D] [--delta W] [--cache]\n",
+                "[--out FILE] [--json FILE] [--device D] [--delta W] [--cache] [--autotune CACHE]\n",
                 argv[0]);
         return 2;
     }
     const char* out_path = nullptr;
     const char* json_path = nullptr;
     bool use_cache = false;
+    const char* tune_path = nullptr;
     dsssp_opts opts;
     dsssp_default_opts(&opts);
     long long val = 0;
@@ -75,6 +78,7 @@ int main(int argc, char** argv) {
         else if (!strcmp(argv[i], "--device") && has_value && parse_int(argv[i + 1], 0, 1023, val)) opts.device = (int)val, i++;
         else if (!strcmp(argv[i], "--delta") && has_value && parse_int(argv[i + 1], -1, 2147483647, val)) opts.delta = (int)val, i++;
         else if (!strcmp(argv[i], "--cache")) use_cache = true;
+        else if (!strcmp(argv[i], "--autotune") && has_value) tune_path = argv[++i];
         else {
             fprintf(stderr, "dsssp_main: bad option %s%s%s\n", argv[i], has_value ? " " : " (no value)",
                     has_value ? argv[i + 1] : "");
@@ -160,6 +164,13 @@ int main(int argc, char** argv) {
     if (rc) return die("loading the SSSP tree", rc);
     printf("reading input data completed\n");
 
+    if (tune_path && k > 0) {  // settings of the cache for this size class, or tuned on this batch
+        dsssp_tune_result tr;
+        rc = dsssp_autotune(g, ch, k, tune_path, 2, 0, &tr);
+        if (rc) return die("autotuning", rc);
+        fprintf(stderr, "dsssp_main: autotune %s: %s (%.4f ms, %d candidates timed)\n", tr.key,
+                tr.cached ? "cached settings" : "tuned", tr.ms, tr.trials);
+    }
     dsssp_stats st;
     rc = dsssp_apply_batch(g, ch, k, nullptr, &st);
     if (rc < 0) return die("applying the change batch", rc);

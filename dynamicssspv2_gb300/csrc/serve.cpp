@@ -501,6 +501,25 @@ struct dsssp_server {
         int64_t total = 0;
         double start = 0;
     };
+    std::string tune_cache;  // autotuner cache (empty: none)
+    std::string tune_key;    // size class whose cached options are set now
+    dsssp_opts base_opts{};  // the options given at creation (classes the cache does not know)
+
+    // Sets the cached options of the epoch's size class when it differs from the last epoch's
+    // (with dev held, no batch pending).
+    void tune_for(int64_t k) {
+        if (tune_cache.empty()) return;
+        int64_t n = 0, entries = 0;
+        if (dsssp_graph_info(pool->g, &n, &entries, nullptr, nullptr, nullptr) != DSSSP_OK) return;
+        char key[32];
+        dsssp_tune_size_class(n, entries, k, key, sizeof key);
+        if (tune_key == key) return;
+        tune_key = key;
+        dsssp_tune_result r;
+        if (dsssp_autotune_lookup(pool->g, k, tune_cache.c_str(), &r) != DSSSP_OK)
+            dsssp_graph_set_opts(pool->g, &base_opts);
+    }
+
     dsssp_change* stage[2] = {nullptr, nullptr};  // pinned staging of two epochs' records
     int64_t stage_cap[2] = {0, 0};
     std::atomic<int> dev_waiters{0};  // threads waiting for the device between epochs
@@ -609,6 +628,7 @@ struct dsssp_server {
                     flying = false;
                 }
                 if (ep[cur].reqs.empty()) break;
+                tune_for(ep[cur].total);
                 ep[cur].start = now_us();
                 int rc = arc;
                 if (!rc) rc = dsssp_apply_batch_host_async(pool->g, stage[cur], ep[cur].total, nullptr);
@@ -667,6 +687,7 @@ void dsssp_default_server_opts(dsssp_server_opts* so) {
     so->compact_dead_frac = 0.25;
     so->compact_spare_frac = 0.75;
     so->reserve_vertices = 0;
+    so->tune_cache = nullptr;
 }
 
 int dsssp_server_create(int32_t count, const int32_t* n, const int64_t* m, const int32_t* const* u,
@@ -686,6 +707,9 @@ int dsssp_server_create(int32_t count, const int32_t* n, const int64_t* m, const
     else dsssp_default_opts(&opts);
     s->slack_pct = opts.slack_pct;
     s->slack_min = opts.slack_min;
+    s->base_opts = opts;
+    if (s->so.tune_cache) s->tune_cache = s->so.tune_cache;
+    s->so.tune_cache = nullptr;  // the caller's string is not kept
     // admission: tenants in order while their estimated footprint fits the budget; the others
     // wait (their ids are reserved in the pool, so that they can come in when memory frees)
     std::vector<int32_t> an, asrc;

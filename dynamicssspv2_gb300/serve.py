@@ -80,7 +80,7 @@ class Request:
 class Server:
     def __init__(self, tenants, memory_budget: int | None = None, max_epoch_requests: int | None = None,
                  compact_dead_frac: float | None = 0.25, compact_spare_frac: float = 0.75,
-                 reserve_vertices: int = 0, **opts):
+                 reserve_vertices: int = 0, tune_cache: str | None = None, **opts):
         self.tenants = list(tenants)
         o = default_opts(**opts)
         self._slack = (o.slack_pct, o.slack_min)
@@ -92,6 +92,8 @@ class Server:
         so.compact_dead_frac = -1.0 if compact_dead_frac is None else float(compact_dead_frac)
         so.compact_spare_frac = float(compact_spare_frac)
         so.reserve_vertices = int(reserve_vertices)
+        self._tune_cache = str(tune_cache).encode() if tune_cache else None  # kept alive for the call
+        so.tune_cache = self._tune_cache
         n = np.asarray([t.n for t in self.tenants], np.int32)
         us = [np.ascontiguousarray(t.u, np.int32) for t in self.tenants]
         vs = [np.ascontiguousarray(t.v, np.int32) for t in self.tenants]

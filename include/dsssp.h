@@ -297,6 +297,39 @@ const char* dsssp_last_error(void);
 const char* dsssp_strerror(int code);
 void dsssp_free(void* p);
 
+/* ---- autotuner ----------------------------------------------------------------------
+ * Times candidate settings of the update -- edges per thread item and the CTA-chunk
+ * thresholds (degree buckets), walk depth before pointer jumping, CTA size and residency,
+ * solo-step width, near-far bucket widths scaled by the batch's mean weight -- on a
+ * representative batch from one starting state (device snapshot and restore), sets the
+ * fastest on the graph and caches it per size class (log2 vertices, log2 adjacency entries,
+ * log2 batch size) in a text file.  No counterpart in the reference (its block size is a
+ * compile-time macro, SSSPmainForUndirected.cu:11). */
+typedef struct {
+    char key[32];      /* size class "v<log2 n>_e<log2 entries>_b<log2 k>" */
+    dsssp_opts opts;   /* the chosen options (also set on the graph) */
+    double ms;         /* their device time on the batch (best of reps) */
+    int32_t trials;    /* candidates timed; 0 when taken from the cache */
+    int32_t cached;    /* 1 = taken from the cache without timing */
+} dsssp_tune_result;
+
+/* Tunes g for batches like changes[0..k): a cached size class is applied without timing
+ * (unless force); otherwise every candidate runs the batch reps times (0 = 2) and the fastest
+ * is set and written to cache_path (NULL: not cached).  Replaces the graph's snapshot and leaves
+ * the graph and tree as they were before the call. */
+int dsssp_autotune(dsssp_graph* g, const dsssp_change* changes, int64_t k, const char* cache_path,
+                   int32_t reps, int32_t force, dsssp_tune_result* out);
+/* Sets the cached options of g's size class for batches of k records; DSSSP_E_INVAL if the
+ * cache has none (nothing changed). */
+int dsssp_autotune_lookup(dsssp_graph* g, int64_t k, const char* cache_path, dsssp_tune_result* out);
+/* The size-class key of a graph of n vertices and `entries` adjacency entries with k-record
+ * batches (no device needed). */
+int dsssp_tune_size_class(int64_t n, int64_t entries, int64_t k, char* key, size_t cap);
+/* The candidate options the tuner times for batch changes[0..k) starting from base: *count of
+ * them, the first cap written to out (no device needed). */
+int dsssp_tune_candidates(const dsssp_opts* base, const dsssp_change* changes, int64_t k,
+                          dsssp_opts* out, int32_t cap, int32_t* count);
+
 /* ---- shortest-path tree without device allocation ---------------------------------- */
 
 /* Largest graph dsssp_sssp_noalloc() accepts: its work space is a fixed static device array
@@ -492,6 +525,9 @@ typedef struct {
     double compact_spare_frac;   /* default 0.75 */
     int64_t reserve_vertices;    /* spare vertex ids for tenants added later (beyond the ids that
                                     tenants waiting at creation hold); default 0 */
+    const char* tune_cache;      /* autotuner cache file (dsssp_autotune): each epoch runs with the
+                                    cached options of its size class when there are any; NULL = the
+                                    options given at creation throughout (default) */
 } dsssp_server_opts;
 
 #define DSSSP_REFUSED 1 /* request status: its tenant is not admitted (waiting, removed, unknown) */

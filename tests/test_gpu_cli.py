@@ -67,3 +67,31 @@ def test_cache_round_trip_gives_the_same_tree(tmp_path):
     od, _ = O.dijkstra(n, gr, 0)
     assert np.array_equal(outs[0][1], od)
     assert O.validate(n, gr, 0, outs[3][1], outs[3][0]) == 0
+
+
+def test_autotune_flag_tunes_then_reads_the_cache(tmp_path):
+    """--autotune CACHE: the first run times the candidates on the batch (on snapshots) and
+    writes the size class to CACHE, the second takes it from CACHE; both trees are exact."""
+    n = 4000
+    u, v, w = D.gen_er(n, 16000, 1, 100, seed=31)
+    d0, p0 = O.dijkstra(n, O.csr(n, u, v, w), 0)
+    g = tmp_path / "graph.txt"
+    g.write_text("".join(f"{a} {b} {c}\n" for a, b, c in zip(u.tolist(), v.tolist(), w.tolist())))
+    s = tmp_path / "SSSP.txt"
+    D.write_sssp(str(s), p0, d0)
+    ch = D.gen_changes(n, u, v, w, 400, 400, seed=32)
+    c = tmp_path / "cE.txt"
+    D.write_changes(str(c), ch)
+    cache = tmp_path / "tune.txt"
+    gr = O.updated_graph(n, u, v, w, ch)
+    od, _ = O.dijkstra(n, gr, 0)
+    for i, word in enumerate(("tuned", "cached settings")):
+        out = tmp_path / f"out{i}.txt"
+        r = run_cli(g, n, len(u), s, c, "--out", out, "--autotune", cache)
+        assert r.returncode == 0, r.stderr
+        assert f"autotune v12_e15_b10: {word}" in r.stderr, r.stderr
+        parent, dist, _ = D.read_sssp(str(out), n)
+        assert np.array_equal(dist, od)
+        assert O.validate(n, gr, 0, dist, parent) == 0
+    lines = [l for l in cache.read_text().splitlines() if not l.startswith("#")]
+    assert len(lines) == 1 and lines[0].startswith("v12_e15_b10 ") and "small_deg=" in lines[0]

@@ -110,13 +110,13 @@ def test_set_opts_keeps_results_exact():
 
 def test_autotuner_picks_and_caches(tmp_path):
     graphs = make_graphs(8, 3)
-    cache = tmp_path / "tune.json"
+    cache = tmp_path / "tune.txt"
     with GraphPool([(n, u, v, w) for n, u, v, w, _ in graphs]) as pool:
         pool.tree_compute([0] * len(graphs))
         before = pool.graph.tree_read()
         union = pool.union_batch([(i, g[4]) for i, g in enumerate(graphs)])
         res = Autotuner(cache, reps=1).tune(pool.graph, union)
-        assert not res["cached"] and len(res["trials"]) >= 4 and cache.exists()
+        assert not res["cached"] and res["trials"] >= 4 and cache.exists()
         after = pool.graph.tree_read()
         assert np.array_equal(before[1], after[1])  # tuning leaves the distances as they were
         res2 = Autotuner(cache).tune(pool.graph, union)

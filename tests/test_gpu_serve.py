@@ -235,3 +235,33 @@ def test_pool_graphs_added_and_removed():
         with pytest.raises(D.DsssspError) as e:
             pool.graph.clear_range(1000, 500)  # would cut graph 1 in two
         assert e.value.code == D.E_INVAL
+
+
+def test_server_takes_options_from_the_tune_cache(tmp_path):
+    """With tune_cache the server sets, per epoch, the cached options of the epoch's size class:
+    a cache naming small_deg 8 and solo_waves 0 for every batch-size class of this pool is taken
+    (the pool's graph carries them after serving) and the results stay exact."""
+    import ctypes as C
+
+    from dynamicssspv2_gb300.autotune import size_class
+
+    tenants = make_tenants(4, 41)
+    n = sum(t.n for t in tenants)
+    entries = 2 * sum(len(t.u) for t in tenants)
+    cache = tmp_path / "tune.txt"
+    cache.write_text("".join(f"{size_class(n, entries, 1 << b)} 1.0 small_deg=8 solo_waves=0\n" for b in range(0, 14)))
+    rng = np.random.default_rng(42)
+    reqs = [Request(t, 0.0, random_batch(rng, tenants[t], 120)) for t in range(4) for _ in range(2)]
+    with Server(tenants, tune_cache=str(cache)) as srv:
+        out = srv.serve(reqs, record=True, realtime=False)
+        g = D.Graph.__new__(D.Graph)  # the pool's graph, owned by the server (not closed here)
+        g._h = C.c_void_p(D._lib.dsssp_pool_graph(D._lib.dsssp_server_pool(srv._h)))
+        o = g.get_opts()
+        g._h = C.c_void_p()
+        assert o.small_deg == 8 and o.solo_waves == 0
+    for t, ten in enumerate(tenants):
+        with D.Graph(ten.n, ten.u, ten.v, ten.w) as g:
+            g.tree_compute(ten.src)
+            for r in sorted([r for r in out if r.tenant == t], key=lambda r: (r.epoch, r.arrival)):
+                g.apply_batch(r.changes)
+                assert np.array_equal(g.tree_read()[1], r.result[1])

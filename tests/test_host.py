@@ -321,7 +321,7 @@ def test_serving_and_tuning_helpers():
     """Host-side helpers of the batching and serving layers: request summaries (p50/p99,
     refused and failed requests), random tenant batches, the autotuner's size classes, near-far
     candidates and cache file, and the footprint estimate's growth."""
-    from dynamicssspv2_gb300.autotune import Autotuner, size_class
+    from dynamicssspv2_gb300.autotune import candidates, size_class
     from dynamicssspv2_gb300.serve import Request, Tenant, estimate_footprint, random_batch, summarize
 
     ch = np.zeros(10, D.CHANGE_DTYPE)
@@ -344,9 +344,13 @@ def test_serving_and_tuning_helpers():
 
     assert size_class(1 << 20, 1 << 24, 1000) == "v20_e24_b10"
     wbar = float(np.mean(b["w"]))
-    cands = Autotuner.near_far_candidates(b)
-    assert [c["delta"] for c in cands] == [max(1, int(round(f * wbar))) for f in (8.0, 96.0)]
-    assert Autotuner.near_far_candidates(np.zeros(0, D.CHANGE_DTYPE)) == []
+    base = D.default_opts()
+    cands = candidates(base, b)
+    # the fixed candidates (the defaults first), then two near-far widths from the batch's mean weight
+    assert len(cands) == 12 and cands[0].small_deg == base.small_deg and cands[0].delta == base.delta
+    assert [c.delta for c in cands[-2:]] == [max(1, int(np.floor(f * wbar + 0.5))) for f in (8.0, 96.0)]
+    assert {c.solo_waves for c in cands} == {0, 2, 4} and {c.bfs_levels for c in cands} == {0, 8, 48}
+    assert len(candidates(base, np.zeros(0, D.CHANGE_DTYPE))) == 10
 
     assert estimate_footprint(1000, 4000) < estimate_footprint(2000, 4000) < estimate_footprint(2000, 8000)
 
