@@ -53,6 +53,11 @@ WORKLOADS = {
     "er10k": dict(kind="er", n=10_000, m=50_000, wlo=1, whi=100, n_ins=500, n_del=500),
     "grid4096": dict(kind="grid", rows=4096, cols=4096, remove=0.05, diag=167_772, wlo=1, whi=1000,
                      n_ins=25_000, n_del=75_000),
+    # smaller cases of the same kernels, for profiler captures that must stay within a few GB
+    "grid2048": dict(kind="grid", rows=2048, cols=2048, remove=0.05, diag=41_943, wlo=1, whi=1000,
+                     n_ins=6_250, n_del=18_750),
+    "batch64": dict(kind="batch", count=64, nlo=3.0, nhi=5.5, degree=8, wlo=1, whi=100, flo=-3.0, fhi=-1.0,
+                    slack_pct=50, slack_min=16),
 }
 
 
@@ -873,17 +878,120 @@ def serving_summary(workload: str, dist: Dist, plain_baseline: bool = True) -> d
     return line
 
 
+def run_once(args) -> int:
+    """One batch of the workload, for a profiler: build the graph (or the pool), compute the tree,
+    apply the batch once.  The update kernel's second launch is the batch's."""
+    import dynamicssspv2_gb300 as D
+    from dynamicssspv2_gb300.pool import GraphPool
+
+    t0 = time.perf_counter()
+    if WORKLOADS[args.workload]["kind"] == "batch":
+        wl = WORKLOADS[args.workload]
+        items = make_batch_inputs(args.workload)
+        with GraphPool([(n, u, v, w) for n, u, v, w, _ in items], slack_pct=wl["slack_pct"],
+                       slack_min=wl["slack_min"]) as pool:
+            pool.tree_compute([0] * len(items))
+            st = pool.apply([(i, it[4]) for i, it in enumerate(items)])
+    else:
+        n, u, v, w, src, ch = make_inputs(args.workload)
+        with D.Graph(n, u, v, w) as g:
+            g.tree_compute(src)
+            st = g.apply_batch(ch)
+    print(json.dumps({"workload": args.workload, "once": True, "t_total_ms": st.t_total_ms,
+                      "t_update_ms": st.t_update_ms, "wall_s": time.perf_counter() - t0}), flush=True)
+    return 0
+
+
+def run_tour(args) -> int:
+    """Every kernel of the library once, on an RMAT scale-20 graph (1M vertices, 8M edges: larger
+    than the L2, a few hundred MB on the device): graph build, tree computation, a batch, the tree
+    reads, the certificate, a batch whose rows grow into the spare region, compaction, a batch that
+    repacks with overflowed entries, tree load, a pool graph added and removed, and the
+    no-allocation entry point.  For a profiler's launch list; prints the host time of each step."""
+    import torch
+
+    import dynamicssspv2_gb300 as D
+    from dynamicssspv2_gb300.pool import GraphPool
+    from oracle import pyoracle as O
+
+    steps = {}
+
+    def step(name, fn):
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        steps[name] = round((time.perf_counter() - t0) * 1e3, 3)
+        return r
+
+    scale, m = 20, 8 << 20
+    n = 1 << scale
+    u, v, w = D.gen_rmat(scale, m, 0.57, 0.19, 0.19, 1, 100, seed=0)
+    src = D.max_degree_vertex(n, u, v)
+    ch = D.gen_changes(n, u, v, w, 100_000, 100_000, D.INS_RMAT, scale, 0.57, 0.19, 0.19, 1, 100, seed=1)
+    g = step("graph_create", lambda: D.Graph(n, u, v, w, spare_pct=50))
+    step("tree_compute", lambda: g.tree_compute(src))
+    step("snapshot", g.snapshot)
+    step("apply_batch", lambda: g.apply_batch(ch))
+    step("tree_read", g.tree_read)
+    step("tree_read_changed", g.tree_read_changed)
+    step("validate", g.validate)
+    # insertions around 64 vertices overflow their rows' slack: the rows move to the spare region
+    rng = np.random.default_rng(3)
+    hubs = rng.integers(0, n, 64)
+    grow = D.make_changes(np.repeat(hubs, 500), rng.integers(0, n, 64 * 500), rng.integers(1, 101, 64 * 500),
+                          np.ones(64 * 500))
+    st = step("apply_batch_growing_rows", lambda: g.apply_batch(grow))
+    steps["growth_overflow_entries"] = int(st.overflow_entries)
+    step("compact", g.compact)
+    parent, dist = g.tree_read()
+    step("tree_load", lambda: g.tree_load(parent, dist))
+    g.close()
+    # no slack and no spare region: the batch's overflowed entries are folded in by a repack
+    n2, m2 = 200_000, 800_000
+    u2, v2, w2 = D.gen_er(n2, m2, 1, 100, seed=4)
+    ch2 = D.gen_changes(n2, u2, v2, w2, 20_000, 20_000, seed=5)
+    with D.Graph(n2, u2, v2, w2, slack_pct=0, slack_min=0, spare_pct=0) as g2:
+        g2.tree_compute(0)
+        st = step("apply_batch_repack", lambda: g2.apply_batch(ch2))
+        steps["repacks"] = int(st.repacks)
+    # a graph added to a pool's reserve and removed again
+    with GraphPool([(n2, u2, v2, w2)], reserve_vertices=n2) as pool:
+        pool.tree_compute([0])
+        gi = step("pool_add_graph", lambda: pool.add_graph(n2, u2, v2, w2, src=7))
+        step("pool_remove_graph", lambda: pool.remove_graph(gi))
+    # the no-allocation entry point on caller-owned device buffers
+    n3 = 60_000
+    u3, v3, w3 = D.gen_er(n3, 4 * n3, 1, 100, seed=6)
+    csr = O.csr(n3, u3, v3, w3)
+    adj = np.ascontiguousarray(np.stack([csr.col, csr.wt], axis=1).astype(np.int32))
+    d_off = torch.from_numpy(csr.off.astype(np.int64)).cuda()
+    d_adj = torch.from_numpy(adj.reshape(-1)).cuda()
+    d_par = torch.empty(n3, dtype=torch.int32, device="cuda")
+    d_dist = torch.empty(n3, dtype=torch.int64, device="cuda")
+    step("sssp_noalloc", lambda: D.sssp_noalloc(n3, len(csr.col), d_off.data_ptr(), d_adj.data_ptr(), 0,
+                                                 d_par.data_ptr(), d_dist.data_ptr()))
+    print(json.dumps({"workload": "tour", "graph": f"RMAT scale {scale}, {m} edges", "step_ms": steps,
+                      "kernel_launches": D.launch_count()}), flush=True)
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["dsssp", "reference"], default="dsssp")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="rmat22")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["tour"], default="rmat22",
+                    help="tour: every kernel of the library once (for a profiler's launch list)")
+    ap.add_argument("--once", action="store_true", help="one batch of the workload, for a profiler")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--headline-only", action="store_true",
                     help="rmat22: skip the batching and serving workloads that the default line also carries")
     args = ap.parse_args()
+    if args.workload == "tour":
+        return run_tour(args)
+    if args.once:
+        return run_once(args)
     dist = Dist()
     if args.impl == "reference":
         if WORKLOADS[args.workload]["kind"] in ("batch", "serve"):
