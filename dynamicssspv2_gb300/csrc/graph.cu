@@ -13,8 +13,8 @@
 #include <cstring>
 #include <vector>
 
+#include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
-#include <cub/device/device_segmented_sort.cuh>
 #include <cuda_runtime.h>
 
 #include "../../include/dsssp.h"
@@ -89,19 +89,15 @@ __device__ __forceinline__ long long lower_key(const unsigned long long* keys, l
     return lo;
 }
 
-// Packed (contiguous) sorted rows -> slack layout.  Thread per entry; row by binary search.
+// Packed (contiguous) sorted rows -> slack layout.  Thread per entry.
 // With twin != nullptr also the slot of the reverse entry: the i-th copy of (c, w) in row r
 // pairs with the i-th copy of (r, w) in row c.
-__global__ void k_spread(const unsigned long long* keys, const long long* poff, const long long* start, int n,
-                         long long total, int2* adj, unsigned* twin) {
+// row[e] = the row of entry e (sorted alongside the keys).
+__global__ void k_spread(const unsigned long long* keys, const unsigned* row, const long long* poff,
+                         const long long* start, long long total, int2* adj, unsigned* twin) {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= total) return;
-    int lo = 0, hi = n;  // last r with poff[r] <= e
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (poff[mid] <= e) lo = mid;
-        else hi = mid;
-    }
+    const int lo = (int)row[e];
     const unsigned long long k = keys[e];
     const long long slot = start[lo] + (e - poff[lo]);
     const int c = (int)(k >> 32), w = (int)(unsigned)k;
@@ -112,6 +108,14 @@ __global__ void k_spread(const unsigned long long* keys, const long long* poff, 
         const long long pos = lower_key(keys, poff[c], poff[c + 1], rk);
         twin[slot] = (unsigned)(start[c] + (pos - poff[c]) + rank);
     }
+}
+
+// Row id of every packed entry: warp per row r fills its segment [poff[r], poff[r+1]).
+__global__ void k_row_ids(const long long* poff, int n, unsigned* ids) {
+    const unsigned lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps)
+        for (long long e = poff[r] + lane; e < poff[r + 1]; e += 32) ids[e] = (unsigned)r;
 }
 
 __global__ void k_rows_init(const long long* start, const long long* deg, const long long* cap, int n,
@@ -757,29 +761,47 @@ int layout_rows(dsssp_graph* g, unsigned long long* keys_in, long long total, co
     const int n = g->n;
     long long *cap = nullptr, *start = nullptr;
     unsigned long long* keys_out = nullptr;
+    unsigned *ids_a = nullptr, *ids_b = nullptr;
+    const unsigned long long* keys_sorted = keys_in;
+    const unsigned* rows_sorted = ids_a;
     void* tmp = nullptr;
     int2* adj = nullptr;
     long long cap_total = 0;
     int rc = dalloc(&cap, (size_t)n + 1, "row caps");
     if (!rc) rc = dalloc(&start, (size_t)n + 1, "row starts");
     if (!rc) rc = dalloc(&keys_out, (size_t)total, "sort buffer");
+    if (!rc) rc = dalloc(&ids_a, (size_t)total, "sort buffer");
+    if (!rc) rc = dalloc(&ids_b, (size_t)total, "sort buffer");
     if (!rc) {
         cudaError_t e = cudaMemsetAsync(cap + n, 0, sizeof(long long), s);
         if (n > 0 && e == cudaSuccess) {
             k_caps<<<blocks_for(n), kThreads, 0, s>>>(deg64, n, g->o.slack_pct, g->o.slack_min, cap);
             count_launch(1);
         }
-        size_t tb1 = 0, tb2 = 0;
+        // Rows sorted by (neighbour, weight) with two stable radix sorts over all entries: by the
+        // (col << 32 | wt) key carrying the row id, then by row id carrying the key, so no row is
+        // sorted by one CTA alone (a segmented sort leaves hub rows of 10^5 entries to one block).
+        int row_bits = 1;
+        while (row_bits < 32 && (1ll << row_bits) < (long long)n) row_bits++;
+        int key_bits = 32 + row_bits;  // column < n, weight < 2^31
+        cub::DoubleBuffer<unsigned long long> dk(keys_in, keys_out);
+        cub::DoubleBuffer<unsigned> dv(ids_a, ids_b);
+        size_t tb1 = 0, tb2 = 0, tb3 = 0;
         if (e == cudaSuccess) e = cub::DeviceScan::ExclusiveSum(nullptr, tb1, cap, start, n + 1, s);
-        if (e == cudaSuccess)
-            e = cub::DeviceSegmentedSort::SortKeys(nullptr, tb2, (const unsigned long long*)keys_in, keys_out, total,
-                                                   n, poff, poff + 1, s);
-        const size_t tb = tb1 > tb2 ? tb1 : tb2;
+        if (e == cudaSuccess) e = cub::DeviceRadixSort::SortPairs(nullptr, tb2, dk, dv, total, 0, key_bits, s);
+        if (e == cudaSuccess) e = cub::DeviceRadixSort::SortPairs(nullptr, tb3, dv, dk, total, 0, row_bits, s);
+        size_t tb = tb1 > tb2 ? tb1 : tb2;
+        tb = tb > tb3 ? tb : tb3;
         if (e == cudaSuccess) e = cudaMalloc(&tmp, tb ? tb : 1);
         if (e == cudaSuccess) e = cub::DeviceScan::ExclusiveSum(tmp, tb1, cap, start, n + 1, s);
-        if (e == cudaSuccess && total > 0)
-            e = cub::DeviceSegmentedSort::SortKeys(tmp, tb2, (const unsigned long long*)keys_in, keys_out, total, n,
-                                                   poff, poff + 1, s);
+        if (e == cudaSuccess && total > 0) {
+            k_row_ids<<<(unsigned)(((long long)n * 32 + kThreads - 1) / kThreads), kThreads, 0, s>>>(poff, n, ids_a);
+            count_launch(1);
+            e = cub::DeviceRadixSort::SortPairs(tmp, tb2, dk, dv, total, 0, key_bits, s);
+            if (e == cudaSuccess) e = cub::DeviceRadixSort::SortPairs(tmp, tb3, dv, dk, total, 0, row_bits, s);
+            keys_sorted = dk.Current();
+            rows_sorted = dv.Current();
+        }
         if (e == cudaSuccess) e = cudaMemcpyAsync(&cap_total, start + n, sizeof(long long), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) rc = cuda_fail(e, "row layout");
@@ -799,7 +821,7 @@ int layout_rows(dsssp_graph* g, unsigned long long* keys_in, long long total, co
     if (!rc && cap_total < 0xFFFFFFFFll) rc = dalloc(&twin, (size_t)cap_total, "twin index");
     if (!rc) {
         if (total > 0) {
-            k_spread<<<blocks_for(total), kThreads, 0, s>>>(keys_out, poff, start, n, total, adj, twin);
+            k_spread<<<blocks_for(total), kThreads, 0, s>>>(keys_sorted, rows_sorted, poff, start, total, adj, twin);
             count_launch(1);
         }
         if (n > 0) {
@@ -827,6 +849,8 @@ int layout_rows(dsssp_graph* g, unsigned long long* keys_in, long long total, co
     dfree(cap);
     dfree(start);
     dfree(keys_out);
+    dfree(ids_a);
+    dfree(ids_b);
     if (tmp) cudaFree(tmp);
     dfree(adj);
     dfree(twin);
