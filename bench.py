@@ -276,10 +276,35 @@ def host_cores() -> int:
 
 # ---- arms -------------------------------------------------------------------------------------
 
+def make_inputs_cpu(name: str):
+    """The workload's inputs from the oracle's restatement of the generators (bit-identical to
+    make_inputs, which uses the library's): the CPU reference arm loads no product library."""
+    from oracle import pyoracle as O
+
+    w = WORKLOADS[name]
+    if w["kind"] == "rmat":
+        n = 1 << w["scale"]
+        u, v, wt = O.gen_rmat(w["scale"], w["m"], 0.57, 0.19, 0.19, w["wlo"], w["whi"], 0)
+        src = O.max_degree_vertex(n, u, v)
+        ch = O.gen_changes(n, u, v, wt, w["n_ins"], w["n_del"], 1, w["scale"], 0.57, 0.19, 0.19, w["wlo"], w["whi"], 1)
+    elif w["kind"] == "er":
+        n = w["n"]
+        u, v, wt = O.gen_er(n, w["m"], w["wlo"], w["whi"], 0)
+        src = 0
+        ch = O.gen_changes(n, u, v, wt, w["n_ins"], w["n_del"], 0, 0, 0.0, 0.0, 0.0, w["wlo"], w["whi"], 1)
+    else:
+        raise ValueError(f"{name}: no CPU restatement of this workload's generator")
+    return n, u, v, wt, src, ch
+
+
 def run_reference(args, dist: Dist) -> int:
     if dist.rank != 0:
         return 0
-    n, u, v, w, src, ch = make_inputs(args.workload)
+    if WORKLOADS[args.workload]["kind"] not in ("rmat", "er"):
+        print(json.dumps({"impl": "reference", "unavailable": f"the CPU reference arm runs the rmat22 and er10k "
+                          f"workloads (their generators are restated on the CPU side); not {args.workload}"}))
+        return 0
+    n, u, v, w, src, ch = make_inputs_cpu(args.workload)
     batch = len(ch)
     for _ in range(args.warmup):
         cpu_recompute(n, u, v, w, ch, src)

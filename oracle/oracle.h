@@ -89,6 +89,22 @@ int orc_ref_update(int32_t n, int64_t m, const int32_t* eu, const int32_t* ev, c
 void orc_read_sssp_semantics(int32_t n, int64_t rows, const int32_t* node, const int32_t* par,
                              const int32_t* dist, int32_t* out_parent, int32_t* out_dist);
 
+/* ---- seeded synthetic inputs (oracle_gen.c) ----------------------------------------
+ * The same streams as the dsssp library's generators (include/dsssp.h dsssp_gen_er,
+ * dsssp_gen_rmat, dsssp_gen_changes with DSSSP_INS_UNIFORM (0) or DSSSP_INS_RMAT (1),
+ * dsssp_max_degree_vertex), restated so that the CPU reference arm of bench.py builds its
+ * workload without the product library; tests check that the outputs are identical.
+ * Outputs are caller arrays of m (edges) or n_ins + n_del (changes) entries; 0 or -1. */
+int orc_gen_er(int32_t n, int64_t m, int32_t wlo, int32_t whi, uint64_t seed, int32_t* u, int32_t* v,
+               int32_t* w);
+int orc_gen_rmat(int32_t scale, int64_t m, double a, double b, double c, int32_t wlo, int32_t whi,
+                 uint64_t seed, int32_t* u, int32_t* v, int32_t* w);
+int32_t orc_max_degree_vertex(int32_t n, int64_t m, const int32_t* u, const int32_t* v);
+int orc_gen_changes(int32_t n, int64_t m, const int32_t* eu, const int32_t* ev, const int32_t* ew,
+                    int64_t n_ins, int64_t n_del, int32_t ins_kind, int32_t scale, double p0, double p1,
+                    double p2, int32_t wlo, int32_t whi, uint64_t seed, int32_t* cu, int32_t* cv,
+                    int32_t* cw, int32_t* cop);
+
 #ifdef __cplusplus
 }
 #endif

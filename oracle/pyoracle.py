@@ -44,7 +44,52 @@ _lib.orc_ref_update.argtypes = [C.c_int32, C.c_int64, _i32, _i32, _i32, C.c_int6
 _lib.orc_read_sssp_semantics.restype = None
 _lib.orc_read_sssp_semantics.argtypes = [C.c_int32, C.c_int64, _i32, _i32, _i32, _i32, _i32]
 
+_lib.orc_gen_er.restype = C.c_int
+_lib.orc_gen_er.argtypes = [C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.c_uint64, _i32, _i32, _i32]
+_lib.orc_gen_rmat.restype = C.c_int
+_lib.orc_gen_rmat.argtypes = [C.c_int32, C.c_int64, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,
+                              C.c_uint64, _i32, _i32, _i32]
+_lib.orc_max_degree_vertex.restype = C.c_int32
+_lib.orc_max_degree_vertex.argtypes = [C.c_int32, C.c_int64, _i32, _i32]
+_lib.orc_gen_changes.restype = C.c_int
+_lib.orc_gen_changes.argtypes = [C.c_int32, C.c_int64, _i32, _i32, _i32, C.c_int64, C.c_int64, C.c_int32, C.c_int32,
+                                 C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32, C.c_uint64, _i32, _i32,
+                                 _i32, _i32]
+
 EXACT_INF = (1 << 62)
+
+CHANGE_DTYPE = np.dtype([("u", "<i4"), ("v", "<i4"), ("w", "<i4"), ("op", "<i4")])
+
+
+def gen_er(n, m, wlo=1, whi=100, seed=0):
+    """Erdos-Renyi edge list of the library's generator (same streams), on the CPU."""
+    u, v, w = (np.empty(m, np.int32) for _ in range(3))
+    if _lib.orc_gen_er(n, m, wlo, whi, seed, u, v, w) != 0:
+        raise ValueError("gen_er: bad arguments")
+    return u, v, w
+
+
+def gen_rmat(scale, m, a=0.57, b=0.19, c=0.19, wlo=1, whi=100, seed=0):
+    u, v, w = (np.empty(m, np.int32) for _ in range(3))
+    if _lib.orc_gen_rmat(scale, m, a, b, c, wlo, whi, seed, u, v, w) != 0:
+        raise ValueError("gen_rmat: bad arguments")
+    return u, v, w
+
+
+def max_degree_vertex(n, u, v):
+    return int(_lib.orc_max_degree_vertex(n, len(u), _a32(u), _a32(v)))
+
+
+def gen_changes(n, u, v, w, n_ins, n_del, kind=0, scale=0, p0=0.0, p1=0.0, p2=0.0, wlo=1, whi=100, seed=0):
+    """A change batch of the library's dsssp_gen_changes (uniform or RMAT insertions)."""
+    k = n_ins + n_del
+    cu, cv, cw, cop = (np.empty(k, np.int32) for _ in range(4))
+    if _lib.orc_gen_changes(n, len(u), _a32(u), _a32(v), _a32(w), n_ins, n_del, kind, scale, p0, p1, p2, wlo, whi,
+                            seed, cu, cv, cw, cop) != 0:
+        raise ValueError("gen_changes: bad arguments or too few new pairs")
+    out = np.empty(k, CHANGE_DTYPE)
+    out["u"], out["v"], out["w"], out["op"] = cu, cv, cw, cop
+    return out
 
 
 def _a32(x):

@@ -129,3 +129,26 @@ def test_reference_dijkstra_timing_harness():
     out = subprocess.run([sys.executable, str(root / "oracle" / "time_ref.py"), "--workload", "er10k", "--reps", "1"],
                          capture_output=True, text=True, timeout=300, check=True).stdout
     assert "reference djk" in out and "oracle restatement" in out
+
+
+def test_oracle_generators_match_the_library():
+    """The oracle's restatement of the seeded generators (used by bench.py's CPU reference arm,
+    which loads no product library) gives exactly the library's edge lists, change batches and
+    highest-degree vertex."""
+    import dynamicssspv2_gb300 as D
+
+    for n, m, wlo, whi, seed in ((1000, 4000, 1, 100, 5), (5000, 30000, 1, 60, 7)):
+        a, b = D.gen_er(n, m, wlo, whi, seed), O.gen_er(n, m, wlo, whi, seed)
+        assert all(np.array_equal(x, y) for x, y in zip(a, b))
+        c1 = D.gen_changes(n, *a, 300, 300, seed=3, wlo=2, whi=9)
+        c2 = O.gen_changes(n, *b, 300, 300, 0, 0, 0.0, 0.0, 0.0, 2, 9, 3)
+        assert np.array_equal(c1.view(np.int32), c2.view(np.int32))
+    for scale, m in ((10, 3000), (14, 100000)):
+        n = 1 << scale
+        a = D.gen_rmat(scale, m, 0.57, 0.19, 0.19, 1, 100, seed=0)
+        b = O.gen_rmat(scale, m, 0.57, 0.19, 0.19, 1, 100, 0)
+        assert all(np.array_equal(x, y) for x, y in zip(a, b))
+        assert D.max_degree_vertex(n, a[0], a[1]) == O.max_degree_vertex(n, b[0], b[1])
+        c1 = D.gen_changes(n, *a, 500, 400, D.INS_RMAT, scale, 0.57, 0.19, 0.19, 1, 100, seed=1)
+        c2 = O.gen_changes(n, *b, 500, 400, 1, scale, 0.57, 0.19, 0.19, 1, 100, 1)
+        assert np.array_equal(c1.view(np.int32), c2.view(np.int32))
