@@ -392,40 +392,78 @@ __global__ void k_tree_changed(const unsigned long long* state, const unsigned* 
 // distance (dist[u] + w < dist[v], an unreachable v included), a reachable non-root v has a
 // live entry to its parent p with dist[p] + w == dist[v], and a root (its own parent) has
 // distance 0.  out[0] counts violations, out[1] roots, out[2] the least violating vertex.
+// Checks of one row's entries (a range of them): a shorter distance on offer (bad), the tight
+// live parent edge (tight).
+__device__ __forceinline__ void validate_entries(const unsigned long long* state, const int2* adj, long long lo,
+                                                 long long hi, long long step, bool reach, unsigned long long dv,
+                                                 unsigned pv, bool& bad, bool& tight) {
+    for (long long i = lo; i < hi; i += step) {
+        const int2 e = adj[i];
+        if (e.y < 0) continue;
+        const unsigned long long su = state[e.x];
+        if (su == kInfState) continue;
+        const unsigned long long du = su >> 32;
+        if (du + (unsigned)e.y < dv) bad = true;  // a shorter distance is on offer
+        if (reach && (unsigned)e.x == pv && du + (unsigned)e.y == dv) tight = true;
+    }
+}
+
+// The verdict on vertex v once its row is checked (one thread).
+__device__ __forceinline__ void validate_vertex(long long v, int n, bool reach, unsigned long long dv, unsigned pv,
+                                                bool bad, bool tight, unsigned* jm, unsigned long long* out) {
+    const bool root = reach && pv == (unsigned)v;
+    if (reach && !root && (pv >= (unsigned)n || !tight)) bad = true;  // no tight live parent edge
+    if (root && dv != 0) bad = true;
+    if (root) atomicAdd(&out[1], 1ull);
+    if (bad) {
+        atomicAdd(&out[0], 1ull);
+        atomicMin(&out[2], (unsigned long long)v);
+    }
+    // pointer-jumping word: terminal (kTagOk) at roots and unreachable vertices
+    jm[v] = (!reach || root || pv >= (unsigned)n) ? kTagOk : pv;
+}
+
+constexpr int kValidateLongRow = 2048;  // rows above this are checked by a whole CTA
+
+// Warp per row; rows above kValidateLongRow entries are listed (long, *nlong) for k_validate_long.
 __global__ void k_validate_rows(const unsigned long long* state, const RowDesc* rows, const int2* adj, int n,
-                                unsigned* jm, unsigned long long* out) {
+                                unsigned* jm, unsigned long long* out, unsigned* lng, unsigned* nlong) {
     const unsigned lane = threadIdx.x & 31;
     const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
     for (long long v = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
+        const RowDesc rd = rows[v];
+        if (rd.deg > kValidateLongRow) {
+            if (lane == 0) lng[atomicAdd(nlong, 1u)] = (unsigned)v;
+            continue;
+        }
         const unsigned long long sv = state[v];
         const bool reach = sv != kInfState;
         const unsigned long long dv = reach ? (sv >> 32) : (unsigned long long)kDistInf;
         const unsigned pv = (unsigned)sv;
-        const RowDesc rd = rows[v];
         bool bad = false, tight = false;
-        for (int i = (int)lane; i < rd.deg; i += 32) {
-            const int2 e = adj[rd.start + i];
-            if (e.y < 0) continue;
-            const unsigned long long su = state[e.x];
-            if (su == kInfState) continue;
-            const unsigned long long du = su >> 32;
-            if (du + (unsigned)e.y < dv) bad = true;  // a shorter distance is on offer
-            if (reach && (unsigned)e.x == pv && du + (unsigned)e.y == dv) tight = true;
-        }
+        validate_entries(state, adj, rd.start + lane, rd.start + rd.deg, 32, reach, dv, pv, bad, tight);
         bad = __any_sync(0xFFFFFFFFu, bad);
         tight = __any_sync(0xFFFFFFFFu, tight);
-        if (lane == 0) {
-            const bool root = reach && pv == (unsigned)v;
-            if (reach && !root && (pv >= (unsigned)n || !tight)) bad = true;  // no tight live parent edge
-            if (root && dv != 0) bad = true;
-            if (root) atomicAdd(&out[1], 1ull);
-            if (bad) {
-                atomicAdd(&out[0], 1ull);
-                atomicMin(&out[2], (unsigned long long)v);
-            }
-            // pointer-jumping word: terminal (kTagOk) at roots and unreachable vertices
-            jm[v] = (!reach || root || pv >= (unsigned)n) ? kTagOk : pv;
-        }
+        if (lane == 0) validate_vertex(v, n, reach, dv, pv, bad, tight, jm, out);
+    }
+}
+
+// CTA per long row (hubs of up to millions of entries would keep one warp busy for ms).
+__global__ void k_validate_long(const unsigned long long* state, const RowDesc* rows, const int2* adj, int n,
+                                unsigned* jm, unsigned long long* out, const unsigned* lng, const unsigned* nlong) {
+    const unsigned count = *nlong;
+    for (unsigned i = blockIdx.x; i < count; i += gridDim.x) {
+        const long long v = lng[i];
+        const RowDesc rd = rows[v];
+        const unsigned long long sv = state[v];
+        const bool reach = sv != kInfState;
+        const unsigned long long dv = reach ? (sv >> 32) : (unsigned long long)kDistInf;
+        const unsigned pv = (unsigned)sv;
+        bool bad = false, tight = false;
+        validate_entries(state, adj, rd.start + threadIdx.x, rd.start + rd.deg, blockDim.x, reach, dv, pv, bad, tight);
+        bad = __syncthreads_or(bad);
+        tight = __syncthreads_or(tight);
+        if (threadIdx.x == 0) validate_vertex(v, n, reach, dv, pv, bad, tight, jm, out);
     }
 }
 
@@ -1853,22 +1891,33 @@ int dsssp_tree_validate(dsssp_graph* g, int64_t* violations, int64_t* roots, int
     if (g->pending) return fail(DSSSP_E_INVAL, "tree_validate: a batch is still pending");
     cudaStream_t s = g->stream;
     unsigned long long* d_out = nullptr;
+    unsigned* d_long = nullptr;  // [0] count, then the long rows
     rc = dalloc(&d_out, 3, "validation counters");
-    if (rc) return rc;
+    const long long long_cap = g->cap_total / kValidateLongRow + 2;
+    if (!rc) rc = dalloc(&d_long, (size_t)long_cap, "validation rows");
+    if (rc) {
+        dfree(d_out);
+        return rc;
+    }
     const unsigned long long init[3] = {0, 0, ~0ull};
     unsigned long long out[3] = {0, 0, 0};
     cudaError_t e = cudaMemcpyAsync(d_out, init, sizeof(init), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_long, 0, sizeof(unsigned), s);
     const unsigned grid = (unsigned)(g->num_sms * 8);
     if (e == cudaSuccess) {
-        k_validate_rows<<<grid, kThreads, 0, s>>>(g->dg.state, g->dg.rows, g->dg.adj, g->n, g->dg.jm, d_out);
+        k_validate_rows<<<grid, kThreads, 0, s>>>(g->dg.state, g->dg.rows, g->dg.adj, g->n, g->dg.jm, d_out,
+                                                  d_long + 1, d_long);
+        k_validate_long<<<grid, kThreads, 0, s>>>(g->dg.state, g->dg.rows, g->dg.adj, g->n, g->dg.jm, d_out,
+                                                  d_long + 1, d_long);
         for (int pass = 0; pass < 32; pass++) k_validate_jump<<<grid, kThreads, 0, s>>>(g->dg.jm, g->n);
         k_validate_cycles<<<grid, kThreads, 0, s>>>(g->dg.jm, g->n, d_out);
-        count_launch(34);
+        count_launch(35);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, sizeof(out), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     dfree(d_out);
+    dfree(d_long);
     if (e != cudaSuccess) return cuda_fail(e, "tree_validate");
     *violations = (int64_t)out[0];
     if (roots) *roots = (int64_t)out[1];

@@ -549,6 +549,28 @@ def test_device_certificate_of_the_tree():
         assert c["violations"] == 3 and c["first_bad"] == 2
 
 
+def test_device_certificate_on_hub_rows():
+    """Rows above 2,048 entries are certified by a whole CTA: a hub whose distance is too large
+    (a neighbour offers less) or whose parent edge is not tight is caught through its own long
+    row, and a correct tree with hubs has no violation."""
+    rng = np.random.default_rng(53)
+    n = 20000
+    hubs = np.array([0, 1, 2])
+    u = np.concatenate([np.repeat(hubs, 6000), rng.integers(0, n, 20000)]).astype(np.int32)
+    v = np.concatenate([rng.integers(3, n, 18000), rng.integers(0, n, 20000)]).astype(np.int32)
+    w = rng.integers(1, 50, len(u)).astype(np.int32)
+    with D.Graph(n, u, v, w) as g:
+        g.tree_compute(0)
+        c = g.validate()
+        assert c["violations"] == 0 and c["roots"] == 1
+        parent, dist = g.tree_read()
+        bad = dist.copy()
+        bad[1] += 1000  # hub 1: a neighbour on its 6,000-entry row now offers less
+        g.tree_load(parent, bad)
+        c = g.validate()
+        assert c["violations"] >= 1 and c["first_bad"] <= 1
+
+
 def test_automatic_near_far_on_a_deep_graph():
     """delta -1 (the default): plain rounds while batches converge in few rounds, near-far
     rounds after one that needed more than 256 (a 400 x 40 grid from its corner)."""
