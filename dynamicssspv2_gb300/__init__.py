@@ -29,6 +29,7 @@ OK = 0
 E_INVAL, E_OOM, E_BAD_VERTEX, E_CUDA, E_NO_CONVERGENCE, E_TIMEOUT = -1, -2, -3, -4, -5, -6
 E_BAD_TREE, E_OVERFLOW, E_IO, E_BAD_WEIGHT, E_NO_DEVICE, E_COOP = -7, -8, -9, -10, -11, -12
 UNREACHABLE = -1
+UNREACHABLE32 = 0xFFFFFFFF
 INS_UNIFORM, INS_RMAT, INS_LOCAL = 0, 1, 2
 
 CHANGE_DTYPE = np.dtype([("u", "<i4"), ("v", "<i4"), ("w", "<i4"), ("op", "<i4")])
@@ -113,6 +114,7 @@ _sig("dsssp_forest_load", C.c_int, _P, _i32p, _i64p)
 _sig("dsssp_tree_add_sources", C.c_int, _P, _i32p, C.c_int32, C.POINTER(Stats))
 _sig("dsssp_graph_clear_range", C.c_int, _P, C.c_int32, C.c_int32)
 _sig("dsssp_tree_read", C.c_int, _P, _P, _P)
+_sig("dsssp_tree_read32", C.c_int, _P, _P, _P)
 _sig("dsssp_tree_read_changed", C.c_int, _P, _P, _P, _P, C.c_int64, C.POINTER(C.c_int64))
 _sig("dsssp_tree_validate", C.c_int, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32))
 _sig("dsssp_debug_set", C.c_int, _P, C.c_int32, C.c_int64)
@@ -232,7 +234,7 @@ NOALLOC_MAX_ENTRIES = 1 << 20
 
 EXPORTED = [
     "dsssp_default_opts", "dsssp_graph_create", "dsssp_graph_destroy", "dsssp_graph_info", "dsssp_tree_load",
-    "dsssp_tree_compute", "dsssp_tree_compute_multi", "dsssp_forest_load", "dsssp_tree_read", "dsssp_apply_batch", "dsssp_apply_batch_async", "dsssp_batch_finish",
+    "dsssp_tree_compute", "dsssp_tree_compute_multi", "dsssp_forest_load", "dsssp_tree_read", "dsssp_tree_read32", "dsssp_apply_batch", "dsssp_apply_batch_async", "dsssp_batch_finish",
     "dsssp_graph_set_opts", "dsssp_graph_get_opts", "dsssp_graph_snapshot", "dsssp_graph_restore", "dsssp_graph_compact", "dsssp_host_alloc", "dsssp_host_free",
     "dsssp_launch_count", "dsssp_last_error", "dsssp_strerror", "dsssp_free", "dsssp_read_graph_file",
     "dsssp_read_changes_file", "dsssp_read_sssp_file", "dsssp_write_sssp_file", "dsssp_gen_er", "dsssp_gen_rmat",
@@ -386,6 +388,16 @@ class Graph:
         if dist is None:
             dist = np.empty(self.n, np.int64)
         _check(_lib.dsssp_tree_read(self._h, parent.ctypes.data, dist.ctypes.data), "tree_read")
+        return parent, dist
+
+    def tree_read32(self, parent: np.ndarray | None = None, dist: np.ndarray | None = None):
+        """(parent int32, dist uint32): the tree with 32-bit distances, UNREACHABLE32 where
+        unreachable (8 bytes per vertex over the host link instead of 12)."""
+        if parent is None:
+            parent = np.empty(self.n, np.int32)
+        if dist is None:
+            dist = np.empty(self.n, np.uint32)
+        _check(_lib.dsssp_tree_read32(self._h, parent.ctypes.data, dist.ctypes.data), "tree_read32")
         return parent, dist
 
     def debug_set(self, what: int, value: int) -> None:

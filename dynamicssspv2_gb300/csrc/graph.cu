@@ -354,6 +354,15 @@ __global__ void k_tree_unpack(const unsigned long long* state, int n, int* paren
     }
 }
 
+// The same with 32-bit distances (0xFFFFFFFF = unreachable, which is the state's own top half).
+__global__ void k_tree_unpack32(const unsigned long long* state, int n, int* parent, unsigned* dist) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const unsigned long long s = state[v];
+    if (parent) parent[v] = s == kInfState ? -1 : (int)(unsigned)s;
+    if (dist) dist[v] = (unsigned)(s >> 32);
+}
+
 // Vertices the last batch may have changed: cut off in this epoch, or holding a push tag or
 // far-list generation of the batch's tag range [lo, hi).  CTA-aggregated append.
 __global__ void k_tree_changed(const unsigned long long* state, const unsigned* inv_tag, const unsigned* chg_tag,
@@ -1802,10 +1811,32 @@ int dsssp_tree_read(dsssp_graph* g, int32_t* parent, int64_t* dist) {
         if (!rc) rc = dalloc(&g->d_dist, (size_t)g->n, "tree staging");
         if (rc) return rc;
     }
-    k_tree_unpack<<<blocks_for(g->n), kThreads, 0, s>>>(g->dg.state, g->n, g->d_par, g->d_dist);
+    k_tree_unpack<<<blocks_for(g->n), kThreads, 0, s>>>(g->dg.state, g->n, parent ? g->d_par : nullptr,
+                                                        dist ? g->d_dist : nullptr);
     count_launch(1);
     if (parent) CK(cudaMemcpyAsync(parent, g->d_par, sizeof(int) * (size_t)g->n, cudaMemcpyDeviceToHost, s), "tree read");
     if (dist) CK(cudaMemcpyAsync(dist, g->d_dist, sizeof(long long) * (size_t)g->n, cudaMemcpyDeviceToHost, s), "tree read");
+    CK(cudaStreamSynchronize(s), "tree read");
+    return DSSSP_OK;
+}
+
+int dsssp_tree_read32(dsssp_graph* g, int32_t* parent, uint32_t* dist) {
+    if (!g) return fail(DSSSP_E_INVAL, "tree_read32: NULL graph");
+    int rc = set_device(g);
+    if (rc) return rc;
+    if (g->pending) return fail(DSSSP_E_INVAL, "tree_read32: a batch is still pending");
+    cudaStream_t s = g->stream;
+    if (!g->d_par) {
+        rc = dalloc(&g->d_par, (size_t)g->n, "tree staging");
+        if (!rc) rc = dalloc(&g->d_dist, (size_t)g->n, "tree staging");
+        if (rc) return rc;
+    }
+    unsigned* d_dist32 = reinterpret_cast<unsigned*>(g->d_dist);  // n int64 slots hold n uint32
+    k_tree_unpack32<<<blocks_for(g->n), kThreads, 0, s>>>(g->dg.state, g->n, parent ? g->d_par : nullptr,
+                                                          dist ? d_dist32 : nullptr);
+    count_launch(1);
+    if (parent) CK(cudaMemcpyAsync(parent, g->d_par, sizeof(int) * (size_t)g->n, cudaMemcpyDeviceToHost, s), "tree read");
+    if (dist) CK(cudaMemcpyAsync(dist, d_dist32, sizeof(unsigned) * (size_t)g->n, cudaMemcpyDeviceToHost, s), "tree read");
     CK(cudaStreamSynchronize(s), "tree read");
     return DSSSP_OK;
 }

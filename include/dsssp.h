@@ -211,6 +211,13 @@ int dsssp_forest_load(dsssp_graph* g, const int32_t* parent, const int64_t* dist
  * Replaces printSSSP and the host print of SSSPmainForUndirected.cu:298-312. */
 int dsssp_tree_read(dsssp_graph* g, int32_t* parent, int64_t* dist);
 
+/* Like dsssp_tree_read with 32-bit distances, the width of RT_Vertex.Dist in the reference
+ * (all_structure_undir.cuh:66-75): dist[v] is the exact distance as an unsigned 32-bit integer
+ * (every distance the engine holds fits), DSSSP_UNREACHABLE32 for an unreachable vertex,
+ * whose parent is -1.  8 bytes per vertex cross the host link instead of 12. */
+#define DSSSP_UNREACHABLE32 0xFFFFFFFFu
+int dsssp_tree_read32(dsssp_graph* g, int32_t* parent, uint32_t* dist);
+
 /* Test hooks for failure detection (not for production use).
  * DSSSP_DEBUG_SPIN_LIMIT: polls of about 1 us before a grid barrier of the update kernel
  *   gives up with DSSSP_E_TIMEOUT (0 = the default 2^20, about 1 s).

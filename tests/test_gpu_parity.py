@@ -505,6 +505,31 @@ def test_changed_entries_rebuild_the_tree(opts):
             g.tree_read_changed()
 
 
+def test_tree_read32_matches_tree_read():
+    """dsssp_tree_read32 gives tree_read's parents and its distances as uint32: exact above
+    2^31 (a path of two 2*10^9 edges), 0xFFFFFFFF where unreachable, before and after a batch;
+    either output may be left out."""
+    n, core = 3000, 2900
+    u, v, w = D.gen_er(core, 12000, 1, 100, 61)
+    u = np.concatenate([u, [0, core]]).astype(np.int32)
+    v = np.concatenate([v, [core, core + 1]]).astype(np.int32)
+    w = np.concatenate([w, [2_000_000_000, 2_000_000_000]]).astype(np.int32)
+    with D.Graph(n, u, v, w) as g:
+        g.tree_compute(0)
+        for b in range(2):
+            p64, d64 = g.tree_read()
+            p32, d32 = g.tree_read32()
+            assert d32.dtype == np.uint32 and np.array_equal(p32, p64)
+            unreach = d64 == D.UNREACHABLE
+            assert np.all(unreach[core + 2:]) and np.all(d32[unreach] == D.UNREACHABLE32)
+            assert np.array_equal(d32[~unreach].astype(np.int64), d64[~unreach])
+            assert d64[core + 1] == 4_000_000_000 + d64[0] and d32[core + 1] == 4_000_000_000
+            only_d = np.full(n, 7, np.uint32)
+            D._check(D._lib.dsssp_tree_read32(g.handle, None, only_d.ctypes.data), "tree_read32")
+            assert np.array_equal(only_d, d32)
+            g.apply_batch(D.gen_changes(core, u[:-2], v[:-2], w[:-2], 200, 200, seed=70 + b))
+
+
 def apply_lines_to(n, u, v, w, ch):
     _, kept = O.updated_graph(n, u, v, w, ch, return_kept=True)
     ins = ch[ch["op"] == 1]
