@@ -81,7 +81,7 @@ class Stats(C.Structure):
                      "bytes_alg_update")
     ] + [("advances", C.c_int64), ("tombstoned", C.c_int64), ("graph_launch", C.c_int64),
          ("bytes_engine_update", C.c_double), ("t_delete_ms", C.c_double), ("t_append_ms", C.c_double),
-         ("recovered_from", C.c_int64), ("t_recompute_ms", C.c_double)]
+         ("recovered_from", C.c_int64), ("t_recompute_ms", C.c_double), ("t_seed_ms", C.c_double)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -229,6 +229,23 @@ _sig("dsssp_write_sssp_binary", C.c_int, C.c_char_p, C.c_int32, _i32p, _i64p)
 _sig("dsssp_read_sssp_binary", C.c_int, C.c_char_p, C.c_int32, _i32p, _i64p)
 _sig("dsssp_sssp_noalloc", C.c_int, C.c_int32, C.c_int64, _P, _P, C.c_int32, _P, _P, _P)
 
+_sig("dsssp_abi_sizes", C.c_int, C.POINTER(C.c_size_t), C.c_int32)
+
+
+def abi_sizes() -> list[int]:
+    """sizeof(dsssp_opts, dsssp_stats, dsssp_server_opts, dsssp_request_info,
+    dsssp_tune_result) as the loaded library was built."""
+    out = (C.c_size_t * 8)()
+    k = _lib.dsssp_abi_sizes(out, 8)
+    return [int(out[i]) for i in range(k)]
+
+
+_built = abi_sizes()
+_bound = [C.sizeof(Opts), C.sizeof(Stats), C.sizeof(ServerOpts), C.sizeof(RequestInfo)]
+if _built[:4] != _bound:
+    raise ImportError(f"{LIB_PATH}: built with struct sizes {_built[:4]}, this binding expects {_bound} "
+                      "(rebuild the library: python -c 'import __graft_entry__ as g; g.build()')")
+
 NOALLOC_MAX_VERTICES = 65536
 NOALLOC_MAX_ENTRIES = 1 << 20
 
@@ -252,6 +269,7 @@ EXPORTED = [
     "dsssp_pool_capacity", "dsssp_server_tenant_state", "dsssp_server_add_tenant", "dsssp_server_remove_tenant",
     "dsssp_server_recovered_epochs", "dsssp_server_debug_set", "dsssp_apply_batch_host_async",
     "dsssp_autotune", "dsssp_autotune_lookup", "dsssp_tune_size_class", "dsssp_tune_candidates",
+    "dsssp_abi_sizes",
 ]
 
 

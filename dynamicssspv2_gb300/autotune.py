@@ -21,7 +21,7 @@ from pathlib import Path
 
 import numpy as np
 
-from . import CHANGE_DTYPE, Graph, Opts, _check, _lib
+from . import CHANGE_DTYPE, Graph, Opts, _check, _lib, abi_sizes
 
 TUNED_FIELDS = ("small_deg", "large_deg", "chunk", "bfs_levels", "block", "ctas_per_sm", "delta", "solo_waves",
                 "group_ctas", "group_waves", "warp_agg", "auto_rounds")
@@ -31,6 +31,9 @@ class TuneResult(C.Structure):
     _fields_ = [("key", C.c_char * 32), ("opts", Opts), ("ms", C.c_double), ("trials", C.c_int32),
                 ("cached", C.c_int32)]
 
+
+if abi_sizes()[4] != C.sizeof(TuneResult):
+    raise ImportError(f"the library's dsssp_tune_result is {abi_sizes()[4]} bytes, this binding's {C.sizeof(TuneResult)}")
 
 _lib.dsssp_autotune.restype = C.c_int
 _lib.dsssp_autotune.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_char_p, C.c_int32, C.c_int32,

@@ -1044,7 +1044,10 @@ void fill_stats(const dsssp_graph* g, const Ctl& c, dsssp_stats* st, bool events
     st->repacks = repacks;
     if (c.ts[1] > c.ts[0]) st->t_inval_ms = (double)(c.ts[1] - c.ts[0]) * 1e-6;
     if (c.ts[3] > c.ts[2]) st->t_relax_ms = (double)(c.ts[3] - c.ts[2]) * 1e-6;
-    if (c.ts[2] > c.ts[1] && c.ts[1] > 0) st->t_relax_ms += (double)(c.ts[2] - c.ts[1]) * 1e-6;
+    if (c.ts[2] > c.ts[1] && c.ts[1] > 0) {
+        st->t_seed_ms = (double)(c.ts[2] - c.ts[1]) * 1e-6;
+        st->t_relax_ms += st->t_seed_ms;
+    }
     if (events) {
         float a = 0, b = 0, t = 0;
         if (cudaEventElapsedTime(&a, g->ev[0], g->ev[1]) == cudaSuccess) st->t_step1_ms = a;
@@ -1422,6 +1425,14 @@ int finish_batch(dsssp_graph* g, dsssp_stats* st) {
 // =========================================================================================
 
 extern "C" {
+
+int dsssp_abi_sizes(size_t* out, int32_t cap) {
+    const size_t sz[] = {sizeof(dsssp_opts), sizeof(dsssp_stats), sizeof(dsssp_server_opts), sizeof(dsssp_request_info),
+                         sizeof(dsssp_tune_result)};
+    int32_t k = 0;
+    for (; out && k < cap && k < (int32_t)(sizeof sz / sizeof sz[0]); k++) out[k] = sz[k];
+    return k;
+}
 
 void dsssp_default_opts(dsssp_opts* o) {
     if (!o) return;

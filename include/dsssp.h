@@ -155,11 +155,18 @@ typedef struct {
                                   level 2; with row growth it spans the growth too) */
     int64_t recovered_from;    /* DSSSP_W_RECOMPUTED: the code of the failure recovered from */
     double t_recompute_ms;     /* DSSSP_W_RECOMPUTED: the recomputation of the trees (CUDA events) */
+    double t_seed_ms;          /* the seeding and pull phase alone (part of t_relax_ms) */
 } dsssp_stats;
 
 /* ---- engine ------------------------------------------------------------------------ */
 
 void dsssp_default_opts(dsssp_opts* o);
+
+/* sizeof of the ABI's structs as this library was built: dsssp_opts, dsssp_stats,
+ * dsssp_server_opts, dsssp_request_info, dsssp_tune_result (out[0..4]), so that a binding
+ * (ctypes, cgo, JNI) can refuse to run against a header it was not written for.  Returns
+ * the number of sizes written, at most cap. */
+int dsssp_abi_sizes(size_t* out, int32_t cap);
 
 /* Builds the device-resident graph (CSR rows sorted by neighbour, with per-row slack) from
  * an undirected edge list; each line (u[i], v[i], w[i]) adds both directions.

@@ -391,3 +391,18 @@ def test_noalloc_refuses_bad_pointers_before_any_launch():
         with pytest.raises(D.DsssspError) as e:
             D.sssp_noalloc(100, 10, off, adj, 0, par, dist)
         assert e.value.code == D.E_INVAL
+
+
+def test_abi_struct_sizes_match_the_binding():
+    """dsssp_abi_sizes: the library's struct sizes equal the ctypes layouts (the binding
+    refuses to import otherwise), and the fields appended last sit at the end."""
+    import ctypes as C
+
+    import dynamicssspv2_gb300 as D
+    from dynamicssspv2_gb300.autotune import TuneResult
+
+    assert D.abi_sizes() == [C.sizeof(D.Opts), C.sizeof(D.Stats), C.sizeof(D.ServerOpts), C.sizeof(D.RequestInfo),
+                             C.sizeof(TuneResult)]
+    assert D.Stats.t_seed_ms.offset + 8 == C.sizeof(D.Stats)
+    out = (C.c_size_t * 2)()
+    assert D._lib.dsssp_abi_sizes(out, 2) == 2 and list(out) == D.abi_sizes()[:2]
