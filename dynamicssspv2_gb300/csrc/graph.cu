@@ -616,6 +616,7 @@ struct dsssp_graph {
     int* d_fail = nullptr;
     long long grow_cap = 0;
     unsigned long long s_spare[2] = {0, 0};  // spare words saved with the snapshot
+    long long s_spare_lo = 0;                // and the first slot of its spare region
     DelSlot* d_hset = nullptr;  // deletion set of the batch
     unsigned long long hcap = 0;
     Ctl* h_ctl = nullptr;  // pinned mirror of the control block
@@ -641,6 +642,7 @@ struct dsssp_graph {
     // tree load or computation, a failed batch or a tag reset
     unsigned delta_lo = 0, delta_hi = 0, delta_epoch = 0;
     bool delta_ok = false;
+    bool delta_empty = false;  // the last batch had no records: nothing changed
     unsigned pend_rb0 = 0;
     int* d_vtx = nullptr;
     unsigned* d_count = nullptr;
@@ -1396,6 +1398,7 @@ int finish_batch(dsssp_graph* g, dsssp_stats* st) {
         g->dead += tombs;
     }
     g->delta_ok = g->h_ctl->status == 0 && g->h_ctl->stat[ST_DIST_OVF] == 0;
+    g->delta_empty = false;
     if (g->h_ctl->status == 0) g->last_rounds = (long long)g->h_ctl->stat[ST_ROUNDS];
     g->delta_lo = g->pend_rb0;
     g->delta_hi = g->h_ctl->round_base;
@@ -1880,6 +1883,10 @@ int dsssp_tree_read_changed(dsssp_graph* g, int32_t* vertex, int32_t* parent, in
     if (rc) return rc;
     if (g->pending) return fail(DSSSP_E_INVAL, "tree_read_changed: a batch is still pending");
     if (!g->delta_ok) return fail(DSSSP_E_INVAL, "tree_read_changed: no successful batch since the tree was set");
+    if (g->delta_empty) {
+        *count = 0;
+        return DSSSP_OK;
+    }
     cudaStream_t s = g->stream;
     if (!g->d_par) {
         rc = dalloc(&g->d_par, (size_t)g->n, "tree staging");
@@ -1974,7 +1981,11 @@ int dsssp_apply_batch_async(dsssp_graph* g, const dsssp_change* d_changes, int64
     if (g->pending) return fail(DSSSP_E_INVAL, "apply_batch: previous batch not finished");
     if (!g->has_tree) return fail(DSSSP_E_BAD_TREE, "apply_batch: no tree loaded");
     cudaStream_t s = stream ? (cudaStream_t)stream : g->stream;
-    if (k == 0) return DSSSP_OK;
+    if (k == 0) {  // nothing to do; the changed-entries read of this batch is empty
+        g->delta_ok = true;
+        g->delta_empty = true;
+        return DSSSP_OK;
+    }
     rc = ensure_batch(g, k);
     if (!rc) rc = next_epoch(g, s);
     if (!rc) rc = enqueue_batch(g, (const int4*)d_changes, k, s);
@@ -1999,7 +2010,7 @@ int dsssp_apply_batch_host_async(dsssp_graph* g, const dsssp_change* changes, in
     int rc = set_device(g);
     if (rc) return rc;
     if (g->pending) return fail(DSSSP_E_INVAL, "apply_batch: previous batch not finished");
-    if (k == 0) return DSSSP_OK;
+    if (k == 0) return dsssp_apply_batch_async(g, nullptr, 0, stream);
     rc = ensure_batch(g, k);
     if (rc) return rc;
     cudaStream_t s = stream ? (cudaStream_t)stream : g->stream;
@@ -2077,6 +2088,7 @@ int dsssp_graph_snapshot(dsssp_graph* g) {
     CK(cudaStreamSynchronize(s), "snapshot");
     g->s_entries = g->entries;
     g->s_dead = g->dead;
+    g->s_spare_lo = g->spare_lo;
     g->s_src = g->src;
     g->s_has_tree = g->has_tree;
     g->s_roots = g->roots;
@@ -2112,6 +2124,7 @@ int dsssp_graph_restore(dsssp_graph* g, void* stream) {
     g->entries = g->s_entries;
     g->dead = g->s_dead;
     g->spare_top = (long long)g->s_spare[0];
+    g->spare_lo = g->s_spare_lo;
     g->src = g->s_src;
     g->has_tree = g->s_has_tree;
     g->roots = g->s_roots;

@@ -254,8 +254,10 @@ int dsssp_tree_read_range(dsssp_graph* g, int32_t first, int32_t count, int32_t*
  * distance differs from before the batch), in no particular order.  vertex/parent/dist get
  * *count entries (at most cap; cap = n always suffices).  A caller that keeps the previous
  * tree on the host applies these entries to have the updated tree, at a fraction of the
- * copy volume of dsssp_tree_read.  DSSSP_E_INVAL when there is no successful batch since the
- * tree was loaded or computed, or when the set exceeds cap (then *count is its size). */
+ * copy volume of dsssp_tree_read.  After a batch with no records *count is 0.  DSSSP_E_INVAL
+ * when there is no successful batch since the tree was loaded or computed (a batch that
+ * returned DSSSP_W_RECOMPUTED computed the whole tree again: read it with dsssp_tree_read), or
+ * when the set exceeds cap (then *count is its size). */
 int dsssp_tree_read_changed(dsssp_graph* g, int32_t* vertex, int32_t* parent, int64_t* dist,
                             int64_t cap, int64_t* count);
 

@@ -488,6 +488,8 @@ def test_changed_entries_rebuild_the_tree(opts):
         g.tree_load(parent, dist)
         with pytest.raises(D.DsssspError):  # no batch yet
             g.tree_read_changed()
+        g.apply_batch(np.zeros(0, D.CHANGE_DTYPE))  # an empty batch changes nothing
+        assert len(g.tree_read_changed()[0]) == 0
         host_p, host_d = parent.copy(), dist.copy()
         for b in range(4):
             ch = D.gen_changes(n, u, v, w, 300, 300, seed=500 + b)
