@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 
 import dynamicssspv2_gb300 as D
+from dynamicssspv2_gb300.pool import GraphPool
 from oracle import pyoracle as O
 from tests.common import check_against_oracle, lines_after
 
@@ -214,3 +215,137 @@ def test_random_cases(block):
         res, kind, _ = one_case(seed)
         kinds[kind] = kinds.get(kind, 0) + (res == "ok")
     assert sum(kinds.values()) > 0
+
+
+def pool_case(seed):
+    """A pooled store of one to six random graphs: batches for random subsets of them in one
+    launch sequence, graphs added into the vertex reserve and removed; every graph's tree
+    checked against the oracle after each step, the union certified on the device."""
+    rng = np.random.default_rng(1_000_000 + seed)
+    graphs = [rand_graph(rng, 50 * seed + i)[1:] for i in range(int(rng.integers(1, 7)))]
+    opts = rand_opts(rng)
+    reserve = int(rng.choice([0, 0, 3000, 12000]))
+    try:
+        pool = GraphPool(graphs, reserve_vertices=reserve, **opts)
+    except D.DsssspError as e:
+        if "invalid dsssp_opts" in str(e):
+            return "skip-opts"
+        raise
+    with pool:
+        live = [{"n": n, "u": u, "v": v, "w": w, "src": int(rng.integers(0, n))} for n, u, v, w in graphs]
+        pool.tree_compute([g["src"] for g in live])
+        for step in range(int(rng.integers(1, 5))):
+            where = f"pool seed {seed} step {step} opts {opts}"
+            if reserve and rng.random() < 0.4:
+                _, n, u, v, w = rand_graph(rng, 50 * seed + 40 + step)
+                if n <= pool.capacity()["largest_free"]:
+                    src = int(rng.integers(0, n))
+                    assert pool.add_graph(n, u, v, w, src) == len(live)
+                    live.append({"n": n, "u": u, "v": v, "w": w, "src": src})
+            alive = [i for i, g in enumerate(live) if g is not None]
+            if len(alive) > 1 and rng.random() < 0.2:
+                gone = alive[int(rng.integers(len(alive)))]
+                pool.remove_graph(gone)
+                live[gone] = None
+                alive.remove(gone)
+            pick = [i for i in alive if rng.random() < 0.7]
+            batches = []
+            for i in pick:
+                g = live[i]
+                parent = pool.tree_read(i)[0]
+                batches.append((i, rand_batch(rng, g["n"], g["u"], g["v"], g["w"], parent, 7 * seed + i)))
+            if batches:
+                st = pool.apply(batches)
+                assert st.recovered_from == 0, f"{where}: recovered from {st.recovered_from}"
+            changes = dict(batches)
+            for i in alive:
+                g = live[i]
+                ch = changes.get(i, np.zeros(0, D.CHANGE_DTYPE))
+                p, d = pool.tree_read(i)
+                check_against_oracle(g["n"], g["u"], g["v"], g["w"], ch, g["src"], p, d, f"{where} graph {i}")
+                g["u"], g["v"], g["w"] = lines_after(g["n"], g["u"], g["v"], g["w"], ch)
+            c = pool.graph.validate()
+            assert c["violations"] == 0, f"{where}: certificate {c}"
+    return "ok"
+
+
+def server_case(seed):
+    """A server with one to five random tenants under a random memory budget: requests
+    submitted at once (epochs of several tenants), tenants removed and added between the
+    rounds of requests; every served request's recorded tree checked against the oracle, the
+    refused ones exactly those of tenants not admitted, the trees certified on the device."""
+    from dynamicssspv2_gb300 import serve as S
+
+    rng = np.random.default_rng(2_000_000 + seed)
+    tenants = []
+    for i in range(int(rng.integers(1, 6))):
+        _, n, u, v, w = rand_graph(rng, 60 * seed + i)
+        tenants.append(S.Tenant(f"t{i}", n, u, v, w, int(rng.integers(0, n))))
+    fps = [S.estimate_footprint(t.n, len(t.u)) for t in tenants]
+    budget = None if rng.random() < 0.5 else int(sum(fps) * rng.uniform(0.4, 1.1))
+    opts = rand_opts(rng)
+    opts.pop("timing", None)
+    try:
+        srv = S.Server(tenants, memory_budget=budget, max_epoch_requests=[None, 1, 3][int(rng.integers(3))],
+                       reserve_vertices=int(rng.choice([0, 8000])), **opts)
+    except D.DsssspError as e:
+        if "invalid dsssp_opts" in str(e):
+            return "skip-opts"
+        raise
+    with srv:
+        graphs = [[t.u, t.v, t.w] for t in tenants]
+        for rnd in range(int(rng.integers(1, 4))):
+            where = f"server seed {seed} round {rnd} opts {opts} budget {budget}"
+            admitted = set(srv.admitted)
+            reqs, expect = [], {}
+            for j in range(int(rng.integers(1, 16))):
+                t = int(rng.integers(len(srv.tenants)))
+                ten = srv.tenants[t]
+                if t in admitted:
+                    u, v, w = expect.get(t, graphs[t])
+                    parent = O.dijkstra(ten.n, O.csr(ten.n, u, v, w), ten.src)[1]
+                    ch = rand_batch(rng, ten.n, u, v, w, parent, 9 * seed + 31 * rnd + j)
+                    expect[t] = list(lines_after(ten.n, u, v, w, ch))
+                else:
+                    ch = D.make_changes([0], [0], [1], [1])
+                reqs.append(S.Request(t, arrival=0.0, changes=ch))
+            for r in srv.serve(reqs, record=True, realtime=False):
+                assert r.error is None and not r.recomputed, f"{where}: request {r.rid}: {r.error}"
+                assert r.refused == (r.tenant not in admitted), f"{where}: request {r.rid} refused={r.refused}"
+                if r.refused:
+                    continue
+                ten = srv.tenants[r.tenant]
+                u, v, w = graphs[r.tenant]
+                check_against_oracle(ten.n, u, v, w, r.changes, ten.src, *r.result, f"{where} request {r.rid}")
+                graphs[r.tenant] = list(lines_after(ten.n, u, v, w, r.changes))
+            c = srv.validate()
+            assert c["violations"] == 0, f"{where}: certificate {c}"
+            if len(admitted) > 1 and rng.random() < 0.3:
+                srv.remove_tenant(sorted(admitted)[int(rng.integers(len(admitted)))])
+            if rng.random() < 0.3:
+                _, n, u, v, w = rand_graph(rng, 60 * seed + 50 + rnd)
+                srv.add_tenant(S.Tenant(f"a{rnd}", n, u, v, w, int(rng.integers(0, n))))
+                graphs.append([u, v, w])
+        for t in srv.admitted:
+            ten = srv.tenants[t]
+            p, d = srv.tree(t)
+            u, v, w = graphs[t]
+            check_against_oracle(ten.n, u, v, w, np.zeros(0, D.CHANGE_DTYPE), ten.src, p, d, f"server seed {seed} final {t}")
+    return "ok"
+
+
+POOL_CASES = int(os.environ.get("DSSSP_SOAK_POOL_CASES", "60"))
+
+
+@pytest.mark.parametrize("block", range(3))
+def test_random_pool_cases(block):
+    per = (POOL_CASES + 2) // 3
+    done = [pool_case(s) for s in range(block * per, min(POOL_CASES, (block + 1) * per))]
+    assert "ok" in done
+
+
+@pytest.mark.parametrize("block", range(3))
+def test_random_server_cases(block):
+    per = (POOL_CASES + 2) // 3
+    done = [server_case(s) for s in range(block * per, min(POOL_CASES, (block + 1) * per))]
+    assert "ok" in done
