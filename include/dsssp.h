@@ -371,10 +371,12 @@ int dsssp_tune_candidates(const dsssp_opts* base, const dsssp_change* changes, i
  * before anything is launched) and a malformed CSR (offsets not monotone from 0 to nnz, a
  * column outside 0..n-1 or a negative weight; found on the device, outputs then undefined).
  * The call is blocking: it synchronizes stream and copies the status word to the host before
- * it returns, so the calling thread waits for the whole computation.
+ * it returns, so the calling thread waits for the whole computation, and no call (the first
+ * or any later one) may be made while stream is being captured into a CUDA graph: the
+ * synchronization would invalidate the capture.
  * It calls no cudaMalloc, cudaFree or other allocating routine.  The first call on a device
- * looks up the work space's device address (cudaGetSymbolAddress) and the update kernel's
- * occupancy; make that first call before any stream capture.  All calls on a device share
+ * also looks up the work space's device address (cudaGetSymbolAddress) and the update
+ * kernel's occupancy.  All calls on a device share
  * the one work space (each call re-initialises what it needs), so calls that overlap on the
  * GPU, from any thread or stream, race and must be serialised by the caller. */
 int dsssp_sssp_noalloc(int32_t n, int64_t nnz, const int64_t* d_row_off, const int32_t* d_adj,
