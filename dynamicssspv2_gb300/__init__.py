@@ -115,6 +115,8 @@ _sig("dsssp_tree_add_sources", C.c_int, _P, _i32p, C.c_int32, C.POINTER(Stats))
 _sig("dsssp_graph_clear_range", C.c_int, _P, C.c_int32, C.c_int32)
 _sig("dsssp_tree_read", C.c_int, _P, _P, _P)
 _sig("dsssp_tree_read32", C.c_int, _P, _P, _P)
+_sig("dsssp_tree_read32_async", C.c_int, _P, _P, _P)
+_sig("dsssp_tree_read_wait", C.c_int, _P)
 _sig("dsssp_tree_read_changed", C.c_int, _P, _P, _P, _P, C.c_int64, C.POINTER(C.c_int64))
 _sig("dsssp_tree_validate", C.c_int, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32))
 _sig("dsssp_debug_set", C.c_int, _P, C.c_int32, C.c_int64)
@@ -251,7 +253,7 @@ NOALLOC_MAX_ENTRIES = 1 << 20
 
 EXPORTED = [
     "dsssp_default_opts", "dsssp_graph_create", "dsssp_graph_destroy", "dsssp_graph_info", "dsssp_tree_load",
-    "dsssp_tree_compute", "dsssp_tree_compute_multi", "dsssp_forest_load", "dsssp_tree_read", "dsssp_tree_read32", "dsssp_apply_batch", "dsssp_apply_batch_async", "dsssp_batch_finish",
+    "dsssp_tree_compute", "dsssp_tree_compute_multi", "dsssp_forest_load", "dsssp_tree_read", "dsssp_tree_read32", "dsssp_tree_read32_async", "dsssp_tree_read_wait", "dsssp_apply_batch", "dsssp_apply_batch_async", "dsssp_batch_finish",
     "dsssp_graph_set_opts", "dsssp_graph_get_opts", "dsssp_graph_snapshot", "dsssp_graph_restore", "dsssp_graph_compact", "dsssp_host_alloc", "dsssp_host_free",
     "dsssp_launch_count", "dsssp_last_error", "dsssp_strerror", "dsssp_free", "dsssp_read_graph_file",
     "dsssp_read_changes_file", "dsssp_read_sssp_file", "dsssp_write_sssp_file", "dsssp_gen_er", "dsssp_gen_rmat",
@@ -417,6 +419,15 @@ class Graph:
             dist = np.empty(self.n, np.uint32)
         _check(_lib.dsssp_tree_read32(self._h, parent.ctypes.data, dist.ctypes.data), "tree_read32")
         return parent, dist
+
+    def tree_read32_async(self, parent_ptr: int | None, dist_ptr: int | None) -> None:
+        """Starts copying the tree (int32 parents, uint32 distances) to host buffers of n
+        entries at these addresses (pinned for an asynchronous copy); tree_read_wait() waits
+        for it.  The next batch may be applied meanwhile."""
+        _check(_lib.dsssp_tree_read32_async(self._h, parent_ptr, dist_ptr), "tree_read32_async")
+
+    def tree_read_wait(self) -> None:
+        _check(_lib.dsssp_tree_read_wait(self._h), "tree_read_wait")
 
     def debug_set(self, what: int, value: int) -> None:
         """Failure-detection test hooks (DEBUG_SPIN_LIMIT, DEBUG_STALL_US)."""

@@ -649,6 +649,13 @@ struct dsssp_graph {
     // tree staging
     int* d_par = nullptr;
     long long* d_dist = nullptr;
+    // asynchronous tree reads: their own staging, copied to the host on a copy stream
+    int* a_par = nullptr;
+    unsigned* a_dist = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_unpacked = nullptr;  // the staging holds the tree (later batches may start)
+    cudaEvent_t ev_copied = nullptr;    // the host arrays hold it (the staging is free again)
+    bool copy_pending = false;
     // snapshot
     unsigned long long* s_state = nullptr;
     RowDesc* s_rows = nullptr;
@@ -1500,7 +1507,12 @@ void dsssp_graph_destroy(dsssp_graph* g) {
     if (!g) return;
     cudaSetDevice(g->dev);
     if (g->stream) cudaStreamSynchronize(g->stream);
+    if (g->copy_stream) cudaStreamSynchronize(g->copy_stream);
     DevGraph& d = g->dg;
+    dfree(g->a_par); dfree(g->a_dist);
+    if (g->ev_unpacked) cudaEventDestroy(g->ev_unpacked);
+    if (g->ev_copied) cudaEventDestroy(g->ev_copied);
+    if (g->copy_stream) cudaStreamDestroy(g->copy_stream);
     dfree(d.state); dfree(d.rows); dfree(d.sorted_len); dfree(d.adj); dfree(d.inv_tag);
     dfree(d.push_tag); dfree(d.jm); dfree(d.invq); dfree(d.rt0); dfree(d.rt1); dfree(d.rc0); dfree(d.rc1);
     dfree(d.it); dfree(d.ic); dfree(d.ctl); dfree(d.far0); dfree(d.far1); dfree(d.far_tag); dfree(d.chg_tag);
@@ -1855,6 +1867,49 @@ int dsssp_tree_read32(dsssp_graph* g, int32_t* parent, uint32_t* dist) {
     return DSSSP_OK;
 }
 
+int dsssp_tree_read32_async(dsssp_graph* g, int32_t* parent, uint32_t* dist) {
+    if (!g) return fail(DSSSP_E_INVAL, "tree_read32_async: NULL graph");
+    int rc = set_device(g);
+    if (rc) return rc;
+    if (g->pending) return fail(DSSSP_E_INVAL, "tree_read32_async: a batch is still pending");
+    if (!g->copy_stream) {
+        CK(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking), "copy stream");
+        CK(cudaEventCreateWithFlags(&g->ev_unpacked, cudaEventDisableTiming), "copy events");
+        CK(cudaEventCreateWithFlags(&g->ev_copied, cudaEventDisableTiming), "copy events");
+    }
+    if (!g->a_par) {
+        rc = dalloc(&g->a_par, (size_t)g->n, "tree staging");
+        if (!rc) rc = dalloc(&g->a_dist, (size_t)g->n, "tree staging");
+        if (rc) return rc;
+    }
+    cudaStream_t s = g->stream;
+    if (g->copy_pending) CK(cudaStreamWaitEvent(s, g->ev_copied, 0), "tree read");  // staging in use
+    k_tree_unpack32<<<blocks_for(g->n), kThreads, 0, s>>>(g->dg.state, g->n, parent ? g->a_par : nullptr,
+                                                          dist ? g->a_dist : nullptr);
+    count_launch(1);
+    CK(cudaEventRecord(g->ev_unpacked, s), "tree read");
+    CK(cudaStreamWaitEvent(g->copy_stream, g->ev_unpacked, 0), "tree read");
+    if (parent)
+        CK(cudaMemcpyAsync(parent, g->a_par, sizeof(int) * (size_t)g->n, cudaMemcpyDeviceToHost, g->copy_stream),
+           "tree read");
+    if (dist)
+        CK(cudaMemcpyAsync(dist, g->a_dist, sizeof(unsigned) * (size_t)g->n, cudaMemcpyDeviceToHost, g->copy_stream),
+           "tree read");
+    CK(cudaEventRecord(g->ev_copied, g->copy_stream), "tree read");
+    g->copy_pending = true;
+    return DSSSP_OK;
+}
+
+int dsssp_tree_read_wait(dsssp_graph* g) {
+    if (!g) return fail(DSSSP_E_INVAL, "tree_read_wait: NULL graph");
+    int rc = set_device(g);
+    if (rc) return rc;
+    if (!g->copy_pending) return DSSSP_OK;
+    CK(cudaEventSynchronize(g->ev_copied), "tree read");
+    g->copy_pending = false;
+    return DSSSP_OK;
+}
+
 int dsssp_tree_read_range(dsssp_graph* g, int32_t first, int32_t count, int32_t* parent, int64_t* dist) {
     if (!g || first < 0 || count < 0 || (long long)first + count > g->n || (count > 0 && (!parent || !dist)))
         return fail(DSSSP_E_INVAL, "tree_read_range: bad arguments");
@@ -1987,6 +2042,7 @@ int dsssp_apply_batch_async(dsssp_graph* g, const dsssp_change* d_changes, int64
         return DSSSP_OK;
     }
     rc = ensure_batch(g, k);
+    if (!rc && g->copy_pending) CK(cudaStreamWaitEvent(s, g->ev_unpacked, 0), "apply_batch");  // a read's unpack
     if (!rc) rc = next_epoch(g, s);
     if (!rc) rc = enqueue_batch(g, (const int4*)d_changes, k, s);
     if (rc) return rc;
@@ -2102,6 +2158,7 @@ int dsssp_graph_restore(dsssp_graph* g, void* stream) {
     if (rc) return rc;
     if (g->pending) return fail(DSSSP_E_INVAL, "restore: a batch is still pending");
     cudaStream_t s = stream ? (cudaStream_t)stream : g->stream;
+    if (g->copy_pending) CK(cudaStreamWaitEvent(s, g->ev_unpacked, 0), "restore");  // a read's unpack
     if (g->cap_total != g->s_cap || (g->s_twin && !g->dg.twin)) {
         CK(cudaStreamSynchronize(s), "restore");
         dfree(g->dg.adj);

@@ -225,6 +225,18 @@ int dsssp_tree_read(dsssp_graph* g, int32_t* parent, int64_t* dist);
 #define DSSSP_UNREACHABLE32 0xFFFFFFFFu
 int dsssp_tree_read32(dsssp_graph* g, int32_t* parent, uint32_t* dist);
 
+/* dsssp_tree_read32 without waiting: the tree as it is now is unpacked on the device at once
+ * (into staging of its own) and copied to the host arrays on a copy stream of the graph, and
+ * the call returns.  The next batch may be applied meanwhile (it waits only for the unpack),
+ * so the copy overlaps its upload and kernels; the host arrays hold the tree once
+ * dsssp_tree_read_wait returns (pinned host memory makes the copy asynchronous; with pageable
+ * memory it completes inside the call).  A later asynchronous read reuses the staging after the
+ * previous copy.  Either array may be NULL.  No counterpart in the reference, which prints
+ * the first distances after the update (SSSPmainForUndirected.cu:298-312). */
+int dsssp_tree_read32_async(dsssp_graph* g, int32_t* parent, uint32_t* dist);
+/* Waits for the copies of dsssp_tree_read32_async (returns at once if none is outstanding). */
+int dsssp_tree_read_wait(dsssp_graph* g);
+
 /* Test hooks for failure detection (not for production use).
  * DSSSP_DEBUG_SPIN_LIMIT: polls of about 1 us before a grid barrier of the update kernel
  *   gives up with DSSSP_E_TIMEOUT (0 = the default 2^20, about 1 s).

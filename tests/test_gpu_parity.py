@@ -532,6 +532,45 @@ def test_tree_read32_matches_tree_read():
             g.apply_batch(D.gen_changes(core, u[:-2], v[:-2], w[:-2], 200, 200, seed=70 + b))
 
 
+def test_tree_read32_async_holds_the_tree_of_the_call():
+    """dsssp_tree_read32_async: the pinned host arrays hold the tree as it was at the call,
+    although the next batch (on the graph's stream or on another) ran before the wait; two reads
+    in a row share the staging; either array may be left out."""
+    import ctypes as C
+
+    n, m = 20000, 80000
+    u, v, w = D.gen_er(n, m, 1, 100, 81)
+    bufs = [D._lib.dsssp_host_alloc(4 * n) for _ in range(4)]
+    assert all(bufs)
+    host = [np.ctypeslib.as_array(C.cast(b, C.POINTER(C.c_int32)), (n,)) for b in bufs]
+    import torch
+
+    other = torch.cuda.Stream()  # odd batches run on a stream of their own
+    try:
+        with D.Graph(n, u, v, w) as g:
+            g.tree_compute(0)
+            for b in range(4):
+                want_p, want_d = g.tree_read32()
+                g.tree_read32_async(bufs[2 * (b % 2)], bufs[2 * (b % 2) + 1])
+                ch = D.gen_changes(n, u, v, w, 400, 400, seed=90 + b)
+                g.apply_batch(ch, other.cuda_stream if b % 2 else None)
+                g.tree_read_wait()
+                assert np.array_equal(host[2 * (b % 2)], want_p), f"batch {b}: parents"
+                assert np.array_equal(host[2 * (b % 2) + 1].view(np.uint32), want_d), f"batch {b}: distances"
+                assert not np.array_equal(g.tree_read32()[1], want_d)  # the batch did change the tree
+                u, v, w = (np.asarray(a) for a in apply_lines_to(n, u, v, w, ch))
+            want_p, want_d = g.tree_read32()
+            g.tree_read32_async(bufs[0], bufs[1])
+            g.tree_read32_async(bufs[2], None)
+            g.tree_read_wait()
+            assert np.array_equal(host[0], want_p) and np.array_equal(host[1].view(np.uint32), want_d)
+            assert np.array_equal(host[2], want_p)
+            g.tree_read_wait()  # nothing outstanding
+    finally:
+        for b in bufs:
+            D._lib.dsssp_host_free(b)
+
+
 def apply_lines_to(n, u, v, w, ch):
     _, kept = O.updated_graph(n, u, v, w, ch, return_kept=True)
     ins = ch[ch["op"] == 1]
