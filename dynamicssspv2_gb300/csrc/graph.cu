@@ -197,6 +197,15 @@ struct GrowParams {
     int* fail;
     int slack_min;
     long long cap_total;
+    // compacting growth (with the twin index)
+    int* sorted_len;
+    long long* new_start;             // per grow-list entry: the row's first slot after growth
+    long long* scratch;               // per grow-list entry: scratch of a row compacted in place, -1: moves
+    int* live;                        // per grow-list entry: live entries (tombstones are dropped)
+    int* live_sorted;                 // ... of them in the neighbour-sorted prefix
+    int* ncap;                        // per grow-list entry: capacity after growth
+    unsigned long long* scr_used;     // scratch slots taken from the free end of the spare region
+    unsigned long long* dropped;      // tombstones dropped
 };
 
 __global__ void k_grow_count(GrowParams q) {
@@ -303,6 +312,168 @@ __global__ void k_grow_reset(GrowParams q) {
     const unsigned r = q.grow_list[j];
     q.need[r] = 0;
     q.gidx[r] = 0;
+}
+
+// ---- compacting growth (twin index): a growing row keeps only its live entries, in their
+// order (the sorted prefix stays sorted).  A row whose live entries and overflow fit its own
+// region with room to spare is compacted in place (through scratch slots at the free end of the
+// spare region, so it uses none of that region); the others move to a region of
+// 2 * (live + need) + slack_min slots.  Every moved live entry leaves its final slot in its old
+// twin word (a forwarding pointer), through which the twins and the batch's recorded slots are
+// re-linked.  Warp per growing row unless noted.
+
+__global__ void k_grow_plan(GrowParams q) {
+    const unsigned j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    if (j >= *q.grow_count) return;
+    const unsigned r = q.grow_list[j];
+    const RowDesc rd = q.rows[r];
+    const int sl = q.sorted_len[r];
+    int live = 0, ls = 0;
+    for (int e = (int)lane; e < rd.cap; e += 32) {
+        const bool l = q.adj[rd.start + e].y >= 0;
+        live += l ? 1 : 0;
+        ls += l && e < sl ? 1 : 0;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        live += __shfl_xor_sync(0xFFFFFFFFu, live, o);
+        ls += __shfl_xor_sync(0xFFFFFFFFu, ls, o);
+    }
+    if (lane != 0) return;
+    const long long need = q.need[r];
+    const long long room = live / 8 > 1 ? live / 8 : 1;  // free slots left after an in-place compaction
+    q.live[j] = live;
+    q.live_sorted[j] = ls;
+    atomicAdd(q.dropped, (unsigned long long)(rd.cap - live));
+    if (live + need + room <= rd.cap) {
+        const unsigned long long at = atomicAdd(q.scr_used, (unsigned long long)live);
+        q.new_start[j] = rd.start;
+        q.scratch[j] = (long long)(q.spare[1] - at - (unsigned long long)live);  // checked on the host
+        q.ncap[j] = rd.cap;
+    } else {
+        const long long nc = 2 * (live + need) + q.slack_min;
+        const unsigned long long pos = atomicAdd(&q.spare[0], (unsigned long long)nc);
+        if (pos + (unsigned long long)nc > q.spare[1] || nc > 0x7FFFFFFFLL) atomicExch(q.fail, 1);
+        q.new_start[j] = (long long)pos;
+        q.scratch[j] = -1;
+        q.ncap[j] = (int)(nc > 0x7FFFFFFFLL ? 0x7FFFFFFFLL : nc);
+    }
+    q.old_start[j] = rd.start;
+    q.old_cap[j] = rd.cap;
+}
+
+__global__ void k_grow_out(GrowParams q) {
+    const unsigned j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    if (j >= *q.grow_count) return;
+    const long long os = q.old_start[j], fin = q.new_start[j];
+    const long long dst = q.scratch[j] >= 0 ? q.scratch[j] : fin;
+    const int cap = q.old_cap[j];
+    int idx = 0;
+    for (int b = 0; b < cap; b += 32) {
+        const int e = b + (int)lane;
+        const int2 x = e < cap ? q.adj[os + e] : make_int2(0, -1);
+        const bool l = x.y >= 0;
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, l);
+        const int at = idx + __popc(m & ((1u << lane) - 1u));
+        if (l) {
+            q.adj[dst + at] = x;
+            q.twin[dst + at] = q.twin[os + e];  // the partner's old slot, re-linked below
+            q.twin[os + e] = (unsigned)(fin + at);
+        }
+        idx += __popc(m);
+    }
+}
+
+// Each compacted entry takes its partner's final slot: from the partner's forwarding pointer
+// when the partner's row grows too, else the partner stays and gets this entry's final slot.
+__global__ void k_grow_relink(GrowParams q) {
+    const unsigned j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    if (j >= *q.grow_count) return;
+    const long long fin = q.new_start[j];
+    const long long at0 = q.scratch[j] >= 0 ? q.scratch[j] : fin;
+    const int live = q.live[j];
+    for (int e = (int)lane; e < live; e += 32) {
+        const unsigned t = q.twin[at0 + e];
+        if (t == kNoTwin) continue;
+        const int c = q.adj[at0 + e].x;  // the partner lives in row c
+        if ((long long)t >= q.cap_total) {  // internal error: report, skip the access
+            atomicExch(q.fail, 2);
+            continue;
+        }
+        unsigned t2 = t;
+        if (q.gidx[c]) t2 = q.twin[t];
+        else q.twin[t] = (unsigned)(fin + e);
+        if ((long long)t2 >= q.cap_total) {
+            atomicExch(q.fail, 2);
+            continue;
+        }
+        q.twin[at0 + e] = t2;
+    }
+}
+
+// Thread per record: the recorded slot of an inserted end that fitted into a growing row.
+__global__ void k_grow_translate(GrowParams q) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= q.k) return;
+    const int4 c = q.chg[i];
+    if (c.w != 1 || q.ins_state[i] != 1) return;
+#pragma unroll
+    for (int side = 0; side < 2; side++) {
+        const long long at = q.slot[2 * i + side];
+        const int r = side ? c.y : c.x;
+        if (at >= 0 && q.gidx[r]) q.slot[2 * i + side] = (long long)q.twin[at];
+    }
+}
+
+__global__ void k_grow_back(GrowParams q) {
+    const unsigned j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    if (j >= *q.grow_count) return;
+    const long long fin = q.new_start[j], scr = q.scratch[j];
+    const int live = q.live[j];
+    if (scr >= 0)
+        for (int e = (int)lane; e < live; e += 32) {
+            q.adj[fin + e] = q.adj[scr + e];
+            q.twin[fin + e] = q.twin[scr + e];
+        }
+    if (lane == 0) {
+        const unsigned r = q.grow_list[j];
+        RowDesc nr;
+        nr.start = fin;
+        nr.deg = live;
+        nr.cap = q.ncap[j];
+        q.rows[r] = nr;
+        q.sorted_len[r] = q.live_sorted[j];
+    }
+}
+
+// Thread per record: the overflowed ends go after the live entries of their grown rows, and
+// every surviving insertion's two ends are paired.
+__global__ void k_grow_place2(GrowParams q) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= q.k) return;
+    const int4 c = q.chg[i];
+    if (c.w != 1 || q.ins_state[i] != 1) return;
+    long long at[2] = {q.slot[2 * i], q.slot[2 * i + 1]};
+    if (at[0] >= 0 && at[1] >= 0) return;  // paired by the batch (and re-linked if moved)
+#pragma unroll
+    for (int side = 0; side < 2; side++) {
+        if (at[side] >= 0) continue;
+        const int r = side ? c.y : c.x, col = side ? c.x : c.y;
+        const int pos = atomicAdd(&q.rows[r].deg, 1);
+        if (pos >= q.rows[r].cap) {  // cannot happen: growth sized the row for its overflow
+            atomicExch(q.fail, 3);
+            return;
+        }
+        at[side] = q.rows[r].start + pos;
+        q.adj[at[side]] = make_int2(col, c.z);
+        q.slot[2 * i + side] = at[side];
+    }
+    q.twin[at[0]] = (unsigned)at[1];
+    q.twin[at[1]] = (unsigned)at[0];
 }
 
 __global__ void k_int_to_ll(const int* a, int n, long long* b) {
@@ -613,6 +784,13 @@ struct dsssp_graph {
     unsigned* d_grow_count = nullptr;
     long long* d_old_start = nullptr;
     int* d_old_cap = nullptr;
+    long long* d_gnew = nullptr;            // per grow-list entry: first slot after growth
+    long long* d_gscr = nullptr;            // per grow-list entry: scratch of an in-place compaction
+    int* d_glive = nullptr;                 // per grow-list entry: live entries, of them sorted, capacity
+    int* d_gsorted = nullptr;
+    int* d_gncap = nullptr;
+    unsigned long long* d_gwords = nullptr; // scratch slots used, tombstones dropped
+    long long grow_dropped = 0;             // tombstones the last row growth dropped
     int* d_fail = nullptr;
     long long grow_cap = 0;
     unsigned long long s_spare[2] = {0, 0};  // spare words saved with the snapshot
@@ -766,6 +944,7 @@ int ensure_batch(dsssp_graph* g, long long k) {
     dfree(g->d_grow_list);
     dfree(g->d_old_start);
     dfree(g->d_old_cap);
+    dfree(g->d_gnew); dfree(g->d_gscr); dfree(g->d_glive); dfree(g->d_gsorted); dfree(g->d_gncap);
     g->grow_cap = 0;
     g->chg_cap = 0;
     g->hcap = 0;
@@ -779,6 +958,12 @@ int ensure_batch(dsssp_graph* g, long long k) {
     if (!rc) rc = dalloc(&g->d_seedq, (size_t)gl, "seed list");
     if (!rc) rc = dalloc(&g->d_old_start, (size_t)gl, "grow list");
     if (!rc) rc = dalloc(&g->d_old_cap, (size_t)gl, "grow list");
+    if (!rc) rc = dalloc(&g->d_gnew, (size_t)gl, "grow list");
+    if (!rc) rc = dalloc(&g->d_gscr, (size_t)gl, "grow list");
+    if (!rc) rc = dalloc(&g->d_glive, (size_t)gl, "grow list");
+    if (!rc) rc = dalloc(&g->d_gsorted, (size_t)gl, "grow list");
+    if (!rc) rc = dalloc(&g->d_gncap, (size_t)gl, "grow list");
+    if (!rc && !g->d_gwords) rc = dalloc(&g->d_gwords, 2, "grow list");
     if (!rc) g->grow_cap = gl;
     if (!rc) {
         g->chg_cap = cap;
@@ -1109,6 +1294,42 @@ constexpr int kSpareExhausted = 1;
 // Moves every row that overflowed in this batch into the spare region and places its
 // overflowed entries; kSpareExhausted if the region is too small (nothing lost: the caller
 // repacks, which folds the overflow list in).
+// Row growth with the twin index: rows compacted in place or moved, tombstones dropped (the
+// kernels above).  kSpareExhausted when the moves and the scratch do not both fit the spare
+// region (nothing has been written then: the caller repacks).
+int grow_rows_compacting(dsssp_graph* g, const GrowParams& q, int novf, long long rows_max, unsigned wb,
+                         cudaStream_t s) {
+    CK(cudaMemsetAsync(g->d_gwords, 0, 2 * sizeof(unsigned long long), s), "row growth");
+    k_grow_count<<<blocks_for(novf), kThreads, 0, s>>>(q);
+    k_grow_plan<<<wb, kThreads, 0, s>>>(q);
+    count_launch(2);
+    int fail = 0;
+    unsigned long long sp[2] = {0, 0}, words[2] = {0, 0};
+    CK(cudaMemcpyAsync(&fail, g->d_fail, sizeof(int), cudaMemcpyDeviceToHost, s), "row growth");
+    CK(cudaMemcpyAsync(sp, g->d_spare, sizeof(sp), cudaMemcpyDeviceToHost, s), "row growth");
+    CK(cudaMemcpyAsync(words, g->d_gwords, sizeof(words), cudaMemcpyDeviceToHost, s), "row growth");
+    CK(cudaStreamSynchronize(s), "row growth");
+    if (fail || sp[0] + words[0] > sp[1]) {
+        k_grow_reset<<<blocks_for(rows_max), kThreads, 0, s>>>(q);
+        count_launch(1);
+        CK(cudaStreamSynchronize(s), "row growth");
+        return kSpareExhausted;
+    }
+    k_grow_out<<<wb, kThreads, 0, s>>>(q);
+    k_grow_relink<<<wb, kThreads, 0, s>>>(q);
+    k_grow_translate<<<blocks_for(g->pend_k), kThreads, 0, s>>>(q);
+    k_grow_back<<<wb, kThreads, 0, s>>>(q);
+    k_grow_place2<<<blocks_for(g->pend_k), kThreads, 0, s>>>(q);
+    k_grow_reset<<<blocks_for(rows_max), kThreads, 0, s>>>(q);
+    count_launch(6);
+    CK(cudaMemcpyAsync(&fail, g->d_fail, sizeof(int), cudaMemcpyDeviceToHost, s), "row growth");
+    CK(cudaStreamSynchronize(s), "row growth");
+    if (fail) return dsssp::fail(DSSSP_E_CUDA, "row growth: internal error %d", fail);
+    g->spare_top = (long long)sp[0];
+    g->grow_dropped = (long long)words[1];
+    return DSSSP_OK;
+}
+
 int grow_rows(dsssp_graph* g, int novf, cudaStream_t s) {
     if (novf <= 0) return DSSSP_OK;
     if (!g->d_need) {
@@ -1138,10 +1359,20 @@ int grow_rows(dsssp_graph* g, int novf, cudaStream_t s) {
     q.fail = g->d_fail;
     q.slack_min = g->o.slack_min > 4 ? g->o.slack_min : 4;
     q.cap_total = g->cap_total;
+    q.sorted_len = g->dg.sorted_len;
+    q.new_start = g->d_gnew;
+    q.scratch = g->d_gscr;
+    q.live = g->d_glive;
+    q.live_sorted = g->d_gsorted;
+    q.ncap = g->d_gncap;
+    q.scr_used = g->d_gwords;
+    q.dropped = g->d_gwords + 1;
+    g->grow_dropped = 0;
     CK(cudaMemsetAsync(g->d_grow_count, 0, sizeof(unsigned), s), "row growth");
     CK(cudaMemsetAsync(g->d_fail, 0, sizeof(int), s), "row growth");
     const long long rows_max = novf < g->grow_cap ? novf : g->grow_cap;
     const unsigned wb = (unsigned)((rows_max * 32 + kThreads - 1) / kThreads);
+    if (g->dg.twin) return grow_rows_compacting(g, q, novf, rows_max, wb, s);
     k_grow_count<<<blocks_for(novf), kThreads, 0, s>>>(q);
     k_grow_move<<<wb, kThreads, 0, s>>>(q);
     count_launch(2);
@@ -1402,8 +1633,9 @@ int finish_batch(dsssp_graph* g, dsssp_stats* st) {
     if (!repacks) {  // a repack counts the live entries itself
         const long long tombs = (long long)g->h_ctl->stat[ST_TOMBS];
         g->entries += 2 * (long long)g->h_ctl->stat[ST_LIVE_INS] - tombs;
-        g->dead += tombs;
+        g->dead += tombs - g->grow_dropped;  // row growth drops the tombstones of the rows it compacts
     }
+    g->grow_dropped = 0;
     g->delta_ok = g->h_ctl->status == 0 && g->h_ctl->stat[ST_DIST_OVF] == 0;
     g->delta_empty = false;
     if (g->h_ctl->status == 0) g->last_rounds = (long long)g->h_ctl->stat[ST_ROUNDS];
@@ -1520,6 +1752,7 @@ void dsssp_graph_destroy(dsssp_graph* g) {
     dfree(g->d_par); dfree(g->d_dist); dfree(g->d_vtx); dfree(g->d_count); dfree(g->d_srcs); dfree(g->d_slot); dfree(g->d_seedq); dfree(g->d_spare);
     dfree(g->d_need); dfree(g->d_gidx); dfree(g->d_grow_list); dfree(g->d_grow_count); dfree(g->d_old_start);
     dfree(g->d_old_cap); dfree(g->d_fail);
+    dfree(g->d_gnew); dfree(g->d_gscr); dfree(g->d_glive); dfree(g->d_gsorted); dfree(g->d_gncap); dfree(g->d_gwords);
     dfree(g->s_state); dfree(g->s_rows); dfree(g->s_sorted); dfree(g->s_adj);
     if (g->bexec) cudaGraphExecDestroy(g->bexec);
     if (g->bgraph) cudaGraphDestroy(g->bgraph);

@@ -940,20 +940,42 @@ __device__ __forceinline__ unsigned tombstone_at(const UpdParams& p, long long j
     return with_twin ? 2u : 1u;
 }
 
-// Tombstones every live entry (col, w) of row r; with the twin index also their reverse
-// entries.  Returns the number of entries examined; `dead` counts the entries tombstoned.
-__device__ unsigned long long tombstone_row(const UpdParams& p, const RowDesc& rd, int sorted_len, int col, int w,
-                                            bool with_twin, unsigned long long& dead) {
+// Tombstones every live entry (col, w) in the neighbour-sorted prefix of a row (binary search)
+// and returns the row's unsorted tail [tlo, thi): the entries appended since the row was laid
+// out, which the caller scans.  With the twin index the reverse entries are tombstoned too.
+// Returns the number of entries examined; `dead` counts the entries tombstoned.
+__device__ unsigned long long tombstone_prefix(const UpdParams& p, const RowDesc& rd, int sorted_len, int col, int w,
+                                               bool with_twin, unsigned long long& dead, long long& tlo,
+                                               long long& thi) {
     const int2* adj = p.g.adj;
-    const long long sl = rd.start + sorted_len, end = rd.start + rd.deg;
+    const long long sl = rd.start + sorted_len;
     long long j = lower_col(adj, rd.start, sl, col);
     unsigned long long probed = 1;
     for (; j < sl && adj[j].x == col; j++, probed++)
         if (adj[j].y == w) dead += tombstone_at(p, j, w, with_twin);
-    for (j = sl; j < end; j++, probed++)
-        if (adj[j].x == col && adj[j].y == w) dead += tombstone_at(p, j, w, with_twin);
+    tlo = sl;
+    thi = rd.start + rd.deg;
     return probed;
 }
+
+__device__ unsigned long long tombstone_tail(const UpdParams& p, long long lo, long long hi, int col, int w,
+                                             bool with_twin, unsigned long long& dead) {
+    for (long long j = lo; j < hi; j++)
+        if (p.g.adj[j].x == col && p.g.adj[j].y == w) dead += tombstone_at(p, j, w, with_twin);
+    return (unsigned long long)(hi > lo ? hi - lo : 0);
+}
+
+__device__ unsigned long long tombstone_row(const UpdParams& p, const RowDesc& rd, int sorted_len, int col, int w,
+                                            bool with_twin, unsigned long long& dead) {
+    long long lo, hi;
+    const unsigned long long probed = tombstone_prefix(p, rd, sorted_len, col, w, with_twin, dead, lo, hi);
+    return probed + tombstone_tail(p, lo, hi, col, w, with_twin, dead);
+}
+
+// Unsorted tails longer than this are scanned by the whole warp, 32 consecutive entries per
+// step, instead of by the deletion's own lane: under sustained insertion and deletion the tails
+// of hub rows grow to thousands of entries until the row moves or the adjacency is repacked.
+constexpr long long kCoopTail = 64;
 
 }  // namespace
 
@@ -993,6 +1015,8 @@ __global__ void k_delete(UpdParams p) {
         const int4 c = i < p.k ? p.chg[i] : make_int4(0, 0, 0, -1);
         bool cut = false;
         unsigned cutv = 0;
+        long long tlo = 0, thi = 0;  // the unsorted tail of the searched row (twin index)
+        int tcol = 0;
         if (c.w == 0) {
             const unsigned a = (unsigned)c.x, b = (unsigned)c.y;
             // gpuFunctions_undir.cuh:189-198: the child end is checked as b first, then as a.
@@ -1007,17 +1031,33 @@ __global__ void k_delete(UpdParams p) {
                 cut = atomicExch(&p.g.inv_tag[cutv], p.epoch) != p.epoch;
                 if (cut) p.g.state[cutv] = kInfState;
             }
-            const RowDesc ra = p.g.rows[a], rb = p.g.rows[b];
-            if (p.g.twin) {
-                // search the shorter row; each match's reverse entry is found through twin[]
-                const bool use_a = ra.deg <= rb.deg;
-                probed += tombstone_row(p, use_a ? ra : rb, p.g.sorted_len[use_a ? a : b], (int)(use_a ? b : a), c.z,
-                                        true, dead);
-            } else {
-                probed += tombstone_row(p, ra, p.g.sorted_len[a], (int)b, c.z, false, dead);
-                probed += tombstone_row(p, rb, p.g.sorted_len[b], (int)a, c.z, false, dead);
+            if (c.z >= 0) {  // a negative weight matches no live entry (tombstones hold -1)
+                const RowDesc ra = p.g.rows[a], rb = p.g.rows[b];
+                if (p.g.twin) {
+                    // search the shorter row; each match's reverse entry is found through twin[]
+                    const bool use_a = ra.deg <= rb.deg;
+                    tcol = (int)(use_a ? b : a);
+                    probed += tombstone_prefix(p, use_a ? ra : rb, p.g.sorted_len[use_a ? a : b], tcol, c.z, true,
+                                               dead, tlo, thi);
+                } else {
+                    probed += tombstone_row(p, ra, p.g.sorted_len[a], (int)b, c.z, false, dead);
+                    probed += tombstone_row(p, rb, p.g.sorted_len[b], (int)a, c.z, false, dead);
+                }
+                if (!hash_insert(p, dpair_key(a, b), c.z)) set_status(ctl, -4 /* deletion set full */);
             }
-            if (c.z >= 0 && !hash_insert(p, dpair_key(a, b), c.z)) set_status(ctl, -4 /* deletion set full */);
+        }
+        // the unsorted tail: a short one by the lane itself, each long one by the whole warp
+        const bool coop = thi - tlo > kCoopTail;
+        if (!coop) probed += tombstone_tail(p, tlo, thi, tcol, c.z, true, dead);
+        for (unsigned pend = __ballot_sync(kFull, coop); pend; pend &= pend - 1) {
+            const int src = __ffs(pend) - 1;
+            const long long lo = __shfl_sync(kFull, tlo, src), hi = __shfl_sync(kFull, thi, src);
+            const int col = __shfl_sync(kFull, tcol, src), w = __shfl_sync(kFull, c.z, src);
+            for (long long j = lo + lane; j < hi; j += 32) {
+                const int2 e = p.g.adj[j];
+                if (e.x == col && e.y == w) dead += tombstone_at(p, j, w, true);
+            }
+            if (lane == 0) probed += (unsigned long long)(hi - lo);
         }
         roots_list.add(cut, cutv);
         roots += cut ? 1 : 0;

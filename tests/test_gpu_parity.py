@@ -571,6 +571,35 @@ def test_tree_read32_async_holds_the_tree_of_the_call():
             D._lib.dsssp_host_free(b)
 
 
+@pytest.mark.parametrize("slack", [{"slack_pct": 0, "slack_min": 1, "spare_pct": 40}, {"slack_pct": 10, "slack_min": 2}])
+def test_churn_compacts_growing_rows(slack):
+    """A batch and its inverse, again and again, with little slack: rows fill with tombstones
+    and overflow; growth keeps only their live entries (in place when they fit): the live count
+    stays exact, the tombstones of grown rows are gone, and every tree is exact."""
+    n, m = 4000, 16000
+    u, v, w = D.gen_er(n, m, 1, 60, 91)
+    ch = D.gen_changes(n, u, v, w, 1500, 1500, seed=92)
+    inv = ch.copy()
+    inv["op"] = 1 - ch["op"]
+    with D.Graph(n, u, v, w, **slack) as g:
+        g.tree_compute(0)
+        tombstoned, grown, repacks = 0, 0, 0
+        for i in range(12):
+            b = ch if i % 2 == 0 else inv
+            st = g.apply_batch(b)
+            tombstoned += st.tombstoned
+            grown += st.overflow_entries
+            repacks += st.repacks
+            p, d = g.tree_read()
+            check_against_oracle(n, u, v, w, b, 0, p, d, f"churn step {i}")
+            u, v, w = (np.asarray(a) for a in apply_lines_to(n, u, v, w, b))
+            h = g.health()
+            assert h["live"] == 2 * len(u), f"step {i}: {h}"
+            assert g.validate()["violations"] == 0
+        assert grown > 0
+        assert g.health()["dead"] < tombstoned  # growth dropped the tombstones of the rows it compacted
+
+
 def apply_lines_to(n, u, v, w, ch):
     _, kept = O.updated_graph(n, u, v, w, ch, return_kept=True)
     ins = ch[ch["op"] == 1]
