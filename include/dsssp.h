@@ -230,8 +230,9 @@ int dsssp_tree_read32(dsssp_graph* g, int32_t* parent, uint32_t* dist);
  * the call returns.  The next batch may be applied meanwhile (it waits only for the unpack),
  * so the copy overlaps its upload and kernels; the host arrays hold the tree once
  * dsssp_tree_read_wait returns (pinned host memory makes the copy asynchronous; with pageable
- * memory it completes inside the call).  A later asynchronous read reuses the staging after the
- * previous copy.  Either array may be NULL.  No counterpart in the reference, which prints
+ * memory it completes inside the call).  A read unpacks only after the previous read's copy has
+ * finished, so once a batch applied after read i + 1 has completed, read i's arrays are
+ * filled.  Either array may be NULL.  No counterpart in the reference, which prints
  * the first distances after the update (SSSPmainForUndirected.cu:298-312). */
 int dsssp_tree_read32_async(dsssp_graph* g, int32_t* parent, uint32_t* dist);
 /* Waits for the copies of dsssp_tree_read32_async (returns at once if none is outstanding). */
