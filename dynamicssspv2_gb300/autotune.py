@@ -75,7 +75,7 @@ def _opts_dict(o: Opts) -> dict:
 
 
 class Autotuner:
-    def __init__(self, cache_path: str | os.PathLike | None = None, reps: int = 2):
+    def __init__(self, cache_path: str | os.PathLike | None = None, reps: int = 3):
         self.path = Path(cache_path) if cache_path else default_cache_path()
         self.reps = reps
 

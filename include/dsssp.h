@@ -337,14 +337,16 @@ void dsssp_free(void* p);
 typedef struct {
     char key[32];      /* size class "v<log2 n>_e<log2 entries>_b<log2 k>" */
     dsssp_opts opts;   /* the chosen options (also set on the graph) */
-    double ms;         /* their device time on the batch (best of reps) */
+    double ms;         /* their device time on the batch (median of reps) */
     int32_t trials;    /* candidates timed; 0 when taken from the cache */
     int32_t cached;    /* 1 = taken from the cache without timing */
 } dsssp_tune_result;
 
 /* Tunes g for batches like changes[0..k): a cached size class is applied without timing
- * (unless force); otherwise every candidate runs the batch reps times (0 = 2) and the fastest
- * is set and written to cache_path (NULL: not cached).  Replaces the graph's snapshot and leaves
+ * (unless force); otherwise every candidate runs the batch once per round for reps rounds
+ * (0 = 3), and the candidate with the least median time is set and written to cache_path
+ * (NULL: not cached) -- the graph's own setting (the first candidate) unless another is at
+ * least 3 % faster.  Replaces the graph's snapshot and leaves
  * the graph and tree as they were before the call. */
 int dsssp_autotune(dsssp_graph* g, const dsssp_change* changes, int64_t k, const char* cache_path,
                    int32_t reps, int32_t force, dsssp_tune_result* out);

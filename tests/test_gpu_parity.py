@@ -535,7 +535,8 @@ def test_tree_read32_matches_tree_read():
 def test_tree_read32_async_holds_the_tree_of_the_call():
     """dsssp_tree_read32_async: the pinned host arrays hold the tree as it was at the call,
     although the next batch (on the graph's stream or on another) ran before the wait; two reads
-    in a row share the staging; either array may be left out."""
+    in a row share the staging; either array may be left out; without waits, read i's arrays
+    are filled once the batch after read i + 1 has completed."""
     import ctypes as C
 
     n, m = 20000, 80000
@@ -566,6 +567,28 @@ def test_tree_read32_async_holds_the_tree_of_the_call():
             assert np.array_equal(host[0], want_p) and np.array_equal(host[1].view(np.uint32), want_d)
             assert np.array_equal(host[2], want_p)
             g.tree_read_wait()  # nothing outstanding
+            # no waits: once the batch that follows read i + 1 has completed, read i's arrays hold
+            # its tree (three pairs of buffers, as for a stream of batches)
+            ring = [D._lib.dsssp_host_alloc(4 * n) for _ in range(6)]
+            assert all(ring)
+            views = [np.ctypeslib.as_array(C.cast(b, C.POINTER(C.c_int32)), (n,)) for b in ring]
+            try:
+                want = {}
+                for i in range(6):
+                    want[i] = g.tree_read32()
+                    g.tree_read32_async(ring[2 * (i % 3)], ring[2 * (i % 3) + 1])
+                    ch = D.gen_changes(n, u, v, w, 300, 300, seed=190 + i)
+                    g.apply_batch(ch)
+                    u, v, w = (np.asarray(a) for a in apply_lines_to(n, u, v, w, ch))
+                    if i >= 1:
+                        j = i - 1
+                        assert np.array_equal(views[2 * (j % 3)], want[j][0]), f"read {j}: parents"
+                        assert np.array_equal(views[2 * (j % 3) + 1].view(np.uint32), want[j][1]), f"read {j}"
+                g.tree_read_wait()
+                assert np.array_equal(views[2 * (5 % 3) + 1].view(np.uint32), want[5][1])
+            finally:
+                for b in ring:
+                    D._lib.dsssp_host_free(b)
     finally:
         for b in bufs:
             D._lib.dsssp_host_free(b)
