@@ -935,7 +935,8 @@ __device__ __forceinline__ void tombstone_twin(const UpdParams& p, long long j) 
 // Tombstones one matching entry; the compare-and-swap makes the count exact when a batch
 // deletes one line twice.  Returns the entries tombstoned (2 with the twin).
 __device__ __forceinline__ unsigned tombstone_at(const UpdParams& p, long long j, int w, bool with_twin) {
-    if (atomicCAS(&p.g.adj[j].y, w, -1) != w) return 0;
+    // a negative weight matches no live entry (tombstones hold -1)
+    if (w < 0 || atomicCAS(&p.g.adj[j].y, w, -1) != w) return 0;
     if (with_twin) tombstone_twin(p, j);
     return with_twin ? 2u : 1u;
 }
@@ -965,17 +966,33 @@ __device__ unsigned long long tombstone_tail(const UpdParams& p, long long lo, l
     return (unsigned long long)(hi > lo ? hi - lo : 0);
 }
 
+// The whole row: the sorted prefix by binary search, the tail by this thread.
 __device__ unsigned long long tombstone_row(const UpdParams& p, const RowDesc& rd, int sorted_len, int col, int w,
                                             bool with_twin, unsigned long long& dead) {
-    long long lo, hi;
-    const unsigned long long probed = tombstone_prefix(p, rd, sorted_len, col, w, with_twin, dead, lo, hi);
-    return probed + tombstone_tail(p, lo, hi, col, w, with_twin, dead);
+    const int2* adj = p.g.adj;
+    const long long sl = rd.start + sorted_len, end = rd.start + rd.deg;
+    long long j = lower_col(adj, rd.start, sl, col);
+    unsigned long long probed = 1;
+    for (; j < sl && adj[j].x == col; j++, probed++)
+        if (adj[j].y == w) dead += tombstone_at(p, j, w, with_twin);
+    for (j = sl; j < end; j++, probed++)
+        if (adj[j].x == col && adj[j].y == w) dead += tombstone_at(p, j, w, with_twin);
+    return probed;
 }
 
 // Unsorted tails longer than this are scanned by the whole warp, 32 consecutive entries per
 // step, instead of by the deletion's own lane: under sustained insertion and deletion the tails
-// of hub rows grow to thousands of entries until the row moves or the adjacency is repacked.
+// of hub rows grow to thousands of entries until the row is compacted or the adjacency is
+// repacked.  The deletion's lane lists such a tail in its warp's staging; the warp scans the
+// listed tails after its records (a lane whose warp's list is full scans its tail itself).
 constexpr long long kCoopTail = 64;
+constexpr int kTailList = 32;
+struct LongTail {
+    long long lo, hi;
+    int col, w;
+};
+__shared__ LongTail s_tails[kMaxWarps][kTailList];
+__shared__ unsigned s_ntails[kMaxWarps];
 
 }  // namespace
 
@@ -1008,15 +1025,15 @@ __global__ void k_delete(UpdParams p) {
     if (__ldcg(&ctl->status) != 0) return;  // set by k_prepare: same for every thread
     const long long nthreads = (long long)gridDim.x * blockDim.x;
     unsigned long long probed = 0, roots = 0, dead = 0;
-    const unsigned lane = lane_id();
-    WarpList roots_list{s_wlist[threadIdx.x >> 5], kListRegion, 0};
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    if (lane == 0) s_ntails[warp] = 0;
+    __syncwarp();
+    WarpList roots_list{s_wlist[warp], kListRegion, 0};
     for (long long base = (long long)blockIdx.x * blockDim.x + threadIdx.x - lane; base < p.k; base += nthreads) {
         const long long i = base + lane;
         const int4 c = i < p.k ? p.chg[i] : make_int4(0, 0, 0, -1);
         bool cut = false;
         unsigned cutv = 0;
-        long long tlo = 0, thi = 0;  // the unsorted tail of the searched row (twin index)
-        int tcol = 0;
         if (c.w == 0) {
             const unsigned a = (unsigned)c.x, b = (unsigned)c.y;
             // gpuFunctions_undir.cuh:189-198: the child end is checked as b first, then as a.
@@ -1031,37 +1048,42 @@ __global__ void k_delete(UpdParams p) {
                 cut = atomicExch(&p.g.inv_tag[cutv], p.epoch) != p.epoch;
                 if (cut) p.g.state[cutv] = kInfState;
             }
-            if (c.z >= 0) {  // a negative weight matches no live entry (tombstones hold -1)
-                const RowDesc ra = p.g.rows[a], rb = p.g.rows[b];
-                if (p.g.twin) {
-                    // search the shorter row; each match's reverse entry is found through twin[]
-                    const bool use_a = ra.deg <= rb.deg;
-                    tcol = (int)(use_a ? b : a);
-                    probed += tombstone_prefix(p, use_a ? ra : rb, p.g.sorted_len[use_a ? a : b], tcol, c.z, true,
-                                               dead, tlo, thi);
-                } else {
-                    probed += tombstone_row(p, ra, p.g.sorted_len[a], (int)b, c.z, false, dead);
-                    probed += tombstone_row(p, rb, p.g.sorted_len[b], (int)a, c.z, false, dead);
+            const RowDesc ra = p.g.rows[a], rb = p.g.rows[b];
+            if (p.g.twin) {
+                // search the shorter row; each match's reverse entry is found through twin[]
+                const bool use_a = ra.deg <= rb.deg;
+                const RowDesc& rs = use_a ? ra : rb;
+                const int sl = p.g.sorted_len[use_a ? a : b];
+                const int col = (int)(use_a ? b : a);
+                if (rs.deg - sl <= kCoopTail) {  // a short unsorted tail: this lane scans it too
+                    probed += tombstone_row(p, rs, sl, col, c.z, true, dead);
+                } else {  // a long one goes to the warp's list (or, when that is full, to this lane)
+                    long long tlo, thi;
+                    probed += tombstone_prefix(p, rs, sl, col, c.z, true, dead, tlo, thi);
+                    const unsigned at = atomicAdd(&s_ntails[warp], 1u);
+                    if (at < (unsigned)kTailList) s_tails[warp][at] = LongTail{tlo, thi, col, c.z};
+                    else probed += tombstone_tail(p, tlo, thi, col, c.z, true, dead);
                 }
-                if (!hash_insert(p, dpair_key(a, b), c.z)) set_status(ctl, -4 /* deletion set full */);
+            } else {
+                probed += tombstone_row(p, ra, p.g.sorted_len[a], (int)b, c.z, false, dead);
+                probed += tombstone_row(p, rb, p.g.sorted_len[b], (int)a, c.z, false, dead);
             }
-        }
-        // the unsorted tail: a short one by the lane itself, each long one by the whole warp
-        const bool coop = thi - tlo > kCoopTail;
-        if (!coop) probed += tombstone_tail(p, tlo, thi, tcol, c.z, true, dead);
-        for (unsigned pend = __ballot_sync(kFull, coop); pend; pend &= pend - 1) {
-            const int src = __ffs(pend) - 1;
-            const long long lo = __shfl_sync(kFull, tlo, src), hi = __shfl_sync(kFull, thi, src);
-            const int col = __shfl_sync(kFull, tcol, src), w = __shfl_sync(kFull, c.z, src);
-            for (long long j = lo + lane; j < hi; j += 32) {
-                const int2 e = p.g.adj[j];
-                if (e.x == col && e.y == w) dead += tombstone_at(p, j, w, true);
-            }
-            if (lane == 0) probed += (unsigned long long)(hi - lo);
+            if (c.z >= 0 && !hash_insert(p, dpair_key(a, b), c.z)) set_status(ctl, -4 /* deletion set full */);
         }
         roots_list.add(cut, cutv);
         roots += cut ? 1 : 0;
         roots_list.flush(p.g.invq, &ctl->inv_count, (unsigned)p.g.n, 32, ctl);
+    }
+    // the listed long tails, each by the whole warp (32 consecutive entries per step)
+    __syncwarp();
+    const unsigned nt = min(s_ntails[warp], (unsigned)kTailList);
+    for (unsigned t = 0; t < nt; t++) {
+        const LongTail lt = s_tails[warp][t];
+        for (long long j = lt.lo + lane; j < lt.hi; j += 32) {
+            const int2 e = p.g.adj[j];
+            if (e.x == lt.col && e.y == lt.w) dead += tombstone_at(p, j, lt.w, true);
+        }
+        if (lane == 0) probed += (unsigned long long)(lt.hi - lt.lo);
     }
     roots_list.flush_cta(p.g.invq, &ctl->inv_count, (unsigned)p.g.n, ctl);
     block_add(&ctl->stat[ST_ROOTS], roots);
