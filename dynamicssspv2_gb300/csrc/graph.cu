@@ -175,7 +175,7 @@ __global__ void k_pack_ovf(const int4* ovf, int novf, const long long* poff, int
     keys[poff[o.x] + atomicAdd(&cursor[o.x], 1)] = make_key(o.y, o.z);
 }
 
-// ---- in-place row growth (rows that ran out of slack move to the spare region) ----------
+// ---- row growth: rows that ran out of slack are compacted in place or move to the spare region ----
 
 struct GrowParams {
     RowDesc* rows;
@@ -219,8 +219,9 @@ __global__ void k_grow_count(GrowParams q) {
     }
 }
 
-// Warp per growing row: a region of 2 * (cap + need) + slack_min slots from the spare
-// region, the row's cap stored entries (and their twin words) copied there.
+// Without the twin index (slot counts above 32 bits): warp per growing row, a region of
+// 2 * (cap + need) + slack_min slots from the spare region, the row's cap stored entries
+// (tombstones included) copied there.
 __global__ void k_grow_move(GrowParams q) {
     const unsigned j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned lane = threadIdx.x & 31;
@@ -1612,8 +1613,9 @@ int finish_batch(dsssp_graph* g, dsssp_stats* st) {
     int repacks = 0;
     if (g->h_ctl->status == kStatusOverflowPending) {
         // deletions are applied and the insertions that fit are placed.  The rows that ran
-        // out of slack move to the spare region with room to grow; only when that region is
-        // used up is the whole adjacency repacked.  Then the update kernel runs.
+        // out of slack drop their tombstones and are compacted in place or move to the spare
+        // region with room to grow; only when that region is used up is the whole adjacency
+        // repacked.  Then the update kernel runs.
         int rc = grow_rows(g, g->h_ctl->ovf_count, s);
         if (rc == kSpareExhausted) {
             rc = repack(g, g->d_ovf, g->h_ctl->ovf_count, s);

@@ -77,7 +77,8 @@ typedef struct {
                              which costs a batch a few microseconds */
     int64_t max_rounds;   /* relaxation round cap; 0 = 2n + 16 */
     int32_t spare_pct;    /* extra adjacency slots, percent of the laid-out rows, into which a
-                             row that runs out of slack moves (no full repack); 0..400 */
+                             row that runs out of slack moves (no full repack) unless dropping
+                             its tombstones leaves it room in place; 0..400 */
     int32_t delta;        /* near-far bucket width of the relaxation rounds: 0 = plain frontier
                              rounds; > 0 = a round relaxes only vertices whose distance is below
                              a threshold T, the others wait until the near frontier is empty and
