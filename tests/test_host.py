@@ -406,3 +406,20 @@ def test_abi_struct_sizes_match_the_binding():
     assert D.Stats.t_seed_ms.offset + 8 == C.sizeof(D.Stats)
     out = (C.c_size_t * 2)()
     assert D._lib.dsssp_abi_sizes(out, 2) == 2 and list(out) == D.abi_sizes()[:2]
+
+
+def test_tree_reads_refuse_a_null_graph_on_the_host():
+    """The tree reads and the asynchronous read's wait refuse a NULL graph with DSSSP_E_INVAL
+    before touching a device; dsssp_abi_sizes writes at most cap sizes."""
+    import ctypes as C
+
+    import dynamicssspv2_gb300 as D
+
+    buf = (C.c_int32 * 4)()
+    assert D._lib.dsssp_tree_read32(None, buf, buf) == D.E_INVAL
+    assert D._lib.dsssp_tree_read32_async(None, buf, buf) == D.E_INVAL
+    assert D._lib.dsssp_tree_read_wait(None) == D.E_INVAL
+    assert D._lib.dsssp_tree_read(None, buf, buf) == D.E_INVAL
+    sizes = (C.c_size_t * 1)()
+    assert D._lib.dsssp_abi_sizes(sizes, 1) == 1 and sizes[0] == C.sizeof(D.Opts)
+    assert D._lib.dsssp_abi_sizes(None, 5) == 0
