@@ -190,6 +190,7 @@ struct UpdParams {
     unsigned group_ctas;  // mid-size steps run on CTAs [0, group_ctas) with a group barrier (0 = off)
     unsigned group_waves; // ... a step is mid-size up to group_ctas * group_waves CTA-waves of items
     int warp_agg;         // 1 = warp-aggregated distance offers (one atomicMin per target and warp)
+    int tails;            // 1 = rows may hold unsorted tails (k_delete scans long ones warp-wide)
 };
 
 // ---- memory-order helpers -------------------------------------------------------------

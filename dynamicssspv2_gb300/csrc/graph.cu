@@ -29,6 +29,7 @@ cudaError_t update_occupancy(int block, int* blocks_per_sm);
 cudaError_t launch_update(const UpdParams& p, int grid, int block, cudaStream_t s);
 void batch_kernels(const void* fns[4]);
 const void* update_kernel(bool warp_agg);
+const void* delete_kernel(bool tails);
 
 static std::atomic<long long> g_launches{0};
 void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
@@ -809,6 +810,10 @@ struct dsssp_graph {
     cudaGraphNode_t bn_hash = nullptr, bn_kern[4] = {nullptr, nullptr, nullptr, nullptr};
     int bgraph_timing = 0;  // the timing level the instantiated graph records
     int bgraph_agg = 0;     // the update kernel it launches (opts.warp_agg)
+    int bgraph_tails = 0;   // the deletion kernel it launches (tails)
+    // rows may hold unsorted tails: set by a batch that appends, cleared by a fresh layout
+    bool tails = false;
+    bool s_tails = false;   // ... as of the snapshot
     bool bgraph_failed = false;
     // pending batch
     bool pending = false;
@@ -1000,6 +1005,7 @@ int row_offsets(dsssp_graph* g, const int* d_deg, long long** deg64, long long**
 // slack-layout adjacency; replaces g's adjacency, rows and sorted prefix lengths.
 int layout_rows(dsssp_graph* g, unsigned long long* keys_in, long long total, const long long* deg64,
                 const long long* poff, cudaStream_t s) {
+    g->tails = false;  // every row is sorted: no tails until a batch appends
     const int n = g->n;
     long long *cap = nullptr, *start = nullptr;
     unsigned long long* keys_out = nullptr;
@@ -1173,6 +1179,7 @@ UpdParams make_params(const dsssp_graph* g, const int4* chg, long long k, int mo
     p.group_ctas = (unsigned)g->o.group_ctas;
     p.group_waves = (unsigned)g->o.group_waves;
     p.warp_agg = g->o.warp_agg;
+    p.tails = g->tails ? 1 : 0;
     return p;
 }
 
@@ -1410,6 +1417,7 @@ struct BatchNodes {
 void batch_nodes(const dsssp_graph* g, const UpdParams& p, unsigned long long h, BatchNodes& b) {
     const void* fns[4];
     batch_kernels(fns);
+    fns[1] = delete_kernel(p.tails != 0);
     fns[3] = update_kernel(p.warp_agg != 0);
     b.p = p;
     b.args[0] = &b.p;
@@ -1499,6 +1507,7 @@ cudaError_t build_batch_graph(dsssp_graph* g, const BatchNodes& b, int timing) {
     }
     g->bgraph_timing = timing;
     g->bgraph_agg = b.p.warp_agg;
+    g->bgraph_tails = b.p.tails;
     return e;
 }
 
@@ -1509,7 +1518,7 @@ bool launch_batch_graph(dsssp_graph* g, const UpdParams& p, unsigned long long h
     batch_nodes(g, p, h, b);
     const int timing = g->o.timing;
     cudaError_t e = cudaSuccess;
-    if (!g->bexec || g->bgraph_timing != timing || g->bgraph_agg != p.warp_agg) {
+    if (!g->bexec || g->bgraph_timing != timing || g->bgraph_agg != p.warp_agg || g->bgraph_tails != p.tails) {
         e = build_batch_graph(g, b, timing);
     } else {
         e = cudaGraphExecMemsetNodeSetParams(g->bexec, g->bn_hash, &b.hash);
@@ -1636,6 +1645,7 @@ int finish_batch(dsssp_graph* g, dsssp_stats* st) {
         const long long tombs = (long long)g->h_ctl->stat[ST_TOMBS];
         g->entries += 2 * (long long)g->h_ctl->stat[ST_LIVE_INS] - tombs;
         g->dead += tombs - g->grow_dropped;  // row growth drops the tombstones of the rows it compacts
+        if (g->h_ctl->stat[ST_LIVE_INS] > 0) g->tails = true;  // insertions appended to row tails
     }
     g->grow_dropped = 0;
     g->delta_ok = g->h_ctl->status == 0 && g->h_ctl->stat[ST_DIST_OVF] == 0;
@@ -2379,6 +2389,7 @@ int dsssp_graph_snapshot(dsssp_graph* g) {
     CK(cudaStreamSynchronize(s), "snapshot");
     g->s_entries = g->entries;
     g->s_dead = g->dead;
+    g->s_tails = g->tails;
     g->s_spare_lo = g->spare_lo;
     g->s_src = g->src;
     g->s_has_tree = g->has_tree;
@@ -2417,6 +2428,7 @@ int dsssp_graph_restore(dsssp_graph* g, void* stream) {
     g->dead = g->s_dead;
     g->spare_top = (long long)g->s_spare[0];
     g->spare_lo = g->s_spare_lo;
+    g->tails = g->s_tails;
     g->src = g->s_src;
     g->has_tree = g->s_has_tree;
     g->roots = g->s_roots;

@@ -1020,14 +1020,21 @@ __global__ void k_prepare(UpdParams p) {
 
 // Deletions: cut off the child end of a deleted tree edge, tombstone every matching entry,
 // record the deletion in the batch's deletion set.
+// kTails: rows may hold unsorted tails (entries appended since the last layout), and long ones
+// are scanned warp-wide; without, every tail is scanned by its deletion's lane (the host picks
+// this form after a layout, a repack or a compaction, until a batch appends again: the long-tail
+// path alone costs the kernel a few percent).
+template <bool kTails>
 __global__ void k_delete(UpdParams p) {
     Ctl* ctl = p.g.ctl;
     if (__ldcg(&ctl->status) != 0) return;  // set by k_prepare: same for every thread
     const long long nthreads = (long long)gridDim.x * blockDim.x;
     unsigned long long probed = 0, roots = 0, dead = 0;
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
-    if (lane == 0) s_ntails[warp] = 0;
-    __syncwarp();
+    if constexpr (kTails) {
+        if (lane == 0) s_ntails[warp] = 0;
+        __syncwarp();
+    }
     WarpList roots_list{s_wlist[warp], kListRegion, 0};
     for (long long base = (long long)blockIdx.x * blockDim.x + threadIdx.x - lane; base < p.k; base += nthreads) {
         const long long i = base + lane;
@@ -1055,7 +1062,7 @@ __global__ void k_delete(UpdParams p) {
                 const RowDesc& rs = use_a ? ra : rb;
                 const int sl = p.g.sorted_len[use_a ? a : b];
                 const int col = (int)(use_a ? b : a);
-                if (rs.deg - sl <= kCoopTail) {  // a short unsorted tail: this lane scans it too
+                if (!kTails || rs.deg - sl <= kCoopTail) {  // a short unsorted tail: this lane scans it too
                     probed += tombstone_row(p, rs, sl, col, c.z, true, dead);
                 } else {  // a long one goes to the warp's list (or, when that is full, to this lane)
                     long long tlo, thi;
@@ -1074,16 +1081,17 @@ __global__ void k_delete(UpdParams p) {
         roots += cut ? 1 : 0;
         roots_list.flush(p.g.invq, &ctl->inv_count, (unsigned)p.g.n, 32, ctl);
     }
-    // the listed long tails, each by the whole warp (32 consecutive entries per step)
-    __syncwarp();
-    const unsigned nt = min(s_ntails[warp], (unsigned)kTailList);
-    for (unsigned t = 0; t < nt; t++) {
-        const LongTail lt = s_tails[warp][t];
-        for (long long j = lt.lo + lane; j < lt.hi; j += 32) {
-            const int2 e = p.g.adj[j];
-            if (e.x == lt.col && e.y == lt.w) dead += tombstone_at(p, j, lt.w, true);
+    if constexpr (kTails) {  // the listed long tails, each by the whole warp (32 entries per step)
+        __syncwarp();
+        const unsigned nt = min(s_ntails[warp], (unsigned)kTailList);
+        for (unsigned t = 0; t < nt; t++) {
+            const LongTail lt = s_tails[warp][t];
+            for (long long j = lt.lo + lane; j < lt.hi; j += 32) {
+                const int2 e = p.g.adj[j];
+                if (e.x == lt.col && e.y == lt.w) dead += tombstone_at(p, j, lt.w, true);
+            }
+            if (lane == 0) probed += (unsigned long long)(lt.hi - lt.lo);
         }
-        if (lane == 0) probed += (unsigned long long)(lt.hi - lt.lo);
     }
     roots_list.flush_cta(p.g.invq, &ctl->inv_count, (unsigned)p.g.n, ctl);
     block_add(&ctl->stat[ST_ROOTS], roots);
@@ -1619,7 +1627,8 @@ cudaError_t launch_front(const UpdParams& p, int grid, cudaStream_t s, cudaEvent
     const unsigned g = (unsigned)(need < grid ? need : grid);
     k_prepare<<<g, 256, 0, s>>>(p);
     if (after_prepare) cudaEventRecord(after_prepare, s);
-    k_delete<<<g, 256, 0, s>>>(p);
+    if (p.tails) k_delete<true><<<g, 256, 0, s>>>(p);
+    else k_delete<false><<<g, 256, 0, s>>>(p);
     if (after_delete) cudaEventRecord(after_delete, s);
     k_append<<<g, 256, 0, s>>>(p);
     count_launch(3);
@@ -1629,9 +1638,13 @@ cudaError_t launch_front(const UpdParams& p, int grid, cudaStream_t s, cudaEvent
 // The batch kernels as graph-node functions: k_prepare, k_delete, k_append, k_update.
 void batch_kernels(const void* fns[4]) {
     fns[0] = (const void*)k_prepare;
-    fns[1] = (const void*)k_delete;
+    fns[1] = (const void*)k_delete<true>;
     fns[2] = (const void*)k_append;
     fns[3] = (const void*)k_update<false>;
+}
+
+const void* delete_kernel(bool tails) {
+    return tails ? (const void*)k_delete<true> : (const void*)k_delete<false>;
 }
 
 const void* update_kernel(bool warp_agg) {
