@@ -10,7 +10,8 @@ other cases are seeded random graphs with the edge cases the engine must handle:
 edges, parallel edges, deletions of absent edges, insert+delete of the same edge in one batch,
 disconnected vertices; and shaped ones: a cut-off subtree deeper than the walk's level limit,
 a hub losing many edges, a source losing all of its edges, a batch of ignored records only,
-repeated records.  The updated-graph file given to op_ssspSeq is built here in plain
+repeated records, a grid with cuts and shortcuts, skewed endpoints (hubs), a cut-off subtree
+reattached by an insertion of the same batch, weights of 0 and 1 only.  The updated-graph file given to op_ssspSeq is built here in plain
 Python from the batch semantics (insertions appended, then every line matching a deletion's
 endpoint pair and weight removed), independently of oracle/oracle.c.
 
@@ -146,6 +147,49 @@ def shaped_cases(rng: np.random.Generator):
     return cases
 
 
+def more_cases(rng: np.random.Generator):
+    """A grid with cut edges and diagonal shortcuts (a high-diameter tree), a graph whose
+    endpoints follow a skewed law (hubs) with hub-heavy changes, a cut-off subtree that an
+    insertion of the same batch reattaches by a cheaper edge, and weights of 0 and 1 only with
+    deletions of tree edges (zero-weight ties)."""
+    cases = []
+    side = 15  # 15 x 15 grid, id = r * 15 + c, weights 1..9
+    n = side * side
+    edges = [(r * side + c, r * side + c + 1, int(rng.integers(1, 10))) for r in range(side) for c in range(side - 1)]
+    edges += [(r * side + c, (r + 1) * side + c, int(rng.integers(1, 10))) for r in range(side - 1) for c in range(side)]
+    pick = rng.choice(len(edges), 20, replace=False)
+    changes = [(edges[int(i)][0], edges[int(i)][1], edges[int(i)][2], 0) for i in pick]
+    changes.append((0, 1, edges[0][2], 0))  # one of the source's two edges
+    for _ in range(10):
+        r, c = int(rng.integers(0, side - 1)), int(rng.integers(0, side - 1))
+        changes.append((r * side + c, (r + 1) * side + c + 1, int(rng.integers(1, 12)), 1))
+    cases.append(("grid_cuts", n, edges, [changes[i] for i in rng.permutation(len(changes))]))
+    n = 512  # skewed endpoints: low ids are hubs
+    def skewed():
+        return int(n * rng.random() ** 3)
+    edges = []
+    while len(edges) < 2000:
+        a, b = skewed(), skewed()
+        if a != b:
+            edges.append((a, b, int(rng.integers(1, 51))))
+    changes = [(*edges[int(i)], 0) for i in rng.choice(len(edges), 100, replace=False)]
+    while len(changes) < 200:
+        a, b = skewed(), skewed()
+        if a != b:
+            changes.append((a, b, int(rng.integers(1, 51)), 1))
+    cases.append(("skewed_hubs", n, edges, [changes[i] for i in rng.permutation(len(changes))]))
+    n = 60  # path 0-...-59 (weights 5) with one long chord; cut at 10-11, reattached by 5-30 (w 1)
+    edges = [(i, i + 1, 5) for i in range(n - 1)] + [(0, 45, 400)]
+    changes = [(10, 11, 5, 0), (5, 30, 1, 1), (40, 41, 5, 0)]
+    cases.append(("insert_reattaches", n, edges, changes))
+    n = 40  # weights 0 and 1: equal-distance ties everywhere
+    edges = [(int(a), int(b), int(rng.integers(0, 2))) for a, b in rng.integers(0, n, (140, 2)) if a != b]
+    changes = [(a, b, w, 0) for (a, b, w) in edges[:25]]
+    changes += [(int(a), int(b), int(rng.integers(0, 2)), 1) for a, b in rng.integers(0, n, (12, 2)) if a != b]
+    cases.append(("weights_0_1", n, edges, [changes[i] for i in rng.permutation(len(changes))]))
+    return cases
+
+
 def make_case(tmp: Path, name: str, n: int, edges, changes, sssp_rows=None):
     g = tmp / f"{name}_graph.txt"
     s = tmp / f"{name}_SSSP.txt"
@@ -198,6 +242,8 @@ def main() -> int:
             edges, changes = random_case(rng, n, m, wmax, ni, nd, extras)
             cases.append(make_case(tmp, name, n, edges, changes))
         for name, n, edges, changes in shaped_cases(np.random.default_rng(20261204)):
+            cases.append(make_case(tmp, name, n, edges, changes))
+        for name, n, edges, changes in more_cases(np.random.default_rng(20261205)):
             cases.append(make_case(tmp, name, n, edges, changes))
     out = HERE / "golden.json"
     out.write_text(json.dumps({"generator": "tests/golden/make_golden.py", "cases": cases}, separators=(",", ":")))

@@ -38,7 +38,7 @@ def test_reference_update_disagrees_with_recompute_only_on_mid():
     """The reference's CUDA update equals a recompute of the updated graph on every golden case
     but `mid`, where it seeds relaxation from an insertion that the same batch deletes again
     (gpuFunctions_undir.cuh:217-251 runs after the tombstoning of 201-213).  The GPU parity
-    tests compare the engine with the reference update on the other twelve."""
+    tests compare the engine with the reference update on all the others."""
     differ = []
     for c in CASES:
         ref = np.array(c["ref_update"]["dist"])
