@@ -44,8 +44,11 @@ int slurp(const char* path, FileBuf& fb) {
 
 inline bool is_space(char c) { return c == ' ' || c == '\t' || c == '\r' || c == '\v' || c == '\f'; }
 
-// Parses one integer token; returns false at end of line.  *flt is set when the token is in
-// floating-point form ("1.2e+06"); its value is then rounded to the nearest integer.
+// Parses one integer field; returns false at end of line or when the next token is not a
+// number.  Without flt it reads like the reference's sscanf("%d"): the integer prefix of the
+// token ("2.5" gives 2, and ".5" then counts as a field that is not a number).  With flt (the
+// distance column of an SSSP file, which the reference's Dijkstra writes through cout, e.g.
+// "1.2e+06") a token in floating-point form is read whole and rounded, and *flt is set.
 inline bool next_int(const char*& p, const char* end, long long& out, bool* flt) {
     while (p < end && is_space(*p)) p++;
     if (p >= end || *p == '\n') return false;
@@ -60,7 +63,7 @@ inline bool next_int(const char*& p, const char* end, long long& out, bool* flt)
         p++;
         any = true;
     }
-    if (p < end && (*p == '.' || *p == 'e' || *p == 'E')) {
+    if (flt && p < end && (*p == '.' || *p == 'e' || *p == 'E')) {
         char* q = nullptr;
         double d = strtod(s, &q);
         p = q;

@@ -423,3 +423,47 @@ def test_tree_reads_refuse_a_null_graph_on_the_host():
     sizes = (C.c_size_t * 1)()
     assert D._lib.dsssp_abi_sizes(sizes, 1) == 1 and sizes[0] == C.sizeof(D.Opts)
     assert D._lib.dsssp_abi_sizes(None, 5) == 0
+
+
+def test_graph_and_change_readers_follow_the_reference_sscanf(tmp_path):
+    """The graph and change readers take each field like the reference's sscanf("%d ...")
+    (all_structure_undir.cuh:89-126, 178-198): whitespace of any kind between fields, a sign,
+    the integer prefix of a token ("2.5" is 2), anything after the last field ignored; a line
+    with fewer fields is skipped.  Files of several MB are parsed in parallel chunks, in order."""
+    rng = np.random.default_rng(5)
+    n = 1000
+    seps = [" ", "  ", "\t", " \t "]
+    ends = ["\n", "\r\n", " \n"]
+    for nf, reader in ((3, D.read_graph), (4, D.read_changes)):
+        lines, want = [], []
+        for _ in range(220000):
+            kind = int(rng.integers(0, 8))
+            vals = [int(rng.integers(0, n)), int(rng.integers(0, n)), int(rng.integers(0, 100)), int(rng.integers(0, 2))][:nf]
+            s = [seps[int(rng.integers(4))] for _ in range(nf)]
+            end = ends[int(rng.integers(3))]
+            body = "".join(f"{s[i - 1] if i else ''}{x}" for i, x in enumerate(vals))
+            if kind == 0:  # one field short: skipped
+                line = "".join(f"{s[i - 1] if i else ''}{x}" for i, x in enumerate(vals[:-1])) + end
+            elif kind == 1:  # decimals in the last field: its integer prefix
+                line = body + f".{int(rng.integers(0, 10))}" + end
+                want.append(tuple(vals))
+            elif kind == 2:  # junk and more numbers after the last field: ignored
+                line = body + "abc 7 8" + end
+                want.append(tuple(vals))
+            elif kind == 3:  # a decimal in the second field: its remainder is not a number, skipped
+                line = f"{vals[0]}{s[1]}{vals[1]}.5" + "".join(f"{s[i]}{vals[i]}" for i in range(2, nf)) + end
+            elif kind == 4:  # blank
+                line = end
+            elif kind == 5:  # explicit sign
+                line = "+" + body + end
+                want.append(tuple(vals))
+            else:  # leading whitespace
+                line = s[0] + body + end
+                want.append(tuple(vals))
+            lines.append(line)
+        f = tmp_path / f"fields{nf}.txt"
+        f.write_text("".join(lines))
+        assert f.stat().st_size > 2 << 20  # several parallel chunks
+        got = reader(str(f), n)
+        rows = list(zip(*got[:3])) if nf == 3 else [tuple(r) for r in got.tolist()]
+        assert rows == want
